@@ -1,0 +1,252 @@
+"""Generates the golden fixtures in tests/golden/ by running theboss itself.
+
+Run in a container where the reference package is importable:
+
+    python tests/golden/make_golden.py /root/reference
+
+theboss's Glynn-Gray calculator imports ``guancodes`` (an un-vendored third-party
+dependency pinned ``~=0.0.3`` in the reference's requirements.txt).  It is not
+installable offline, so this script installs a test-only stand-in module that
+yields the binary-reflected Gray code flip sequence (step t flips bit ctz(t)).
+Only Glynn's summation order depends on it; its value does not.
+
+Every fixture stores its input matrices, so nothing downstream needs scipy's
+random generators or the reference package.
+"""
+import json
+import os
+import sys
+import types
+
+import numpy as np
+
+
+def _install_gray_shim():
+    mod = types.ModuleType("guancodes")
+    sub = types.ModuleType("guancodes.GrayCode")
+
+    def get_gray_code_update_indices(n):
+        return [((t & -t).bit_length() - 1) for t in range(1, 1 << n)]
+
+    sub.get_gray_code_update_indices = get_gray_code_update_indices
+    mod.GrayCode = sub
+    sys.modules["guancodes"] = mod
+    sys.modules["guancodes.GrayCode"] = sub
+
+
+def _c(z):
+    z = complex(z)
+    return [z.real, z.imag]
+
+
+def _m(U):
+    U = np.asarray(U, dtype=np.complex128)
+    return {"re": U.real.tolist(), "im": U.imag.tolist()}
+
+
+def main(ref_root):
+    sys.path.insert(0, ref_root)
+    sys.dont_write_bytecode = True
+    _install_gray_shim()
+    from scipy.stats import unitary_group
+
+    from theboss.boson_sampling_utilities.permanent_calculators.ryser_permanent_calculator import (
+        RyserPermanentCalculator,
+    )
+    from theboss.boson_sampling_utilities.permanent_calculators.chin_huh_permanent_calculator import (
+        ChinHuhPermanentCalculator,
+    )
+    from theboss.boson_sampling_utilities.permanent_calculators.glynn_gray_permanent_calculator import (
+        GlynnGrayPermanentCalculator,
+    )
+    from theboss.boson_sampling_utilities.permanent_calculators.classic_permanent_calculator import (
+        ClassicPermanentCalculator,
+    )
+    from theboss.boson_sampling_utilities.permanent_calculators.bs_cc_ryser_submatrices_permanent_calculator import (
+        BSCCRyserSubmatricesPermanentCalculator,
+    )
+    from theboss.boson_sampling_utilities.permanent_calculators.bs_cc_ch_submatrices_permanent_calculator import (
+        BSCCCHSubmatricesPermanentCalculator,
+    )
+    from theboss.boson_sampling_utilities.permanent_calculators.bs_permanent_calculator_base import (
+        BSGuanCodeBasedPermanentCalculatorBase,
+    )
+    from theboss.simulation_strategies.generalized_cliffords_b_simulation_strategy import (
+        GeneralizedCliffordsBSimulationStrategy,
+    )
+    from theboss.simulation_strategies.generalized_cliffords_b_uniform_losses_simulation_strategy import (
+        GeneralizedCliffordsBUniformLossesSimulationStrategy,
+    )
+    from theboss.simulation_strategies.lossy_networks_generalized_cliffords_simulation_strategy import (
+        LossyNetworksGeneralizedCliffordsSimulationStrategy,
+    )
+    from theboss.simulation_strategies.generalized_cliffords_simulation_strategy import (
+        GeneralizedCliffordsSimulationStrategy,
+    )
+    from theboss.distribution_calculators.bs_exact_distribution_with_uniform_losses import (
+        BSDistributionCalculatorWithUniformLosses,
+        BosonSamplingExperimentConfiguration,
+    )
+
+    out_dir = os.path.dirname(os.path.abspath(__file__))
+    rng = np.random.default_rng(20261203)
+
+    # ---- single permanents ------------------------------------------------
+    patterns4 = [  # tests/test_bs_permanent_calculators.py:88-122
+        ([1, 1, 1, 1], [1, 1, 1, 1]),
+        ([1, 1, 1, 0], [1, 0, 1, 1]),
+        ([2, 1, 0, 0], [0, 1, 1, 1]),
+        ([1, 1, 1, 0], [2, 1, 0, 0]),
+        ([2, 1, 1, 0], [1, 1, 0, 2]),
+        ([0, 0, 4, 0], [1, 1, 0, 2]),
+        ([1, 1, 0, 2], [0, 1, 3, 0]),
+        ([0, 2, 0, 2], [0, 0, 4, 0]),
+        ([0, 0, 0, 0], [0, 0, 0, 0]),
+    ]
+
+    def rand_pattern(m, n, max_mult=3):
+        s = np.zeros(m, dtype=int)
+        for _ in range(n):
+            while True:
+                i = rng.integers(0, m)
+                if s[i] < max_mult:
+                    s[i] += 1
+                    break
+        return s.tolist()
+
+    cases = []
+    for seed in (11, 12):
+        U = unitary_group.rvs(4, random_state=seed)
+        for S, T in patterns4:
+            cases.append((U, S, T, seed))
+    for seed, m, n in [(21, 6, 3), (22, 6, 5), (23, 8, 4), (24, 8, 6), (25, 8, 7), (26, 10, 6), (27, 12, 8)]:
+        U = unitary_group.rvs(m, random_state=seed)
+        for _ in range(3):
+            cases.append((U, rand_pattern(m, n), rand_pattern(m, n), seed))
+    # larger single-photon-input cases (the C2 shape at small n)
+    for seed, n in [(31, 9), (32, 10), (33, 11)]:
+        m = 2 * n
+        U = unitary_group.rvs(m, random_state=seed)
+        S = [1] * n + [0] * n
+        T = rand_pattern(m, n, max_mult=2)
+        cases.append((U, S, T, seed))
+
+    perms = []
+    for U, S, T, seed in cases:
+        n = sum(S)
+        rec = {"seed": seed, "U": _m(U), "S": S, "T": T}
+        rec["ryser"] = _c(RyserPermanentCalculator(U, S, T).compute_permanent())
+        rec["chin_huh"] = _c(ChinHuhPermanentCalculator(U, S, T).compute_permanent())
+        if sum(S) == sum(T):
+            rec["glynn"] = _c(GlynnGrayPermanentCalculator(U, S, T).compute_permanent())
+            if n <= 8:
+                rec["classic"] = _c(ClassicPermanentCalculator(U, S, T).compute_permanent())
+        perms.append(rec)
+    with open(os.path.join(out_dir, "perms.json"), "w") as f:
+        json.dump(perms, f)
+
+    # ---- Guan code sequences ----------------------------------------------
+    guan = []
+    for S in ([1, 1, 1], [2, 1, 0, 3], [0, 2, 1], [1, 0, 2, 1, 1], [3]):
+        calc = RyserPermanentCalculator(np.eye(len(S), dtype=complex), S, S)
+        BSGuanCodeBasedPermanentCalculatorBase._initialize_guan_codes_variables(calc)
+        seq_idx, seq_r = [-1], [list(calc._r_vector)]
+        while True:
+            calc._update_guan_code()
+            if calc._index_to_update == len(calc._r_vector):
+                break
+            seq_idx.append(int(calc._index_to_update))
+            seq_r.append([int(x) for x in calc._r_vector])
+        guan.append({"S": S, "idx": seq_idx, "r": seq_r})
+    with open(os.path.join(out_dir, "guan.json"), "w") as f:
+        json.dump(guan, f)
+
+    # ---- submatrices (all-minors) ------------------------------------------
+    sub_cases = []
+    U4 = unitary_group.rvs(4, random_state=41)
+    # tests/test_bs_submatrices_permanent_calculators.py:41-73
+    sub_cases.append((U4, [1, 1, 1, 1], [0, 1, 1, 1]))
+    sub_cases.append((U4, [1.0, 3.0, 0.0, 0.0], [0, 1, 1, 1]))
+    sub_cases.append((U4, [1.0, 0.0, 0.0, 0.0], [0.0, 0.0, 0.0, 0.0]))
+    for seed, m, k in [(42, 6, 3), (43, 8, 5), (44, 8, 6), (45, 12, 8), (46, 16, 10)]:
+        U = unitary_group.rvs(m, random_state=seed)
+        for mm in (1, 2):
+            S = rand_pattern(m, k, max_mult=mm)
+            T = rand_pattern(m, k - 1, max_mult=2)
+            sub_cases.append((U, S, T))
+    subs = []
+    for U, S, T in sub_cases:
+        rec = {"U": _m(U), "S": [float(x) for x in S], "T": [float(x) for x in T]}
+        rec["ryser"] = [_c(v) for v in BSCCRyserSubmatricesPermanentCalculator(U, np.array(S), np.array(T)).compute_permanents()]
+        rec["chin_huh"] = [_c(v) for v in BSCCCHSubmatricesPermanentCalculator(U, np.array(S), np.array(T)).compute_permanents()]
+        subs.append(rec)
+    with open(os.path.join(out_dir, "submatrices.json"), "w") as f:
+        json.dump(subs, f)
+
+    # ---- seeded GCC-B sample streams -----------------------------------------
+    gcc = []
+    for seed, m, n, eta, N in [(51, 8, 4, 0.5, 40), (52, 10, 6, 0.7, 30), (53, 12, 6, None, 20), (54, 6, 3, 0.5, 60)]:
+        U = unitary_group.rvs(m, random_state=seed)
+        inp = [1] * n + [0] * (m - n)
+        np.random.seed(seed)
+        if eta is None:
+            strat = GeneralizedCliffordsBSimulationStrategy(RyserPermanentCalculator(U))
+        else:
+            strat = GeneralizedCliffordsBUniformLossesSimulationStrategy(RyserPermanentCalculator(U), eta)
+        samples = strat.simulate(inp, N)
+        after = float(np.random.random())
+        gcc.append({"kind": "gccb" if eta is None else "gccb_uniform", "seed": seed, "U": _m(U), "input": inp,
+                    "eta": eta, "N": N, "samples": [[int(x) for x in s] for s in samples], "next_random": after})
+    # binned input (multi-photon modes)
+    U = unitary_group.rvs(5, random_state=55)
+    np.random.seed(55)
+    strat = GeneralizedCliffordsBUniformLossesSimulationStrategy(RyserPermanentCalculator(U), 0.8)
+    samples = strat.simulate([2, 1, 1, 0, 0], 40)
+    gcc.append({"kind": "gccb_uniform", "seed": 55, "U": _m(U), "input": [2, 1, 1, 0, 0], "eta": 0.8, "N": 40,
+                "samples": [[int(x) for x in s] for s in samples], "next_random": float(np.random.random())})
+    # non-uniform (network) losses: lossy matrix U diag(sqrt(t))
+    for seed, m, n, N in [(56, 4, 2, 30), (57, 6, 3, 20)]:
+        U = unitary_group.rvs(m, random_state=seed)
+        t = np.random.default_rng(seed).uniform(0.3, 0.9, m)
+        M = U @ np.diag(np.sqrt(t))
+        calc = RyserPermanentCalculator(M.copy())
+        strat = LossyNetworksGeneralizedCliffordsSimulationStrategy(calc)
+        inp = [1] * n + [0] * (m - n)
+        np.random.seed(seed)
+        samples = strat.simulate(inp, N)
+        gcc.append({"kind": "lossy_net", "seed": seed, "U": _m(M), "expanded": _m(calc.matrix), "input": inp,
+                    "N": N, "samples": [[int(x) for x in s] for s in samples],
+                    "next_random": float(np.random.random())})
+    # plain (A-version) GCC
+    for seed, m, n, N in [(58, 6, 3, 15)]:
+        U = unitary_group.rvs(m, random_state=seed)
+        inp = [1] * n + [0] * (m - n)
+        np.random.seed(seed)
+        strat = GeneralizedCliffordsSimulationStrategy(RyserPermanentCalculator(U))
+        samples = strat.simulate(inp, N)
+        gcc.append({"kind": "gcc", "seed": seed, "U": _m(U), "input": inp, "N": N,
+                    "samples": [[int(x) for x in s] for s in samples],
+                    "next_random": float(np.random.random())})
+    with open(os.path.join(out_dir, "gcc_samples.json"), "w") as f:
+        json.dump(gcc, f)
+
+    # ---- exact uniform-loss distribution (the reference's known-answer test) ----
+    P = np.array([[0, 0, 1, 0, 0], [1, 0, 0, 0, 0], [0, 0, 0, 1, 0], [0, 0, 0, 0, 1], [0, 1, 0, 0, 0]],
+                 dtype=np.complex128)
+    cfg = BosonSamplingExperimentConfiguration(
+        interferometer_matrix=P, initial_state=[1, 1, 1, 0, 0], number_of_modes=5, initial_number_of_particles=3,
+        number_of_particles_lost=2, number_of_particles_left=1, uniform_transmissivity=0.8)
+    dist = BSDistributionCalculatorWithUniformLosses(cfg, ChinHuhPermanentCalculator(P)).calculate_distribution()
+    U6 = unitary_group.rvs(4, random_state=61)
+    cfg2 = BosonSamplingExperimentConfiguration(
+        interferometer_matrix=U6, initial_state=[1, 1, 1, 0], number_of_modes=4, initial_number_of_particles=3,
+        number_of_particles_lost=0, number_of_particles_left=3, uniform_transmissivity=0.6)
+    dist2 = BSDistributionCalculatorWithUniformLosses(cfg2, ChinHuhPermanentCalculator(U6)).calculate_distribution()
+    with open(os.path.join(out_dir, "distributions.json"), "w") as f:
+        json.dump([{"U": _m(P), "input": [1, 1, 1, 0, 0], "eta": 0.8, "distribution": [float(x) for x in dist]},
+                   {"U": _m(U6), "input": [1, 1, 1, 0], "eta": 0.6, "distribution": [float(x) for x in dist2]}], f)
+    print("fixtures written to", out_dir)
+
+
+if __name__ == "__main__":
+    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
