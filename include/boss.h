@@ -1,0 +1,109 @@
+/*
+ * boss.h -- C ABI of libboss_gb300.so, the GB300 (sm_103a) implementation of
+ * theboss's permanent hot path.
+ *
+ * theboss is pure Python and has no FFI of its own; each entry point below
+ * replaces one Python-level interface of the reference (cited per function,
+ * paths inside the theboss project) and is what a ctypes / cffi binding in that
+ * project would bind.
+ *
+ * Conventions shared by every entry point:
+ *   - matrices are complex128 (two doubles per entry, real then imaginary),
+ *     row-major m x m, indexed U[output_mode][input_mode] exactly as theboss
+ *     indexes them (ryser_permanent_calculator.py:62-64);
+ *   - occupation vectors are int32, length `len` (len <= m), mode-occupation
+ *     ("second quantisation") form;
+ *   - every pointer is a HOST pointer; the library copies to and from the GPU
+ *     itself and returns only after the results are back in host memory;
+ *   - the return value is a status code (BOSS_OK = 0); boss_last_error() gives a
+ *     one-line message for the calling thread;
+ *   - calls are serialised by an internal mutex; all GPU work runs on one
+ *     library-owned CUDA stream of the current device.
+ */
+#ifndef BOSS_GB300_H
+#define BOSS_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define BOSS_ABI_VERSION 1
+
+#if defined(__GNUC__)
+#define BOSS_API __attribute__((visibility("default")))
+#else
+#define BOSS_API
+#endif
+
+/* Status codes. */
+#define BOSS_OK 0
+#define BOSS_ERR_SIZE 1      /* size mismatch; theboss raises AttributeError (bs_permanent_calculator_base.py:179-180) */
+#define BOSS_ERR_LIMIT 2     /* beyond this library's limits (distinct modes, code count) */
+#define BOSS_ERR_CUDA 3      /* CUDA runtime failure */
+#define BOSS_ERR_ARG 4       /* invalid argument */
+#define BOSS_ERR_PMF 5       /* a sampling pmf could not be normalised; theboss raises ValueError
+                                from numpy.random.choice (generalized_cliffords_b_simulation_strategy.py:107-110) */
+#define BOSS_ERR_NODEVICE 6  /* no CUDA device */
+
+/* Permanent formulas (bs_permanent_calculator_factory.py:29-33). */
+#define BOSS_CLASSIC 3   /* classic_permanent_calculator.py:18-67 semantics (zero-particle rules), Glynn sweep */
+#define BOSS_GLYNN 2     /* glynn_gray_permanent_calculator.py:27-84 */
+#define BOSS_CHIN_HUH 1  /* chin_huh_permanent_calculator.py:18-59 */
+#define BOSS_RYSER 0     /* ryser_permanent_calculator.py:19-64 */
+
+/* Message of the last failed call on this thread (empty if none). */
+BOSS_API const char* boss_last_error(void);
+
+/* BOSS_ABI_VERSION of the loaded library. */
+BOSS_API int boss_abi_version(void);
+
+/* Number of SMs of the current device (also initialises the library's context). */
+BOSS_API int boss_device_sm_count(int32_t* sm_count);
+
+/*
+ * Permanents of `count` effective scattering matrices U[T_k, S_k] of one matrix.
+ * Replaces BSPermanentCalculatorInterface.compute_permanent
+ * (bs_permanent_calculator_interface.py:18-22) of the calculator chosen by
+ * `variant` (RyserPermanentCalculator.compute_permanent,
+ * bs_permanent_calculator_base.py:166-198; ChinHuhPermanentCalculator, same;
+ * GlynnGrayPermanentCalculator.compute_permanent, glynn_gray_permanent_calculator.py:41-71;
+ * ClassicPermanentCalculator.compute_permanent, classic_permanent_calculator.py:27-39),
+ * batched over the output patterns a sampler or distribution calculator asks for
+ * (bs_distribution_calculator_with_fixed_losses.py:127-142).
+ *   matrix         : m x m complex128
+ *   input_states   : count x len int32 (S_k)
+ *   output_states  : count x len int32 (T_k)
+ *   results        : count complex128 (2*count doubles)
+ */
+BOSS_API int boss_perm_batch(const double* matrix, int32_t m, const int32_t* input_states, const int32_t* output_states,
+                    int32_t len, int32_t count, int32_t variant, double* results);
+
+/*
+ * All-minors permanents: for each k and each input mode i, perm(U[T_k, S_k - e_i])
+ * (0 where S_k[i] = 0), in one sweep per k.  Replaces
+ * BSSubmatricesPermanentCalculatorInterface.compute_permanents
+ * (bs_submatrices_permanent_calculator_interface.py:17-20) of
+ * BSCCRyserSubmatricesPermanentCalculator (bs_cc_ryser_submatrices_permanent_calculator.py:16-119)
+ * and BSCCCHSubmatricesPermanentCalculator (bs_cc_ch_submatrices_permanent_calculator.py:25-105),
+ * including the one-particle edge case (bs_submatrices_permanent_calculator_base.py:157-158).
+ *   variant        : BOSS_RYSER or BOSS_CHIN_HUH
+ *   results        : count x len complex128
+ */
+BOSS_API int boss_submatrices_batch(const double* matrix, int32_t m, const int32_t* input_states,
+                           const int32_t* output_states, int32_t len, int32_t count, int32_t variant,
+                           double* results);
+
+/*
+ * FP64 throughput of the current GPU: a dependency-free DFMA stream on every SM,
+ * timed with CUDA events.  Writes TFLOP/s (an FMA counts 2 flops) and the kernel
+ * time.  No reference counterpart: it is the denominator of the FP64 roofline.
+ */
+BOSS_API int boss_fp64_peak(double* tflops, double* milliseconds);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* BOSS_GB300_H */

@@ -1,0 +1,143 @@
+"""ctypes binding of libboss_gb300.so (the C ABI declared in include/boss.h).
+
+The library is built in-tree by ``theboss_gb300.build``.  There is no CPU
+fallback: when the library cannot be loaded, or no GPU is present, the calls
+raise instead of computing anything on the host.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import threading
+
+import numpy as np
+
+from . import build as _build
+
+BOSS_OK = 0
+BOSS_ERR_SIZE = 1
+BOSS_ERR_LIMIT = 2
+BOSS_ERR_CUDA = 3
+BOSS_ERR_ARG = 4
+BOSS_ERR_PMF = 5
+BOSS_ERR_NODEVICE = 6
+
+RYSER, CHIN_HUH, GLYNN, CLASSIC = 0, 1, 2, 3
+
+_lock = threading.Lock()
+_lib = None
+
+
+class GB300Error(RuntimeError):
+    """A CUDA or library failure inside libboss_gb300.so."""
+
+
+def load() -> ctypes.CDLL:
+    """Loads the in-tree library (building it first if the sources are newer)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        path = _build.LIB
+        if not _build.up_to_date():
+            path = _build.build()
+        L = ctypes.CDLL(path)
+        dp = ctypes.POINTER(ctypes.c_double)
+        ip = ctypes.POINTER(ctypes.c_int32)
+        L.boss_last_error.restype = ctypes.c_char_p
+        L.boss_last_error.argtypes = []
+        L.boss_abi_version.restype = ctypes.c_int
+        L.boss_device_sm_count.restype = ctypes.c_int
+        L.boss_device_sm_count.argtypes = [ip]
+        for name in ("boss_perm_batch", "boss_submatrices_batch"):
+            f = getattr(L, name)
+            f.restype = ctypes.c_int
+            f.argtypes = [dp, ctypes.c_int32, ip, ip, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, dp]
+        L.boss_fp64_peak.restype = ctypes.c_int
+        L.boss_fp64_peak.argtypes = [dp, dp]
+        _lib = L
+        return L
+
+
+def library_path() -> str:
+    return _build.LIB
+
+
+def check(status: int) -> None:
+    if status == BOSS_OK:
+        return
+    msg = load().boss_last_error().decode(errors="replace")
+    if status == BOSS_ERR_SIZE:
+        raise AttributeError(msg)
+    if status == BOSS_ERR_PMF:
+        raise ValueError(msg)
+    if status == BOSS_ERR_ARG:
+        raise ValueError(msg)
+    raise GB300Error(f"libboss_gb300 status {status}: {msg}")
+
+
+def _dp(a: np.ndarray):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def _ip(a: np.ndarray):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_int32))
+
+
+def as_matrix(matrix) -> np.ndarray:
+    U = np.asarray(matrix)
+    if U.dtype != np.complex128 or not U.flags.c_contiguous:
+        U = np.ascontiguousarray(U, dtype=np.complex128)
+    if U.ndim != 2:
+        raise AttributeError("matrix must be two-dimensional")
+    return U
+
+
+def as_states(states, length: int) -> np.ndarray:
+    """Occupation vectors (ints or integer-valued floats) -> int32 array."""
+    a = np.asarray(states)
+    if a.dtype.kind == "f":
+        a = np.rint(a)
+    return np.ascontiguousarray(a, dtype=np.int32).reshape(-1, length)
+
+
+def perm_batch(U: np.ndarray, S: np.ndarray, T: np.ndarray, variant: int) -> np.ndarray:
+    """Permanents of U[T_k, S_k]; S, T int32 (count x len).  Returns complex128 (count,)."""
+    L = load()
+    count, n = S.shape
+    out = np.empty(count, dtype=np.complex128)
+    if count == 0:
+        return out
+    check(L.boss_perm_batch(_dp(U.view(np.float64)), U.shape[0], _ip(S), _ip(T), n, count, variant,
+                            _dp(out.view(np.float64))))
+    return out
+
+
+def submatrices_batch(U: np.ndarray, S: np.ndarray, T: np.ndarray, variant: int) -> np.ndarray:
+    """All-minors permanents; returns complex128 (count x len)."""
+    L = load()
+    count, n = S.shape
+    out = np.empty((count, n), dtype=np.complex128)
+    if count == 0:
+        return out
+    check(L.boss_submatrices_batch(_dp(U.view(np.float64)), U.shape[0], _ip(S), _ip(T), n, count, variant,
+                                   _dp(out.view(np.float64))))
+    return out
+
+
+def fp64_peak():
+    """(TFLOP/s, ms) of the FP64 FMA microbenchmark on the current GPU."""
+    L = load()
+    t = np.zeros(1)
+    ms = np.zeros(1)
+    check(L.boss_fp64_peak(_dp(t), _dp(ms)))
+    return float(t[0]), float(ms[0])
+
+
+def sm_count() -> int:
+    L = load()
+    v = np.zeros(1, dtype=np.int32)
+    check(L.boss_device_sm_count(_ip(v)))
+    return int(v[0])
