@@ -96,6 +96,45 @@ BOSS_API int boss_submatrices_batch(const double* matrix, int32_t m, const int32
                            double* results);
 
 /*
+ * The random stream theboss's C&C-B samplers draw, replayed on the host without a
+ * GPU.  numpy's legacy global RandomState is an MT19937 generator; its state
+ * (numpy.random.get_state(): 624-word key and position) is passed in and
+ * returned advanced exactly as theboss's own draws would advance it:
+ *   per sample, with particle_weights (uniform losses): one random() compared with
+ *   the running sum of the weights (generalized_cliffords_b_uniform_losses_simulation_strategy.py:67-85);
+ *   per step: randint(0, remaining) picks the popped particle
+ *   (generalized_cliffords_b_simulation_strategy.py:102-105) and one random_sample()
+ *   is consumed by numpy.random.choice (:107-110).
+ * particle_weights NULL means lossless (every particle kept, no count draw).
+ *   particles_kept : n_samples int32
+ *   popped_modes   : n_samples x n int32 (n = sum(input_state)); -1 past the kept count; may be NULL
+ *   uniforms       : n_samples x n doubles; may be NULL
+ */
+BOSS_API int boss_gccb_predraw(const int32_t* input_state, int32_t m, const double* particle_weights,
+                               int32_t n_weights, uint32_t* mt_key, int32_t* mt_pos, int32_t n_samples,
+                               int32_t* particles_kept, int32_t* popped_modes, double* uniforms);
+
+/*
+ * n_samples generalized Clifford & Clifford (version B) samples on the GPU.
+ * Replaces GeneralizedCliffordsBSimulationStrategy.simulate
+ * (generalized_cliffords_b_simulation_strategy.py:41-67) when particle_weights is
+ * NULL, and GeneralizedCliffordsBUniformLossesSimulationStrategy.simulate
+ * (generalized_cliffords_b_uniform_losses_simulation_strategy.py:87-109) with the
+ * binomial particle-number weights (:50-65); LossyNetworksGeneralizedCliffordsSimulationStrategy
+ * (lossy_networks_generalized_cliffords_simulation_strategy.py:53-83) is the lossless
+ * call on the 2m x 2m expanded matrix.  Consumes numpy's MT19937 stream exactly as
+ * boss_gccb_predraw describes and returns the advanced state, so the samples are
+ * the ones theboss draws with the same seed (given the same probabilities).
+ * All samples run level-synchronously: the all-minors sweeps of every sample at
+ * one step in one launch, the whole loop as one CUDA graph.
+ *   matrix   : m x m complex128, m <= 256;  sum(input_state) <= 32
+ *   samples  : n_samples x m int32 output occupations
+ */
+BOSS_API int boss_gccb_sample(const double* matrix, int32_t m, const int32_t* input_state,
+                              const double* particle_weights, int32_t n_weights, uint32_t* mt_key, int32_t* mt_pos,
+                              int32_t n_samples, int32_t* samples);
+
+/*
  * FP64 throughput of the current GPU: a dependency-free DFMA stream on every SM,
  * timed with CUDA events.  Writes TFLOP/s (an FMA counts 2 flops) and the kernel
  * time.  No reference counterpart: it is the denominator of the FP64 roofline.

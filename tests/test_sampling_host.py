@@ -1,0 +1,55 @@
+"""Host-side parts of the batched sampler (no GPU): the MT19937 replay inside
+libboss_gb300.so must draw exactly what numpy's global RandomState draws for
+theboss's C&C-B samplers, and leave the generator in the same state."""
+import numpy as np
+import pytest
+
+
+@pytest.mark.parametrize("inp,eta,N", [([1] * 6 + [0] * 4, 0.5, 200), ([2, 1, 1, 0, 0], 0.8, 100),
+                                       ([1] * 20 + [0] * 20, None, 50), ([1] * 20 + [0] * 20, 0.5, 500),
+                                       ([0, 0, 0], 0.3, 20), ([1], None, 30)])
+def test_predraw_matches_numpy_replay(oracle, inp, eta, N):
+    from theboss_gb300 import _native
+
+    n = sum(inp)
+    w = None if eta is None else oracle.binomial_weights(n, eta)
+    np.random.seed(1234)
+    L_ref, A_ref, U_ref = oracle.predraw_gccb(inp, N, w)
+    after_ref = np.random.random()
+    np.random.seed(1234)
+    kept, popped, uni = _native.gccb_predraw(inp, w, N)
+    after = np.random.random()
+    assert after == after_ref
+    assert kept.tolist() == L_ref.tolist()
+    for s in range(N):
+        l = kept[s]
+        assert popped[s, :l].tolist() == A_ref[s, :l].tolist()
+        assert uni[s, :l].tolist() == U_ref[s, :l].tolist()
+
+
+def test_predraw_state_positions_across_twist(oracle):
+    """Long streams cross many MT19937 regenerations (every 624 words)."""
+    from theboss_gb300 import _native
+
+    np.random.seed(7)
+    for _ in range(3):
+        np.random.random()
+    st = np.random.get_state()
+    inp = [1] * 12 + [0] * 12
+    L_ref, A_ref, U_ref = oracle.predraw_gccb(inp, 400, None)
+    ref_next = np.random.random()
+    np.random.set_state(st)
+    kept, popped, uni = _native.gccb_predraw(inp, None, 400)
+    assert np.random.random() == ref_next
+    assert (popped == A_ref).all() and (uni == U_ref).all()
+
+
+def test_expanded_space_matrix_matches_reference():
+    from conftest import as_matrix, load_golden
+    from theboss_gb300.utilities import prepare_interferometer_matrix_in_expanded_space
+
+    for rec in load_golden("gcc_samples.json"):
+        if rec["kind"] != "lossy_net":
+            continue
+        got = prepare_interferometer_matrix_in_expanded_space(as_matrix(rec["U"]))
+        assert np.array_equal(got, as_matrix(rec["expanded"]))

@@ -57,6 +57,11 @@ def load() -> ctypes.CDLL:
             f.argtypes = [dp, ctypes.c_int32, ip, ip, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, dp]
         L.boss_fp64_peak.restype = ctypes.c_int
         L.boss_fp64_peak.argtypes = [dp, dp]
+        up = ctypes.POINTER(ctypes.c_uint32)
+        L.boss_gccb_predraw.restype = ctypes.c_int
+        L.boss_gccb_predraw.argtypes = [ip, ctypes.c_int32, dp, ctypes.c_int32, up, ip, ctypes.c_int32, ip, ip, dp]
+        L.boss_gccb_sample.restype = ctypes.c_int
+        L.boss_gccb_sample.argtypes = [dp, ctypes.c_int32, ip, dp, ctypes.c_int32, up, ip, ctypes.c_int32, ip]
         _lib = L
         return L
 
@@ -141,3 +146,61 @@ def sm_count() -> int:
     v = np.zeros(1, dtype=np.int32)
     check(L.boss_device_sm_count(_ip(v)))
     return int(v[0])
+
+
+# ---------------------------------------------------------------------------
+# numpy's global legacy RandomState <-> the library's MT19937 replay
+# ---------------------------------------------------------------------------
+def _get_mt():
+    st = np.random.get_state()
+    if st[0] != "MT19937":
+        raise ValueError("numpy's global generator is not MT19937")
+    key = np.array(st[1], dtype=np.uint32, copy=True)
+    pos = np.array([st[2]], dtype=np.int32)
+    return st, key, pos
+
+
+def _set_mt(st, key, pos) -> None:
+    np.random.set_state((st[0], key, int(pos[0]), st[3], st[4]))
+
+
+def _weights_arg(weights):
+    if weights is None:
+        return None, 0, None
+    w = np.ascontiguousarray(weights, dtype=np.float64)
+    return w, len(w), _dp(w)
+
+
+def gccb_predraw(input_state, weights, n_samples: int):
+    """Replays, without a GPU, the numbers theboss's C&C-B sampler draws from numpy's
+    global RandomState and advances that state the same way.  Returns
+    (particles_kept, popped_modes, uniforms)."""
+    L = load()
+    inp = np.ascontiguousarray(input_state, dtype=np.int32)
+    n = int(inp.sum())
+    w, nw, wp = _weights_arg(weights)
+    st, key, pos = _get_mt()
+    kept = np.zeros(n_samples, dtype=np.int32)
+    popped = np.zeros((n_samples, max(n, 1)), dtype=np.int32)
+    uni = np.zeros((n_samples, max(n, 1)), dtype=np.float64)
+    check(L.boss_gccb_predraw(_ip(inp), len(inp), wp, nw, key.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32)),
+                              _ip(pos), n_samples, _ip(kept), _ip(popped), _dp(uni)))
+    _set_mt(st, key, pos)
+    return kept, popped[:, :n], uni[:, :n]
+
+
+def gccb_sample(U: np.ndarray, input_state, weights, n_samples: int) -> np.ndarray:
+    """n_samples C&C-B samples on the GPU; consumes numpy's global RandomState like
+    theboss does.  Returns int32 (n_samples x m)."""
+    L = load()
+    inp = np.ascontiguousarray(input_state, dtype=np.int32)
+    m = U.shape[0]
+    if len(inp) != m:
+        raise AttributeError("input state length differs from the matrix dimension")
+    w, nw, wp = _weights_arg(weights)
+    st, key, pos = _get_mt()
+    out = np.zeros((n_samples, m), dtype=np.int32)
+    check(L.boss_gccb_sample(_dp(U.view(np.float64)), m, _ip(inp), wp, nw,
+                             key.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32)), _ip(pos), n_samples, _ip(out)))
+    _set_mt(st, key, pos)
+    return out

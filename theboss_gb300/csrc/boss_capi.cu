@@ -47,6 +47,10 @@ Context* context(int* status) {
     *status = fail_cuda(e, "cudaStreamCreate");
     return nullptr;
   }
+  if ((e = prepare_sweep_kernels()) != cudaSuccess) {
+    *status = fail_cuda(e, "kernel attributes");
+    return nullptr;
+  }
   g_ctx.ready = true;
   return &g_ctx;
 }

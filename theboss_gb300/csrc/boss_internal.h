@@ -23,6 +23,7 @@ struct SweepLaunch {
   int grid = 1;
 };
 
+cudaError_t prepare_sweep_kernels();
 cudaError_t launch_perm_sweep(const SweepLaunch& L, cudaStream_t st);
 cudaError_t launch_minors_sweep(const SweepLaunch& L, cudaStream_t st);
 cudaError_t launch_perm_reduce(const SweepPlan* plans, const int32_t* out_plans, const int32_t* out_begin, int n_out,

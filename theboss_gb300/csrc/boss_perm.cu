@@ -252,18 +252,26 @@ static cudaError_t launch_perm_nc(const SweepLaunch& L, cudaStream_t st) {
   return cudaGetLastError();
 }
 
+constexpr size_t kMinorsSmem = 4 * 16 * 32 * sizeof(double2);
+
 template <int NC>
 static cudaError_t launch_minors_nc(const SweepLaunch& L, cudaStream_t st) {
-  const size_t smem = 4 * 16 * 32 * sizeof(double2);
-  static bool configured = false;
-  if (!configured) {
-    cudaError_t e = cudaFuncSetAttribute(minors_sweep_kernel<NC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    configured = true;
-  }
-  minors_sweep_kernel<NC><<<L.grid, 128, smem, st>>>(L.plans, L.n_plans, L.pool, L.total_items, L.counter,
-                                                    L.partials);
+  minors_sweep_kernel<NC><<<L.grid, 128, kMinorsSmem, st>>>(L.plans, L.n_plans, L.pool, L.total_items, L.counter,
+                                                           L.partials);
   return cudaGetLastError();
+}
+
+// Kernel attributes are set once per process, outside any stream capture.
+cudaError_t prepare_sweep_kernels() {
+  cudaError_t e;
+  if ((e = cudaFuncSetAttribute(minors_sweep_kernel<8>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)kMinorsSmem)) != cudaSuccess)
+    return e;
+  if ((e = cudaFuncSetAttribute(minors_sweep_kernel<16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)kMinorsSmem)) != cudaSuccess)
+    return e;
+  return cudaFuncSetAttribute(minors_sweep_kernel<32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)kMinorsSmem);
 }
 
 cudaError_t launch_perm_sweep(const SweepLaunch& L, cudaStream_t st) {

@@ -1,0 +1,298 @@
+"""Drop-in GB300 replacements for theboss's generalized Clifford & Clifford samplers.
+
+  SimulationStrategyInterface                          simulation_strategy_interface.py:7-23
+  GeneralizedCliffordsBSimulationStrategy              generalized_cliffords_b_simulation_strategy.py:31-110
+  GeneralizedCliffordsBUniformLossesSimulationStrategy generalized_cliffords_b_uniform_losses_simulation_strategy.py:24-121
+  LossyNetworksGeneralizedCliffordsSimulationStrategy  lossy_networks_generalized_cliffords_simulation_strategy.py:24-88
+  GeneralizedCliffordsSimulationStrategy               generalized_cliffords_simulation_strategy.py:20-266
+  GeneralizedCliffordsUniformLossesSimulationStrategy  generalized_cliffords_uniform_losses_simulation_strategy.py:19-173
+
+The B-version samplers hand the whole request to the batched GPU sampler
+(libboss_gb300.so, boss_gccb_sample): it consumes numpy's global RandomState
+exactly as theboss does (same calls, same order), so with the same seed it
+returns the samples theboss returns (given the same probabilities) and leaves
+the generator in the same state.  Return types follow theboss: tuples for the
+lossless and network-loss samplers, int64 arrays for the uniform-loss sampler.
+
+GCCBPlainDriver is the reference's per-step loop with the GPU all-minors
+calculator dropped in (one GPU launch per sampling step); it exists to measure
+what batching buys.
+"""
+from __future__ import annotations
+
+import abc
+import random as _stdlib_random
+from collections import defaultdict
+from copy import copy
+from math import factorial
+from typing import List, Sequence, Tuple
+
+import numpy as np
+
+from . import _native
+from .permanent_calculators import BSPermanentCalculatorInterface
+from .submatrices_calculators import BSCCRyserSubmatricesPermanentCalculator
+from .utilities import mode_occupation_to_mode_assignment, prepare_interferometer_matrix_in_expanded_space
+
+
+class SimulationStrategyInterface(abc.ABC):
+    @abc.abstractmethod
+    def simulate(self, input_state: Sequence[int], samples_number: int = 1):
+        raise NotImplementedError
+
+
+def _binomial_weights(n: int, eta: float) -> List[float]:
+    """generalized_cliffords_b_uniform_losses_simulation_strategy.py:50-65 (same
+    expression, same evaluation order)."""
+    from scipy.special import binom
+
+    return [binom(n, l) * pow(eta, l) * pow(1 - eta, n - l) for l in range(n + 1)]
+
+
+class GeneralizedCliffordsBSimulationStrategy(SimulationStrategyInterface):
+    """C&C-B, lossless.  simulate() -> list of tuples."""
+
+    def __init__(self, bs_permanent_calculator: BSPermanentCalculatorInterface) -> None:
+        self._bs_permanent_calculator = bs_permanent_calculator
+        self.r_sample: List[int] = []
+        self.input_state: Sequence[int] = []
+        self.number_of_input_photons = 0
+
+    def set_new_matrix(self, new_matrix) -> None:
+        self._bs_permanent_calculator.matrix = new_matrix
+
+    def _gpu_samples(self, input_state, samples_number: int, weights) -> np.ndarray:
+        U = _native.as_matrix(self._bs_permanent_calculator.matrix)
+        inp = np.asarray(input_state)
+        if inp.dtype.kind == "f":
+            inp = np.rint(inp)
+        return _native.gccb_sample(U, inp.astype(np.int32), weights, int(samples_number))
+
+    def simulate(self, input_state: Sequence[int], samples_number: int = 1) -> List[Tuple[int, ...]]:
+        self.input_state = input_state
+        self.number_of_input_photons = int(sum(input_state))
+        out = self._gpu_samples(input_state, samples_number, None)
+        return [tuple(row) for row in out.tolist()]
+
+
+class GeneralizedCliffordsBUniformLossesSimulationStrategy(GeneralizedCliffordsBSimulationStrategy):
+    """C&C-B with uniform losses (binomial number of surviving particles).
+    simulate() -> list of int64 arrays."""
+
+    def __init__(self, bs_permanent_calculator: BSPermanentCalculatorInterface, transmissivity: float = 1.0) -> None:
+        super().__init__(bs_permanent_calculator)
+        self._transmissivity = transmissivity
+        self._binomial_weights: List[float] = []
+
+    def simulate(self, input_state, samples_number: int = 1) -> List[np.ndarray]:
+        self.input_state = input_state
+        self.number_of_input_photons = int(sum(input_state))
+        self._binomial_weights = _binomial_weights(self.number_of_input_photons, self._transmissivity)
+        out = self._gpu_samples(input_state, samples_number, self._binomial_weights).astype(np.int64)
+        return list(out)
+
+
+class LossyNetworksGeneralizedCliffordsSimulationStrategy(SimulationStrategyInterface):
+    """Non-uniform (mode-dependent) losses: lossless C&C-B in the 2m-mode unitary
+    dilation of the lossy matrix, extra modes trimmed.  simulate() -> list of tuples."""
+
+    def __init__(self, bs_permanent_calculator: BSPermanentCalculatorInterface) -> None:
+        bs_permanent_calculator.matrix = prepare_interferometer_matrix_in_expanded_space(
+            bs_permanent_calculator.matrix)
+        self._helper_strategy = GeneralizedCliffordsBSimulationStrategy(bs_permanent_calculator)
+
+    def simulate(self, input_state: Sequence[int], samples_number: int = 1) -> List[Tuple[int, ...]]:
+        m = len(input_state)
+        expanded = np.concatenate([np.asarray(input_state), np.zeros(m, dtype=int)])
+        out = self._helper_strategy._gpu_samples(expanded, samples_number, None)
+        return [tuple(row[:m]) for row in out.tolist()]
+
+    def set_new_matrix(self, matrix) -> None:
+        self._helper_strategy.set_new_matrix(prepare_interferometer_matrix_in_expanded_space(matrix))
+
+
+class GCCBPlainDriver(GeneralizedCliffordsBUniformLossesSimulationStrategy):
+    """theboss's own per-sample, per-step C&C-B loop
+    (generalized_cliffords_b_simulation_strategy.py:69-110 with the uniform-loss
+    particle count of generalized_cliffords_b_uniform_losses_simulation_strategy.py:67-121),
+    calling the GPU all-minors calculator once per step.  Same samples and random
+    stream as the batched sampler."""
+
+    def simulate(self, input_state, samples_number: int = 1) -> List[np.ndarray]:
+        self.input_state = input_state
+        self.number_of_input_photons = int(sum(input_state))
+        self._binomial_weights = _binomial_weights(self.number_of_input_photons, self._transmissivity)
+        particles = list(mode_occupation_to_mode_assignment(input_state))
+        U = self._bs_permanent_calculator.matrix
+        m = len(input_state)
+        samples = []
+        while len(samples) < samples_number:
+            kept, acc, thr = 0, 0, np.random.random()
+            for w in self._binomial_weights:
+                acc += w
+                if acc > thr:
+                    break
+                kept += 1
+            current = np.zeros(m, dtype=np.int64)
+            work = particles.copy()
+            r = [0] * m
+            while kept > sum(r):
+                current[work.pop(np.random.randint(0, len(work)))] += 1
+                sub = BSCCRyserSubmatricesPermanentCalculator(U, current, r).compute_permanents()
+                perms = np.asarray(U) @ (current * np.asarray(sub))
+                pmf = [abs(p) ** 2 for p in perms]
+                total = sum(pmf)
+                pmf = [v / total for v in pmf]
+                r[np.random.choice(range(m), p=pmf)] += 1
+            samples.append(np.array(r, dtype=np.int64))
+        return samples
+
+
+class GeneralizedCliffordsSimulationStrategy(SimulationStrategyInterface):
+    """Plain (A-version) generalized C&C: per new output prefix, every output's
+    probability is a weighted sum of |perm|^2 over the input's sub-multisets; all
+    permanents of one layer go to the GPU in one batched launch.  Layers are
+    memoised per prefix and sampling follows generalized_cliffords_simulation_strategy.py:249-266."""
+
+    def __init__(self, bs_permanent_calculator: BSPermanentCalculatorInterface) -> None:
+        self.r_sample: List[int] = []
+        self.number_of_input_photons = 0
+        self.pmfs = dict()
+        self._bs_permanent_calculator = bs_permanent_calculator
+        self.input_state: Sequence[int] = []
+        self._labeled_states = defaultdict(list)
+        self.possible_outputs = dict()
+        self.current_key = tuple(self.r_sample)
+        self.current_sample_probability = 1
+
+    def set_new_matrix(self, new_matrix) -> None:
+        self._bs_permanent_calculator.matrix = new_matrix
+
+    def simulate(self, input_state, samples_number: int = 1):
+        self.input_state = input_state
+        self.number_of_input_photons = int(sum(input_state))
+        self._get_sorted_possible_states()
+        self.pmfs = dict()
+        samples = []
+        while len(samples) < samples_number:
+            self._fill_r_sample()
+            samples.append(tuple(self.r_sample))
+        return samples
+
+    def _get_sorted_possible_states(self) -> None:
+        states = [()]
+        for v in reversed(list(self.input_state)):  # generalized_cliffords_simulation_strategy.py:95-121 order
+            states = [(i,) + s for i in range(int(v) + 1) for s in states]
+        self._labeled_states = defaultdict(list)
+        for s in states:
+            self._labeled_states[sum(s)].append(np.array(s, dtype=np.int64))
+
+    def _fill_r_sample(self) -> None:
+        self.r_sample = [0 for _ in self.input_state]
+        self.current_key = tuple(self.r_sample)
+        self.current_sample_probability = 1
+        while self.number_of_input_photons > sum(self.r_sample):
+            if self.current_key not in self.pmfs:
+                self._calculate_new_layer_of_pmfs()
+            self._sample_from_latest_pmf()
+
+    def _weights(self, k_vectors) -> np.ndarray:
+        from scipy.special import binom
+
+        n = int(sum(self.input_state))
+        out = []
+        for kv in k_vectors:
+            l = int(sum(kv))
+            w = factorial(l) * factorial(n - l) / factorial(n)
+            for mm in range(len(self.input_state)):
+                w *= binom(self.input_state[mm], kv[mm])
+            out.append(w)
+        return np.asarray(out, dtype=np.float64)
+
+    def _layer_probabilities(self, inputs, outputs) -> np.ndarray:
+        """|perm(U[out, in])|^2 / prod(in!) / |in|! for every (output, input) pair,
+        as one batched GPU call.  Returns (len(outputs), len(inputs))."""
+        n_in = len(inputs)
+        L = len(self.input_state)
+        S = np.repeat(np.asarray(inputs, dtype=np.int32).reshape(1, n_in, L), len(outputs), axis=0).reshape(-1, L)
+        T = np.repeat(np.asarray(outputs, dtype=np.int32), n_in, axis=0)
+        calc = self._bs_permanent_calculator
+        variant = getattr(calc, "_VARIANT", _native.RYSER)
+        perms = _native.perm_batch(_native.as_matrix(calc.matrix), np.ascontiguousarray(S), np.ascontiguousarray(T),
+                                   variant)
+        prob = (np.abs(perms) ** 2).reshape(len(outputs), n_in)
+        # generalized_cliffords_simulation_strategy.py:240-245: one division per mode, then by |S|!
+        for i, s in enumerate(inputs):
+            for v in s:
+                prob[:, i] /= factorial(int(v))
+            prob[:, i] /= factorial(int(sum(s)))
+        return prob
+
+    def _calculate_new_layer_of_pmfs(self) -> None:
+        k = sum(self.r_sample) + 1
+        inputs = self._labeled_states[k]
+        weights = self._weights([[self.input_state[i] - s[i] for i in range(len(s))] for s in inputs])
+        weights /= sum(weights)
+        outputs = self._generate_possible_output_states()
+        self.possible_outputs[self.current_key] = outputs
+        probs = self._layer_probabilities(inputs, outputs)
+        pmf = []
+        for o in range(len(outputs)):
+            acc = 0
+            for i in range(len(inputs)):
+                acc += probs[o, i] * weights[i]
+            pmf.append(acc)
+        self.pmfs[self.current_key] = pmf
+
+    def _generate_possible_output_states(self) -> List[List[int]]:
+        out = []
+        for i in range(len(self.r_sample)):
+            new = copy(self.r_sample)
+            new[i] += 1
+            out.append(new)
+        return out
+
+    def _sample_from_latest_pmf(self) -> None:
+        pmf = self.pmfs[self.current_key]
+        idx = 0
+        rv = np.random.random() * sum(pmf)
+        acc = 0
+        for p in pmf:
+            acc += p
+            if acc > rv:
+                break
+            idx += 1
+        self.current_sample_probability = pmf[idx]
+        self.r_sample = self.possible_outputs[self.current_key][idx]
+        self.current_key = tuple(self.r_sample)
+
+
+class GeneralizedCliffordsUniformLossesSimulationStrategy(GeneralizedCliffordsSimulationStrategy):
+    """A-version with per-photon uniform losses drawn from Python's ``random``
+    module (generalized_cliffords_uniform_losses_simulation_strategy.py:125-138)."""
+
+    def __init__(self, bs_permanent_calculator: BSPermanentCalculatorInterface, transmissivity: float = 0) -> None:
+        self._transmissivity = transmissivity
+        super().__init__(bs_permanent_calculator)
+
+    def simulate(self, input_state, samples_number: int = 1) -> List[np.ndarray]:
+        self.input_state = input_state
+        self.number_of_input_photons = int(sum(input_state))
+        self._get_sorted_possible_states()
+        self.pmfs = dict()
+        samples = []
+        while len(samples) < samples_number:
+            self._fill_r_sample()
+            samples.append(np.array(self.r_sample, dtype=np.int64))
+        return samples
+
+    def _fill_r_sample(self) -> None:
+        self.r_sample = [0 for _ in self._bs_permanent_calculator.matrix]
+        self.current_key = tuple(self.r_sample)
+        self.current_sample_probability = 1
+        for _ in range(self.number_of_input_photons):
+            if _stdlib_random.random() >= self._transmissivity:
+                continue
+            if self.current_key not in self.pmfs:
+                self._calculate_new_layer_of_pmfs()
+            self._sample_from_latest_pmf()
