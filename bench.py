@@ -1,0 +1,335 @@
+"""Benchmark of the GB300 permanent hot path (one JSON line on rank 0).
+
+Workload (the configuration the headline metric is quoted on): generalized
+Clifford & Clifford B sampling with uniform losses, transmissivity 0.5, n = 20
+single photons in modes 0..19 of m = 40 modes, 10^4 samples per step, on a
+seeded Haar-random 40 x 40 complex128 unitary (Mezzadri QR), numpy's global
+generator seeded like theboss's own runs.  A step is one full batch of 10^4
+samples through the captured sampler graph.
+
+  value    samples/s on the GPU with the inputs (matrix, random stream) resident
+           in HBM, CUDA-event timed per step, L2 flushed (256 MiB memset) between
+           steps.
+  e2e      samples/s through the C ABI with host buffers (boss_gccb_sample: host
+           random-stream replay, H2D, graph, D2H).
+  roofline the all-minors sweep kernel (the dominant kernel) against the FP64 FMA
+           peak measured live by boss_fp64_peak.
+  plain_gpu / batched_vs_plain
+           theboss's own per-step loop with the GPU all-minors calculator (one
+           launch per sampling step) on a bounded number of samples.
+  single_permanents
+           64 permanents per size n in {16, 20, 24, 28, 30} of an m = 2n Haar
+           unitary, single photons in, ~20% doubly-occupied outputs, Glynn sweep,
+           device-timed, against the same FP64 peak.
+  cpu_baseline
+           the CPU restatement of theboss's sampler (oracle/, C + OpenMP on all
+           host threads) on a bounded sample of the same workload.
+
+--impl reference times that CPU restatement alone (theboss is pure Python; its
+algorithm restated in C is the reference implementation that runs on the box).
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "GCC samples/s n=20,m=40 batched vs plain GPU; perms/s %FP64 peak; rel err≤10^-10".replace(
+    "10^-10", "1e-10")
+N_PHOTONS, N_MODES, ETA = 20, 40, 0.5
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--samples", type=int, default=10000)
+    ap.add_argument("--seed", type=int, default=2026)
+    ap.add_argument("--quick", action="store_true", help="skip the single-permanent and plain-driver sections")
+    return ap.parse_args()
+
+
+def workload(seed):
+    from scipy.special import binom
+
+    from theboss_gb300.utilities import haar_unitary
+
+    U = haar_unitary(N_MODES, seed)
+    inp = np.array([1] * N_PHOTONS + [0] * (N_MODES - N_PHOTONS), dtype=np.int32)
+    w = [binom(N_PHOTONS, l) * pow(ETA, l) * pow(1 - ETA, N_PHOTONS - l) for l in range(N_PHOTONS + 1)]
+    return U, inp, w
+
+
+def config(args, extra=None):
+    c = {"workload": "GCC-B uniform losses eta=0.5, n=20 photons, m=40 modes, 10^4 samples/step, Haar unitary",
+         "n": N_PHOTONS, "m": N_MODES, "eta": ETA, "samples_per_step": args.samples, "seed": args.seed,
+         "l2": "flushed between timed steps (256 MiB memset)", "parallelism": f"replicas x{args.gpus}"}
+    if extra:
+        c.update(extra)
+    return c
+
+
+class Clocks:
+    """Samples nvidia-smi clocks and throttle reasons while a region runs."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index=0):
+        self.idx = gpu_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                                          "-lms", "200", "-i", str(self.idx)], stdout=self.f,
+                                         stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.close()
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            p = [x.strip() for x in line.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                mx = max(mx, float(p[2]))
+            except ValueError:
+                continue
+            for name, v in zip(names, p[5:9]):
+                if v.lower() == "active":
+                    reasons.add(name)
+        os.unlink(self.path)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_baseline(U, inp, w, seed, budget_s=10.0):
+    """theboss's sampler restated in C (oracle/) on all host threads, on a bounded
+    sample of the workload sized to about budget_s seconds."""
+    from oracle import oracle as O
+
+    threads = os.cpu_count() or 1
+    os.environ.setdefault("OMP_NUM_THREADS", str(threads))
+    O.lib()
+
+    def run(n):
+        np.random.seed(seed)
+        L, A, Uu = O.predraw_gccb(list(inp), n, w)
+        t = time.perf_counter()
+        O.gccb_run(U, L, A, Uu)
+        return time.perf_counter() - t
+
+    probe = 200
+    dt = run(probe)
+    n = int(min(10 ** 5, max(probe, probe * budget_s / max(dt, 1e-6))))
+    dt = run(n)
+    return {"value": n / dt, "unit": "samples/s", "cores": int(os.environ["OMP_NUM_THREADS"]), "kind": "port",
+            "sample": f"{n} samples of the workload (same seed and matrix), C restatement of theboss's "
+                      f"GCC-B sampler, OpenMP over samples, {dt:.1f} s"}
+
+
+def c2_patterns(n, count, seed):
+    """Output patterns with about 20% of the occupied modes doubly occupied."""
+    rng = np.random.default_rng(seed)
+    m = 2 * n
+    out = []
+    for _ in range(count):
+        distinct = int(round(n / 1.2))
+        doubles = n - distinct
+        modes = rng.choice(m, size=distinct, replace=False)
+        T = np.zeros(m, dtype=np.int32)
+        T[modes] = 1
+        T[modes[:doubles]] = 2
+        out.append(T)
+    return np.array(out, dtype=np.int32)
+
+
+def single_permanents(peak_tflops, seed):
+    from theboss_gb300 import _native
+    from theboss_gb300.utilities import haar_unitary
+
+    res = {}
+    for n in (16, 20, 24, 28, 30):
+        U = haar_unitary(2 * n, seed + n)
+        T = c2_patterns(n, 64, seed + n)
+        S = np.zeros_like(T)
+        S[:, :n] = 1
+        b = _native.perm_bench(U, S, T, _native.GLYNN, warmup=1, steps=2 if n >= 28 else 5)
+        ms = float(np.mean(b["sweep_ms"]))
+        tf = b["flops"] / (ms / 1e3) / 1e12
+        res[str(n)] = {"perms_per_s": 64 / (ms / 1e3), "ms_per_64": ms, "codes": b["codes"],
+                       "achieved_tflops": tf, "frac_of_fp64_peak": tf / peak_tflops}
+    return res
+
+
+def run_ours(args, rank, world):
+    from theboss_gb300 import _native
+    from theboss_gb300.simulation_strategies import GCCBPlainDriver
+    from theboss_gb300.permanent_calculators import RyserPermanentCalculator
+
+    U, inp, w = workload(args.seed)
+    peak, _ = _native.fp64_peak()
+    clocks = Clocks(int(os.environ.get("LOCAL_RANK", "0")))
+    np.random.seed(args.seed + rank)
+    _barrier(world)
+    clocks.start()
+    t_wall = time.perf_counter()
+    b = _native.gccb_bench(U, inp, w, args.samples, args.warmup, args.steps)
+    t_wall = time.perf_counter() - t_wall
+    clk = clocks.stop()
+    _barrier(world)
+    total_ms = float(np.sum(b["step_ms"]))
+    total_ms = _max_over_ranks(total_ms, world)
+    value = world * args.samples * args.steps / (total_ms / 1e3)
+    sweep_s = float(np.mean(b["sweep_ms"])) / 1e3
+    achieved = b["sweep_flops"] / sweep_s / 1e12
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "sweep_traffic.json")
+    if os.path.exists(tpath):
+        try:
+            traffic = json.load(open(tpath)).get("dram_bytes_per_step")
+        except Exception:
+            traffic = None
+    # e2e through the C ABI with host buffers; the samples must equal the device run's
+    e2e_t = []
+    for _ in range(args.steps):
+        np.random.seed(args.seed + rank)
+        t = time.perf_counter()
+        out = _native.gccb_sample(U, inp, w, args.samples)
+        e2e_t.append(time.perf_counter() - t)
+    if not np.array_equal(out, b["samples"]):
+        raise SystemExit("e2e samples differ from the device-timed run")
+    e2e = {"value": args.samples * args.steps / sum(e2e_t), "unit": "samples/s",
+           "h2d_bytes_per_step": b["h2d_bytes"], "d2h_bytes_per_step": b["d2h_bytes"]}
+    line = {"metric": METRIC, "value": value, "unit": "samples/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded Haar unitary)",
+            "config": config(args), "clocks": clk, "e2e": e2e,
+            "gpu_launches": b["kernels"] * args.steps,
+            "roofline": {"bound": "fp64", "kernel": "minors_sweep_kernel (all levels of a step)",
+                         "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
+                         "traffic": traffic, "peak_source": "boss_fp64_peak, measured in this run",
+                         "sweep_ms_per_step": sweep_s * 1e3, "flops_per_step": b["sweep_flops"]},
+            "wall_s_device_section": t_wall}
+    if rank == 0 and not args.quick:
+        # theboss's per-step loop with the GPU all-minors calculator, bounded sample
+        n_plain = 200
+        np.random.seed(args.seed)
+        t = time.perf_counter()
+        GCCBPlainDriver(RyserPermanentCalculator(U), ETA).simulate(list(inp), n_plain)
+        plain = n_plain / (time.perf_counter() - t)
+        line["plain_gpu"] = {"value": plain, "unit": "samples/s", "samples": n_plain}
+        line["batched_vs_plain"] = {"device": value / world / plain, "e2e": e2e["value"] / plain}
+        line["single_permanents"] = single_permanents(peak, args.seed)
+    if rank == 0:
+        line["cpu_baseline"] = cpu_baseline(U, inp, w, args.seed)
+        print(json.dumps(line), flush=True)
+
+
+def run_reference(args, rank):
+    if rank != 0:
+        return
+    from oracle import oracle as O
+
+    U, inp, w = workload(args.seed)
+    threads = os.cpu_count() or 1
+    os.environ.setdefault("OMP_NUM_THREADS", str(threads))
+    O.lib()
+    # calibrate a per-step sample of about 3 s
+    np.random.seed(args.seed)
+    L, A, Uu = O.predraw_gccb(list(inp), 200, w)
+    t = time.perf_counter()
+    O.gccb_run(U, L, A, Uu)
+    per = (time.perf_counter() - t) / 200
+    n = int(min(args.samples, max(200, 3.0 / max(per, 1e-9))))
+    times = []
+    for it in range(args.warmup + args.steps):
+        np.random.seed(args.seed)
+        L, A, Uu = O.predraw_gccb(list(inp), n, w)
+        t = time.perf_counter()
+        O.gccb_run(U, L, A, Uu)
+        dt = time.perf_counter() - t
+        if it >= args.warmup:
+            times.append(dt)
+    value = n * len(times) / sum(times)
+    sample = (f"{n} of the {args.samples} samples per step (same seed and matrix), C restatement of theboss's "
+              f"GCC-B sampler, OpenMP over samples")
+    line = {"metric": METRIC, "value": value, "unit": "samples/s", "impl": "reference", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * args.samples / value,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded Haar unitary)", "config": config(args),
+            "cpu_baseline": {"value": value, "unit": "samples/s", "cores": int(os.environ["OMP_NUM_THREADS"]),
+                             "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": "samples/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def _barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def _max_over_ranks(x, world):
+    if world <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def main():
+    args = parse()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("gloo")
+    if args.impl == "reference":
+        run_reference(args, rank)
+    else:
+        from theboss_gb300 import _native
+
+        _native.select_device(int(os.environ.get("LOCAL_RANK", "0")))
+        run_ours(args, rank, world)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

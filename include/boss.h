@@ -59,6 +59,10 @@ BOSS_API const char* boss_last_error(void);
 /* BOSS_ABI_VERSION of the loaded library. */
 BOSS_API int boss_abi_version(void);
 
+/* Binds the library to a CUDA device (call before any other GPU entry point; one
+ * process drives one GPU).  Without it the library uses the current device. */
+BOSS_API int boss_select_device(int32_t device);
+
 /* Number of SMs of the current device (also initialises the library's context). */
 BOSS_API int boss_device_sm_count(int32_t* sm_count);
 
@@ -94,6 +98,21 @@ BOSS_API int boss_perm_batch(const double* matrix, int32_t m, const int32_t* inp
 BOSS_API int boss_submatrices_batch(const double* matrix, int32_t m, const int32_t* input_states,
                            const int32_t* output_states, int32_t len, int32_t count, int32_t variant,
                            double* results);
+
+/*
+ * Benchmark form of boss_perm_batch for `count` permanents with the same number
+ * of product-side particles: planned and uploaded once, then the sweep kernel and
+ * its reduction run n_warmup + n_steps times (an L2-evicting memset of
+ * flush_bytes before each).  sweep_ms receives the sweep kernel's CUDA-event time
+ * per timed run; info[0..3] = codes swept per run, algorithmic flops per run
+ * (codes x (8 nf - 4): nf complex adds, nf - 1 complex products and one signed
+ * add per code), threads, and nf.  results (optional) receives the permanents.
+ * No reference counterpart.
+ */
+BOSS_API int boss_perm_bench(const double* matrix, int32_t m, const int32_t* input_states,
+                             const int32_t* output_states, int32_t len, int32_t count, int32_t variant,
+                             int32_t n_warmup, int32_t n_steps, int64_t flush_bytes, double* sweep_ms, double* info,
+                             double* results);
 
 /*
  * The random stream theboss's C&C-B samplers draw, replayed on the host without a
@@ -133,6 +152,22 @@ BOSS_API int boss_gccb_predraw(const int32_t* input_state, int32_t m, const doub
 BOSS_API int boss_gccb_sample(const double* matrix, int32_t m, const int32_t* input_state,
                               const double* particle_weights, int32_t n_weights, uint32_t* mt_key, int32_t* mt_pos,
                               int32_t n_samples, int32_t* samples);
+
+/*
+ * Benchmark form of boss_gccb_sample: the random stream is replayed and the
+ * inputs uploaded once, then the captured sampler graph runs n_warmup + n_steps
+ * times with inputs resident in GPU memory.  Before every run a flush_bytes
+ * memset evicts L2.  Per timed run it writes the graph time (step_ms) and the
+ * summed time of its all-minors sweep launches (sweep_ms), both from CUDA events
+ * on the library stream.  info[0..5] = algorithmic flops of the sweeps per run,
+ * H2D bytes and D2H bytes of one boss_gccb_sample call, kernels per run, sweep
+ * launches per run, and the deepest level.  samples (optional) receives the last
+ * run's samples.  No reference counterpart.
+ */
+BOSS_API int boss_gccb_bench(const double* matrix, int32_t m, const int32_t* input_state,
+                             const double* particle_weights, int32_t n_weights, uint32_t* mt_key, int32_t* mt_pos,
+                             int32_t n_samples, int32_t n_warmup, int32_t n_steps, int64_t flush_bytes,
+                             double* step_ms, double* sweep_ms, double* info, int32_t* samples);
 
 /*
  * FP64 throughput of the current GPU: a dependency-free DFMA stream on every SM,

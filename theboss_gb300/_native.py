@@ -49,6 +49,8 @@ def load() -> ctypes.CDLL:
         L.boss_last_error.restype = ctypes.c_char_p
         L.boss_last_error.argtypes = []
         L.boss_abi_version.restype = ctypes.c_int
+        L.boss_select_device.restype = ctypes.c_int
+        L.boss_select_device.argtypes = [ctypes.c_int32]
         L.boss_device_sm_count.restype = ctypes.c_int
         L.boss_device_sm_count.argtypes = [ip]
         for name in ("boss_perm_batch", "boss_submatrices_batch"):
@@ -62,6 +64,12 @@ def load() -> ctypes.CDLL:
         L.boss_gccb_predraw.argtypes = [ip, ctypes.c_int32, dp, ctypes.c_int32, up, ip, ctypes.c_int32, ip, ip, dp]
         L.boss_gccb_sample.restype = ctypes.c_int
         L.boss_gccb_sample.argtypes = [dp, ctypes.c_int32, ip, dp, ctypes.c_int32, up, ip, ctypes.c_int32, ip]
+        L.boss_gccb_bench.restype = ctypes.c_int
+        L.boss_gccb_bench.argtypes = [dp, ctypes.c_int32, ip, dp, ctypes.c_int32, up, ip, ctypes.c_int32,
+                                      ctypes.c_int32, ctypes.c_int32, ctypes.c_int64, dp, dp, dp, ip]
+        L.boss_perm_bench.restype = ctypes.c_int
+        L.boss_perm_bench.argtypes = [dp, ctypes.c_int32, ip, ip, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
+                                      ctypes.c_int32, ctypes.c_int32, ctypes.c_int64, dp, dp, dp]
         _lib = L
         return L
 
@@ -141,6 +149,10 @@ def fp64_peak():
     return float(t[0]), float(ms[0])
 
 
+def select_device(device: int) -> None:
+    check(load().boss_select_device(int(device)))
+
+
 def sm_count() -> int:
     L = load()
     v = np.zeros(1, dtype=np.int32)
@@ -204,3 +216,43 @@ def gccb_sample(U: np.ndarray, input_state, weights, n_samples: int) -> np.ndarr
                              key.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32)), _ip(pos), n_samples, _ip(out)))
     _set_mt(st, key, pos)
     return out
+
+
+# ---------------------------------------------------------------------------
+# Device-timed benchmark entry points
+# ---------------------------------------------------------------------------
+def gccb_bench(U: np.ndarray, input_state, weights, n_samples: int, warmup: int, steps: int,
+               flush_bytes: int = 256 << 20):
+    """Runs the captured sampler graph warmup + steps times on resident inputs.
+    Returns dict(step_ms, sweep_ms, sweep_flops, h2d_bytes, d2h_bytes, kernels, sweeps, levels, samples)."""
+    L = load()
+    inp = np.ascontiguousarray(input_state, dtype=np.int32)
+    m = U.shape[0]
+    w, nw, wp = _weights_arg(weights)
+    st, key, pos = _get_mt()
+    step_ms = np.zeros(steps)
+    sweep_ms = np.zeros(steps)
+    info = np.zeros(8)
+    samples = np.zeros((n_samples, m), dtype=np.int32)
+    check(L.boss_gccb_bench(_dp(U.view(np.float64)), m, _ip(inp), wp, nw,
+                            key.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32)), _ip(pos), n_samples, warmup, steps,
+                            int(flush_bytes), _dp(step_ms), _dp(sweep_ms), _dp(info), _ip(samples)))
+    _set_mt(st, key, pos)
+    return dict(step_ms=step_ms, sweep_ms=sweep_ms, sweep_flops=float(info[0]), h2d_bytes=int(info[1]),
+                d2h_bytes=int(info[2]), kernels=int(info[3]), sweeps=int(info[4]), levels=int(info[5]),
+                samples=samples)
+
+
+def perm_bench(U: np.ndarray, S: np.ndarray, T: np.ndarray, variant: int, warmup: int, steps: int,
+               flush_bytes: int = 256 << 20):
+    """Device-timed sweeps of a batch of permanents sharing one product size.
+    Returns dict(sweep_ms, codes, flops, threads, nf, results)."""
+    L = load()
+    count, n = S.shape
+    sweep_ms = np.zeros(steps)
+    info = np.zeros(4)
+    res = np.zeros(count, dtype=np.complex128)
+    check(L.boss_perm_bench(_dp(U.view(np.float64)), U.shape[0], _ip(S), _ip(T), n, count, variant, warmup, steps,
+                            int(flush_bytes), _dp(sweep_ms), _dp(info), _dp(res.view(np.float64))))
+    return dict(sweep_ms=sweep_ms, codes=float(info[0]), flops=float(info[1]), threads=int(info[2]),
+                nf=int(info[3]), results=res)

@@ -83,144 +83,114 @@ int ensure_pinned(Context* cx, size_t bytes) {
 
 static inline size_t align_up(size_t x, size_t a) { return (x + a - 1) & ~(a - 1); }
 
-static int ilog2_floor(uint64_t x) { return x ? 63 - __builtin_clzll(x) : 0; }
+// A list of sweeps that share one factor count, uploaded and ready to launch.
+struct SweepBatch {
+  int n = 0, nf = 0;
+  bool minors = false;
+  int nd_max = 1;
+  SweepLaunch L;
+  size_t out_elems = 0;
+  double codes = 0.0;  // codes swept per launch
+};
 
-// Cuts sweeps into segments, uploads plans + matrices in one copy, launches the
-// sweep and the reduction, and copies the results back.
-int run_sweeps(Context* cx, const std::vector<HostSweep>& sweeps, bool minors, int nd_max, double2* results_host) {
-  const int n_out = (int)sweeps.size();
-  if (n_out == 0) return kOk;
-  const int chunk_cap = minors ? 12 : 16;
-  uint64_t total_all = 0;
-  for (const auto& s : sweeps) total_all += s.total_codes;
-  const uint64_t resident_warps = (uint64_t)cx->sm_count * 12;
-  const int c_global = ilog2_floor(std::max<uint64_t>(1, total_all / (32ull * resident_warps * 8ull)));
-
-  // pool: D then base of each sweep
-  std::vector<int64_t> mat_off(n_out), base_off(n_out);
-  int64_t pool_n = 0;
-  for (int o = 0; o < n_out; ++o) {
-    mat_off[o] = pool_n;
-    pool_n += (int64_t)sweeps[o].D.size();
-    base_off[o] = pool_n;
-    pool_n += (int64_t)sweeps[o].base.size();
+static int sweeps_prepare(Context* cx, const std::vector<HostSweep>& sweeps, bool minors, int nd_max, SweepBatch& B) {
+  const int n = (int)sweeps.size();
+  B.n = n;
+  B.nf = sweeps[0].nf;
+  B.minors = minors;
+  B.nd_max = nd_max;
+  const SweepOp op = minors ? SweepOp::kMinors : SweepOp::kPerm;
+  std::vector<uint64_t> codes(n);
+  B.codes = 0.0;
+  for (int p = 0; p < n; ++p) {
+    codes[p] = sweeps[p].total_codes;
+    B.codes += (double)codes[p];
   }
-  std::vector<SweepPlan> big, small;
-  int max_nc = 1;
-  for (int o = 0; o < n_out; ++o) {
-    const HostSweep& s = sweeps[o];
-    max_nc = std::max(max_nc, s.nc);
-    SweepPlan p;
-    memset(&p, 0, sizeof(p));
-    p.nd = s.nd;
-    p.nb = s.nb;
-    p.nc = s.nc;
-    p.kind = s.kind;
-    p.parity0 = s.parity0;
-    p.has_base = s.has_base;
-    p.all_pow1 = 1;
-    for (int l = 0; l < s.nc; ++l) {
-      p.pw[l] = s.pw[l];
-      if (s.pw[l] != 1) p.all_pow1 = 0;
-    }
-    for (int i = 0; i < s.nd; ++i) p.mult[i] = s.mult[i];
-    p.mat_off = mat_off[o];
-    p.base_off = base_off[o];
-    p.scale = s.scale;
-    p.out_idx = o;
-    const uint64_t T = s.total_codes;
-    int c = std::min(std::min(c_global, s.nb), chunk_cap);
-    c = std::min(c, ilog2_floor(std::max<uint64_t>(1, T / 32)));
-    c = std::max(c, 0);
-    const uint64_t nch = T >> c;
-    if (nch >= 256 && c >= 3) {
-      const uint64_t a = nch - nch / 8;
-      SweepPlan p1 = p;
-      p1.c = c;
-      p1.code_off = 0;
-      p1.n_chunks = (int64_t)a;
-      big.push_back(p1);
-      SweepPlan p2 = p;
-      p2.c = c - 3;
-      p2.code_off = (int64_t)(a << c);
-      p2.n_chunks = (int64_t)((T - (a << c)) >> (c - 3));
-      small.push_back(p2);
-    } else {
-      SweepPlan p1 = p;
-      p1.c = c;
-      p1.code_off = 0;
-      p1.n_chunks = (int64_t)nch;
-      big.push_back(p1);
-    }
+  std::vector<int64_t> nthr;
+  partition_threads(codes, sweep_resident_threads(B.nf, op, cx->sm_count), nthr);
+  std::vector<SweepProblem> probs(n);
+  int64_t pool_n = 0, threads = 0, parts = 0;
+  for (int p = 0; p < n; ++p) {
+    const HostSweep& h = sweeps[p];
+    SweepProblem& P = probs[p];
+    memset(&P, 0, sizeof(P));
+    P.nd = h.nd;
+    P.nb = h.nb;
+    P.nf = h.nf;
+    P.kind = h.kind;
+    P.parity0 = h.parity0;
+    P.fx = h.fx;
+    P.has_base = h.has_base;
+    P.out_idx = p;
+    P.n_codes = (int64_t)h.total_codes;
+    P.thread_begin = threads;
+    P.n_threads = nthr[p];
+    P.mat_off = pool_n;
+    pool_n += (int64_t)h.D.size();
+    P.base_off = pool_n;
+    pool_n += (int64_t)h.base.size();
+    P.part_off = parts;
+    P.scale = h.scale;
+    for (int i = 0; i < h.nd; ++i) P.mult[i] = h.mult[i];
+    threads += nthr[p];
+    parts += nthr[p] * (minors ? h.nd : 1);
   }
-  std::vector<SweepPlan> plans(big);
-  plans.insert(plans.end(), small.begin(), small.end());
-  const int n_plans = (int)plans.size();
-  int64_t items = 0, parts = 0;
-  for (auto& p : plans) {
-    p.n_items = (p.n_chunks + 31) / 32;
-    p.item_off = items;
-    p.part_off = parts;
-    items += p.n_items;
-    parts += p.n_items * (minors ? p.nd : 1);
-  }
-  std::vector<int32_t> out_plans(n_plans), out_begin(n_out + 1, 0);
-  for (int i = 0; i < n_plans; ++i) out_begin[plans[i].out_idx + 1]++;
-  for (int o = 0; o < n_out; ++o) out_begin[o + 1] += out_begin[o];
-  {
-    std::vector<int32_t> fill(out_begin.begin(), out_begin.end() - 1);
-    for (int i = 0; i < n_plans; ++i) out_plans[fill[plans[i].out_idx]++] = i;
-  }
-
-  // arena: counter | plans | out_plans | out_begin | pool
+  // arena: problems | pool
   size_t off = 0;
-  const size_t o_counter = off; off = align_up(off + 16, 256);
-  const size_t o_plans = off; off = align_up(off + sizeof(SweepPlan) * n_plans, 256);
-  const size_t o_oplans = off; off = align_up(off + sizeof(int32_t) * n_plans, 256);
-  const size_t o_obegin = off; off = align_up(off + sizeof(int32_t) * (n_out + 1), 256);
-  const size_t o_pool = off; off = align_up(off + sizeof(double2) * std::max<int64_t>(pool_n, 1), 256);
+  const size_t o_probs = off; off = align_up(off + sizeof(SweepProblem) * n, 256);
+  const size_t o_pool = off; off = align_up(off + sizeof(longlong2) * std::max<int64_t>(pool_n, 1), 256);
   const size_t arena_bytes = off;
-  const size_t out_elems = (size_t)n_out * (minors ? nd_max : 1);
+  B.out_elems = (size_t)n * (minors ? nd_max : 1);
   int st;
   if ((st = ensure(cx->plans, arena_bytes))) return st;
   if ((st = ensure(cx->partials, sizeof(double2) * std::max<int64_t>(parts, 1)))) return st;
-  if ((st = ensure(cx->out, sizeof(double2) * out_elems))) return st;
-  if ((st = ensure_pinned(cx, std::max(arena_bytes, sizeof(double2) * out_elems)))) return st;
+  if ((st = ensure(cx->out, sizeof(double2) * B.out_elems))) return st;
+  if ((st = ensure_pinned(cx, std::max(arena_bytes, sizeof(double2) * B.out_elems)))) return st;
   char* h = (char*)cx->pinned;
-  memset(h + o_counter, 0, 16);
-  memcpy(h + o_plans, plans.data(), sizeof(SweepPlan) * n_plans);
-  memcpy(h + o_oplans, out_plans.data(), sizeof(int32_t) * n_plans);
-  memcpy(h + o_obegin, out_begin.data(), sizeof(int32_t) * (n_out + 1));
-  double2* hp = (double2*)(h + o_pool);
-  for (int o = 0; o < n_out; ++o) {
-    std::copy(sweeps[o].D.begin(), sweeps[o].D.end(), hp + mat_off[o]);
-    std::copy(sweeps[o].base.begin(), sweeps[o].base.end(), hp + base_off[o]);
+  memcpy(h + o_probs, probs.data(), sizeof(SweepProblem) * n);
+  longlong2* hp = (longlong2*)(h + o_pool);
+  for (int p = 0; p < n; ++p) {
+    std::copy(sweeps[p].D.begin(), sweeps[p].D.end(), hp + probs[p].mat_off);
+    std::copy(sweeps[p].base.begin(), sweeps[p].base.end(), hp + probs[p].base_off);
   }
   char* d = (char*)cx->plans.ptr;
   cudaError_t e = cudaMemcpyAsync(d, h, arena_bytes, cudaMemcpyHostToDevice, cx->stream);
-  if (e != cudaSuccess) return fail_cuda(e, "H2D plans");
-  SweepLaunch L;
-  L.plans = (const SweepPlan*)(d + o_plans);
-  L.n_plans = n_plans;
-  L.pool = (const double2*)(d + o_pool);
-  L.total_items = items;
-  L.counter = (unsigned long long*)(d + o_counter);
-  L.partials = (double2*)cx->partials.ptr;
-  L.max_nc = max_nc;
-  L.grid = (int)std::max<int64_t>(1, std::min<int64_t>((int64_t)cx->sm_count * 8, (items + 3) / 4));
-  e = minors ? launch_minors_sweep(L, cx->stream) : launch_perm_sweep(L, cx->stream);
+  if (e != cudaSuccess) return fail_cuda(e, "H2D sweeps");
+  B.L.probs = (const SweepProblem*)(d + o_probs);
+  B.L.n_probs = n;
+  B.L.pool = (const longlong2*)(d + o_pool);
+  B.L.total_threads = threads;
+  B.L.partials = (double2*)cx->partials.ptr;
+  B.L.grid = (int)((threads + 127) / 128);
+  return kOk;
+}
+
+static int sweeps_launch(Context* cx, const SweepBatch& B, cudaEvent_t after_sweep = nullptr) {
+  cudaError_t e = launch_sweep(B.nf, B.minors ? SweepOp::kMinors : SweepOp::kPerm, B.L, cx->stream);
   if (e != cudaSuccess) return fail_cuda(e, "sweep launch");
-  e = minors ? launch_minors_reduce(L.plans, (const int32_t*)(d + o_oplans), (const int32_t*)(d + o_obegin), n_out,
-                                    L.partials, (double2*)cx->out.ptr, nd_max, cx->stream)
-             : launch_perm_reduce(L.plans, (const int32_t*)(d + o_oplans), (const int32_t*)(d + o_obegin), n_out,
-                                  L.partials, (double2*)cx->out.ptr, cx->stream);
-  if (e != cudaSuccess) return fail_cuda(e, "reduce launch");
-  e = cudaMemcpyAsync(cx->pinned, cx->out.ptr, sizeof(double2) * out_elems, cudaMemcpyDeviceToHost, cx->stream);
+  if (after_sweep) cudaEventRecord(after_sweep, cx->stream);
+  e = B.minors ? launch_minors_reduce(B.L.probs, B.n, B.L.partials, (double2*)cx->out.ptr, B.nd_max, cx->stream)
+               : launch_perm_reduce(B.L.probs, B.n, B.L.partials, (double2*)cx->out.ptr, cx->stream);
+  return e == cudaSuccess ? kOk : fail_cuda(e, "reduce launch");
+}
+
+static int sweeps_collect(Context* cx, const SweepBatch& B, double2* results_host) {
+  cudaError_t e =
+      cudaMemcpyAsync(cx->pinned, cx->out.ptr, sizeof(double2) * B.out_elems, cudaMemcpyDeviceToHost, cx->stream);
   if (e != cudaSuccess) return fail_cuda(e, "D2H results");
   e = cudaStreamSynchronize(cx->stream);
   if (e != cudaSuccess) return fail_cuda(e, "sweep");
-  memcpy(results_host, cx->pinned, sizeof(double2) * out_elems);
+  memcpy(results_host, cx->pinned, sizeof(double2) * B.out_elems);
   return kOk;
+}
+
+int run_sweeps(Context* cx, const std::vector<HostSweep>& sweeps, bool minors, int nd_max, double2* results_host) {
+  if (sweeps.empty()) return kOk;
+  SweepBatch B;
+  int st = sweeps_prepare(cx, sweeps, minors, nd_max, B);
+  if (st) return st;
+  if ((st = sweeps_launch(cx, B))) return st;
+  return sweeps_collect(cx, B, results_host);
 }
 
 // ---------------------------------------------------------------------------
@@ -254,8 +224,21 @@ static Side make_side(const int32_t* occ, int len) {
   return s;
 }
 
-// Fills a sweep that iterates `dig` and multiplies over `col`.  entry(a, l) gives
-// the matrix element between digit mode a and column mode l.
+// Fixed-point fraction bits for sums bounded by `bound` (|s| <= bound): the
+// integer sums stay below 2^61.
+static int choose_fx(double bound) {
+  if (!(bound > 0.0) || !std::isfinite(bound)) return 56;
+  int ex = 0;
+  std::frexp(bound, &ex);  // bound < 2^ex
+  int fx = 61 - ex;
+  return std::max(-900, std::min(fx, 200));
+}
+
+static inline long long to_fixed(double v, int fx) { return std::llrint(std::ldexp(v, fx)); }
+
+// Fills a sweep that iterates `dig` and multiplies over the particles of `col`
+// (a mode occupied p times gives p factors).  entry(a, l) is the matrix element
+// between digit mode a and product mode l.
 template <class F>
 static int fill_sweep(HostSweep& hs, const Side& dig, const Side& col, int kind, bool halve, F entry) {
   int drop = -1;
@@ -263,9 +246,12 @@ static int fill_sweep(HostSweep& hs, const Side& dig, const Side& col, int kind,
   hs.kind = kind;
   hs.nd = (int)dig.modes.size() - (drop >= 0 ? 1 : 0);
   hs.nb = dig.nb - (drop >= 0 ? 1 : 0);
-  hs.nc = (int)col.modes.size();
-  if (hs.nd > kMaxDigits || hs.nc > kMaxCols) {
-    set_error("sweep exceeds 64 distinct iterated modes or 32 distinct product modes");
+  std::vector<int> fmode;
+  for (size_t l = 0; l < col.modes.size(); ++l)
+    for (int k = 0; k < col.mult[l]; ++k) fmode.push_back(col.modes[l]);
+  hs.nf = (int)fmode.size();
+  if (hs.nd > kMaxDigits || hs.nf > kMaxFactors || hs.nf < 1) {
+    set_error("sweep exceeds 64 distinct iterated modes or 32 product-side particles");
     return kErrLimit;
   }
   hs.total_codes = 1;
@@ -282,29 +268,43 @@ static int fill_sweep(HostSweep& hs, const Side& dig, const Side& col, int kind,
     hs.total_codes *= b;
     ++a_out;
   }
-  for (int l = 0; l < hs.nc; ++l) hs.pw[l] = (uint8_t)col.mult[l];
-  hs.D.resize((size_t)hs.nd * hs.nc);
-  const double f = (kind == kGlynn) ? 2.0 : 1.0;
+  // |row sum| <= sum_a mult_a * max component of the entries
+  double bound = 0.0;
+  for (size_t a = 0; a < dig.modes.size(); ++a) {
+    double mx = 0.0;
+    for (int f = 0; f < hs.nf; ++f) {
+      const double2 z = entry(dig.modes[a], fmode[f]);
+      mx = std::max(mx, std::max(std::fabs(z.x), std::fabs(z.y)));
+    }
+    bound += dig.mult[a] * mx;
+  }
+  hs.fx = choose_fx(bound);
+  hs.D.resize((size_t)hs.nd * hs.nf);
+  const long long fsign = (kind == kGlynn) ? -2 : 1;  // Glynn: s = base - 2 sum r U
   a_out = 0;
   for (size_t a = 0; a < dig.modes.size(); ++a) {
     if ((int)a == drop) continue;
-    for (int l = 0; l < hs.nc; ++l) {
-      const double2 z = entry(dig.modes[a], col.modes[l]);
-      hs.D[(size_t)a_out * hs.nc + l] = make_double2(f * z.x, f * z.y);
+    for (int f = 0; f < hs.nf; ++f) {
+      const double2 z = entry(dig.modes[a], fmode[f]);
+      longlong2 v;
+      v.x = fsign * to_fixed(z.x, hs.fx);
+      v.y = fsign * to_fixed(z.y, hs.fx);
+      hs.D[(size_t)a_out * hs.nf + f] = v;
     }
     ++a_out;
   }
   hs.has_base = (kind == kGlynn);
   if (hs.has_base) {
-    hs.base.assign(hs.nc, make_double2(0.0, 0.0));
-    for (int l = 0; l < hs.nc; ++l) {
-      double re = 0.0, im = 0.0;
+    hs.base.assign(hs.nf, longlong2{0, 0});
+    for (int f = 0; f < hs.nf; ++f) {
+      long long re = 0, im = 0;
       for (size_t a = 0; a < dig.modes.size(); ++a) {
-        const double2 z = entry(dig.modes[a], col.modes[l]);
-        re += dig.mult[a] * z.x;
-        im += dig.mult[a] * z.y;
+        const double2 z = entry(dig.modes[a], fmode[f]);
+        re += (long long)dig.mult[a] * to_fixed(z.x, hs.fx);
+        im += (long long)dig.mult[a] * to_fixed(z.y, hs.fx);
       }
-      hs.base[l] = make_double2(re, im);
+      hs.base[f].x = re;
+      hs.base[f].y = im;
     }
     hs.scale = std::ldexp(1.0, -dig.n) * (drop >= 0 ? 2.0 : 1.0);
     hs.parity0 = 0;
@@ -367,7 +367,7 @@ static int plan_permanent(const double* U, int m, const int32_t* S, const int32_
       const uint64_t ci = in.nb ? in.codes / 2 : in.codes;
       const uint64_t co = out.nb ? out.codes / 2 : out.codes;
       int st;
-      if (co < ci || (co == ci && out.modes.size() <= kMaxDigits && in.modes.size() > kMaxCols))
+      if (co < ci)
         st = fill_sweep(hs, out, in, kGlynn, true, entry_out_in);
       else
         st = fill_sweep(hs, in, out, kGlynn, true, entry_in_out);
@@ -409,8 +409,8 @@ static int plan_minors(const double* U, int m, const int32_t* S, const int32_t* 
   }
   for (int i = 0; i < len; ++i) direct[i] = make_double2(0.0, 0.0);
   if (in.n == 0) return kOk;
-  if (in.modes.size() > (size_t)kMaxMinorDigits || out.modes.size() > (size_t)kMaxCols) {
-    set_error("all-minors sweep exceeds 32 distinct input or output modes");
+  if (in.modes.size() > (size_t)kMaxMinorDigits || out.n > kMaxFactors) {
+    set_error("all-minors sweep exceeds 32 distinct input modes or 32 output particles");
     return kErrLimit;
   }
   if (out.modes.empty()) {
@@ -466,6 +466,17 @@ const char* boss_last_error(void) { return g_last_error.c_str(); }
 
 int boss_abi_version(void) { return BOSS_ABI_VERSION; }
 
+int boss_select_device(int32_t device) {
+  std::lock_guard<std::mutex> lk(g_api_mutex);
+  if (g_ctx.ready) {
+    if (g_ctx.device == device) return kOk;
+    set_error("the library's context is already bound to another device");
+    return kErrArg;
+  }
+  cudaError_t e = cudaSetDevice(device);
+  return e == cudaSuccess ? kOk : fail_cuda(e, "cudaSetDevice");
+}
+
 int boss_device_sm_count(int32_t* sm_count) {
   std::lock_guard<std::mutex> lk(g_api_mutex);
   int st;
@@ -482,9 +493,9 @@ int boss_perm_batch(const double* matrix, int32_t m, const int32_t* input_states
     return kErrArg;
   }
   std::lock_guard<std::mutex> lk(g_api_mutex);
-  std::vector<HostSweep> sweeps;
-  std::vector<int> which;
-  sweeps.reserve(count);
+  std::vector<HostSweep> by_nf[kMaxFactors + 1];
+  std::vector<int> which[kMaxFactors + 1];
+  bool any = false;
   for (int k = 0; k < count; ++k) {
     HostSweep hs;
     bool need = false;
@@ -493,23 +504,27 @@ int boss_perm_batch(const double* matrix, int32_t m, const int32_t* input_states
                                   variant, hs, need, v);
     if (st) return st;
     if (need) {
-      sweeps.push_back(std::move(hs));
-      which.push_back(k);
+      which[hs.nf].push_back(k);
+      by_nf[hs.nf].push_back(std::move(hs));
+      any = true;
     } else {
       results[2 * k] = v.x;
       results[2 * k + 1] = v.y;
     }
   }
-  if (sweeps.empty()) return kOk;
+  if (!any) return kOk;
   int st;
   Context* cx = context(&st);
   if (!cx) return st;
-  std::vector<double2> out(sweeps.size());
-  st = run_sweeps(cx, sweeps, false, 1, out.data());
-  if (st) return st;
-  for (size_t a = 0; a < which.size(); ++a) {
-    results[2 * which[a]] = out[a].x;
-    results[2 * which[a] + 1] = out[a].y;
+  for (int nf = 1; nf <= kMaxFactors; ++nf) {
+    if (by_nf[nf].empty()) continue;
+    std::vector<double2> out(by_nf[nf].size());
+    st = run_sweeps(cx, by_nf[nf], false, 1, out.data());
+    if (st) return st;
+    for (size_t a = 0; a < out.size(); ++a) {
+      results[2 * which[nf][a]] = out[a].x;
+      results[2 * which[nf][a] + 1] = out[a].y;
+    }
   }
   return kOk;
 }
@@ -526,9 +541,10 @@ int boss_submatrices_batch(const double* matrix, int32_t m, const int32_t* input
     return kErrArg;
   }
   std::lock_guard<std::mutex> lk(g_api_mutex);
-  std::vector<HostSweep> sweeps;
-  std::vector<int> which;
+  std::vector<HostSweep> by_nf[kMaxFactors + 1];
+  std::vector<int> which[kMaxFactors + 1];
   double2* res = (double2*)results;
+  bool any = false;
   for (int k = 0; k < count; ++k) {
     HostSweep hs;
     bool need = false;
@@ -536,23 +552,98 @@ int boss_submatrices_batch(const double* matrix, int32_t m, const int32_t* input
                                need, res + (size_t)k * len);
     if (st) return st;
     if (need) {
-      sweeps.push_back(std::move(hs));
-      which.push_back(k);
+      which[hs.nf].push_back(k);
+      by_nf[hs.nf].push_back(std::move(hs));
+      any = true;
     }
   }
-  if (sweeps.empty()) return kOk;
+  if (!any) return kOk;
   int st;
   Context* cx = context(&st);
   if (!cx) return st;
   const int nd_max = kMaxMinorDigits;
-  std::vector<double2> out(sweeps.size() * nd_max);
-  st = run_sweeps(cx, sweeps, true, nd_max, out.data());
-  if (st) return st;
-  for (size_t a = 0; a < which.size(); ++a) {
-    const HostSweep& hs = sweeps[a];
-    double2* row = res + (size_t)which[a] * len;
-    for (int d = 0; d < hs.nd; ++d) row[hs.digit_mode[d]] = out[a * nd_max + d];
+  for (int nf = 1; nf <= kMaxFactors; ++nf) {
+    if (by_nf[nf].empty()) continue;
+    std::vector<double2> out(by_nf[nf].size() * nd_max);
+    st = run_sweeps(cx, by_nf[nf], true, nd_max, out.data());
+    if (st) return st;
+    for (size_t a = 0; a < by_nf[nf].size(); ++a) {
+      const HostSweep& hs = by_nf[nf][a];
+      double2* row = res + (size_t)which[nf][a] * len;
+      for (int d = 0; d < hs.nd; ++d) row[hs.digit_mode[d]] = out[a * nd_max + d];
+    }
   }
+  return kOk;
+}
+
+int boss_perm_bench(const double* matrix, int32_t m, const int32_t* input_states, const int32_t* output_states,
+                    int32_t len, int32_t count, int32_t variant, int32_t n_warmup, int32_t n_steps,
+                    int64_t flush_bytes, double* sweep_ms, double* info, double* results) {
+  if (!matrix || !input_states || !output_states || m <= 0 || count <= 0 || n_steps <= 0 || !sweep_ms || !info) {
+    set_error("null pointer or bad size");
+    return kErrArg;
+  }
+  std::lock_guard<std::mutex> lk(g_api_mutex);
+  std::vector<HostSweep> sweeps;
+  double flops = 0.0;
+  for (int k = 0; k < count; ++k) {
+    HostSweep hs;
+    bool need = false;
+    double2 v;
+    const int st = plan_permanent(matrix, m, input_states + (size_t)k * len, output_states + (size_t)k * len, len,
+                                  variant, hs, need, v);
+    if (st) return st;
+    if (!need) {
+      set_error("benchmark permanents must need a sweep");
+      return kErrArg;
+    }
+    if (!sweeps.empty() && hs.nf != sweeps[0].nf) {
+      set_error("benchmark permanents must share one product size");
+      return kErrArg;
+    }
+    // per code: nf complex adds, nf - 1 complex products, one signed complex add
+    flops += (double)hs.total_codes * (8.0 * hs.nf - 4.0);
+    sweeps.push_back(std::move(hs));
+  }
+  int st;
+  Context* cx = context(&st);
+  if (!cx) return st;
+  SweepBatch B;
+  if ((st = sweeps_prepare(cx, sweeps, false, 1, B))) return st;
+  if (flush_bytes > 0 && (st = ensure(cx->misc, (size_t)flush_bytes))) return st;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  cudaError_t e = cudaSuccess;
+  for (int it = 0; it < n_warmup + n_steps && !st; ++it) {
+    if (flush_bytes > 0) e = cudaMemsetAsync(cx->misc.ptr, it & 0xff, (size_t)flush_bytes, cx->stream);
+    if (e != cudaSuccess) break;
+    cudaEventRecord(e0, cx->stream);
+    st = sweeps_launch(cx, B, e1);
+    if (st) break;
+    e = cudaEventSynchronize(e1);
+    if (e != cudaSuccess) break;
+    if (it >= n_warmup) {
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, e0, e1);
+      sweep_ms[it - n_warmup] = ms;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (!st && e != cudaSuccess) st = fail_cuda(e, "perm bench");
+  if (st) return st;
+  std::vector<double2> out(B.out_elems);
+  if ((st = sweeps_collect(cx, B, out.data()))) return st;
+  if (results)
+    for (int k = 0; k < count; ++k) {
+      results[2 * k] = out[k].x;
+      results[2 * k + 1] = out[k].y;
+    }
+  info[0] = B.codes;
+  info[1] = flops;
+  info[2] = (double)B.L.total_threads;
+  info[3] = (double)B.nf;
   return kOk;
 }
 

@@ -20,6 +20,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <cmath>
 #include <mutex>
 #include <numeric>
 #include <vector>
@@ -132,31 +133,32 @@ static int predraw(const int32_t* input_state, int m, const double* weights, int
 // Device side
 // ---------------------------------------------------------------------------
 struct LevelSample {  // host-computed layout of one sample's sweep at one level
-  int64_t item_off;
+  int64_t n_codes;
+  int64_t thread_begin;
+  int64_t n_threads;
   int64_t part_off;
-  int64_t n_chunks;
   int64_t pool_off;
-  int32_t n_items;
-  int32_t c;
 };
 
 struct FinalizeArgs {
-  int k;                 // level (number of input particles of this step)
-  int A;                 // active samples at this level
-  int A_next;            // active samples at level k + 1
+  int k;       // level = input particles of this step
+  int A;       // active samples at this level
+  int A_next;  // active samples at level k + 1
   int m;
-  int n;                 // add/u row stride
-  const double2* U;
-  uint8_t* S;            // [sample][m] current input occupations
-  uint8_t* T;            // [sample][m] output occupations
-  const uint8_t* add;    // [sample][n] popped input modes
-  const double* uni;     // [sample][n] uniforms
-  const SweepPlan* plans_cur;
+  int n;       // row stride of add / uni
+  int fx;      // fixed-point fraction bits of the sweep rows
+  const double2* U;       // m x m
+  const longlong2* Ufx;   // m x m, U * 2^fx rounded
+  uint8_t* S;             // [sample][m] current input occupations
+  uint8_t* T;             // [sample][m] output occupations
+  const uint8_t* add;     // [sample][n] popped input modes
+  const double* uni;      // [sample][n] uniforms
+  const SweepProblem* probs_cur;
   const uint8_t* dmode_cur;  // [sample][32]
   const double2* partials;
-  SweepPlan* plans_next;
+  SweepProblem* probs_next;
   uint8_t* dmode_next;
-  double2* pool_next;
+  longlong2* pool_next;
   const LevelSample* next_tab;  // A_next entries
   int* err;
 };
@@ -167,8 +169,7 @@ __global__ void __launch_bounds__(kFinWarps * 32) gccb_finalize_kernel(FinalizeA
   __shared__ double2 sub_s[kFinWarps][32];
   __shared__ uint8_t dm_s[kFinWarps][32];
   __shared__ uint8_t mult_s[kFinWarps][32];
-  __shared__ uint8_t cm_s[kFinWarps][32];
-  __shared__ uint8_t pw_s[kFinWarps][32];
+  __shared__ uint8_t fm_s[kFinWarps][32];
   __shared__ double pmf_s[kFinWarps][256];
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int j = blockIdx.x * kFinWarps + w;
@@ -189,12 +190,12 @@ __global__ void __launch_bounds__(kFinWarps * 32) gccb_finalize_kernel(FinalizeA
     }
     nd = 1;
   } else {
-    const SweepPlan& P = a.plans_cur[j];
+    const SweepProblem& P = a.probs_cur[j];
     nd = P.nd;
     if (lane < nd) {
       double sx = 0.0, sy = 0.0;
-      for (int it = 0; it < P.n_items; ++it) {
-        const double2 v = a.partials[P.part_off + (int64_t)it * nd + lane];
+      for (int64_t q = 0; q < P.n_threads; ++q) {
+        const double2 v = a.partials[P.part_off + q * nd + lane];
         sx += v.x;
         sy += v.y;
       }
@@ -204,15 +205,15 @@ __global__ void __launch_bounds__(kFinWarps * 32) gccb_finalize_kernel(FinalizeA
     }
   }
   __syncwarp();
-  // Laplace expansion: perm(T + e_o) = sum_i S_i sub_i U[o][i]
+  // Laplace expansion perm(T + e_o) = sum_i S_i sub_i U[o][i]
   // (generalized_cliffords_b_simulation_strategy.py:82-89), then |.|^2.
   for (int o = lane; o < m; o += 32) {
     double re = 0.0, im = 0.0;
     for (int d = 0; d < nd; ++d) {
-      const double2 s = sub_s[w][d];
+      const double2 sv = sub_s[w][d];
       const double mu = (double)mult_s[w][d];
       const double2 u = a.U[(size_t)o * m + dm_s[w][d]];
-      const double cr = mu * s.x, ci = mu * s.y;
+      const double cr = mu * sv.x, ci = mu * sv.y;
       re = fma(cr, u.x, fma(-ci, u.y, re));
       im = fma(cr, u.y, fma(ci, u.x, im));
     }
@@ -251,18 +252,18 @@ __global__ void __launch_bounds__(kFinWarps * 32) gccb_finalize_kernel(FinalizeA
   __syncwarp();
   if (j >= a.A_next) return;
 
-  // ---- plan of level k + 1 ----
+  // ---- the all-minors sweep of level k + 1 ----
   if (lane == 0) {
     const int mode = a.add[(size_t)j * a.n + a.k];
     S[mode] = (uint8_t)(S[mode] + 1);
   }
   __syncwarp();
-  int nb = 0, nmul = 0, nc = 0, tsum = 0, all1 = 1;
+  int nb = 0, nmul = 0, nf = 0;
   for (int base = 0; base < m; base += 32) {
     const int mode = base + lane;
-    const int s = (mode < m) ? S[mode] : 0;
-    const unsigned b1 = __ballot_sync(0xffffffffu, s == 1);
-    if (s == 1) {
+    const int sv = (mode < m) ? S[mode] : 0;
+    const unsigned b1 = __ballot_sync(0xffffffffu, sv == 1);
+    if (sv == 1) {
       const int pos = nb + __popc(b1 & ((1u << lane) - 1u));
       dm_s[w][pos] = (uint8_t)mode;
       mult_s[w][pos] = 1;
@@ -271,137 +272,144 @@ __global__ void __launch_bounds__(kFinWarps * 32) gccb_finalize_kernel(FinalizeA
   }
   for (int base = 0; base < m; base += 32) {
     const int mode = base + lane;
-    const int s = (mode < m) ? S[mode] : 0;
-    const unsigned bm = __ballot_sync(0xffffffffu, s > 1);
-    if (s > 1) {
+    const int sv = (mode < m) ? S[mode] : 0;
+    const unsigned bm = __ballot_sync(0xffffffffu, sv > 1);
+    if (sv > 1) {
       const int pos = nb + nmul + __popc(bm & ((1u << lane) - 1u));
       dm_s[w][pos] = (uint8_t)mode;
-      mult_s[w][pos] = (uint8_t)s;
+      mult_s[w][pos] = (uint8_t)sv;
     }
     nmul += __popc(bm);
   }
+  // factors: every output particle (a mode occupied p times gives p factors)
   for (int base = 0; base < m; base += 32) {
     const int mode = base + lane;
-    const int t = (mode < m) ? T[mode] : 0;
-    const unsigned bt = __ballot_sync(0xffffffffu, t > 0);
-    if (t > 0) {
-      const int pos = nc + __popc(bt & ((1u << lane) - 1u));
-      cm_s[w][pos] = (uint8_t)mode;
-      pw_s[w][pos] = (uint8_t)t;
+    const int tv = (mode < m) ? T[mode] : 0;
+    int incl = tv;
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, incl, off);
+      if (lane >= off) incl += y;
     }
-    nc += __popc(bt);
-    tsum += __reduce_add_sync(0xffffffffu, (unsigned)t);
-    all1 &= __all_sync(0xffffffffu, t <= 1);
+    for (int q = 0; q < tv; ++q) fm_s[w][nf + incl - tv + q] = (uint8_t)mode;
+    nf += __shfl_sync(0xffffffffu, incl, 31);
   }
   __syncwarp();
   nd = nb + nmul;
   const LevelSample& ls = a.next_tab[j];
-  double2* D = a.pool_next + ls.pool_off;
-  for (int e = lane; e < nd * nc; e += 32) {
-    const int d = e / nc, l = e - d * nc;
-    D[e] = a.U[(size_t)cm_s[w][l] * m + dm_s[w][d]];
+  longlong2* D = a.pool_next + ls.pool_off;
+  for (int e = lane; e < nd * nf; e += 32) {
+    const int d = e / nf, f = e - d * nf;
+    D[e] = a.Ufx[(size_t)fm_s[w][f] * m + dm_s[w][d]];  // Ryser rows: U[out][in]
   }
-  SweepPlan& P = a.plans_next[j];
-  if (lane < 32) {
-    P.mult[lane] = (lane < nd) ? mult_s[w][lane] : 0;
-    P.mult[lane + 32] = 0;
-    P.pw[lane] = (lane < nc) ? pw_s[w][lane] : 0;
-    a.dmode_next[(size_t)j * 32 + lane] = (lane < nd) ? dm_s[w][lane] : 0;
-  }
+  SweepProblem& P = a.probs_next[j];
+  P.mult[lane] = (lane < nd) ? mult_s[w][lane] : 0;
+  P.mult[lane + 32] = 0;
+  a.dmode_next[(size_t)j * 32 + lane] = (lane < nd) ? dm_s[w][lane] : 0;
   if (lane == 0) {
     P.nd = nd;
     P.nb = nb;
-    P.c = ls.c;
-    P.nc = nc;
+    P.nf = nf;
     P.kind = kRyser;
-    P.parity0 = tsum & 1;  // multiplier (-1)^sum(T), bs_submatrices_permanent_calculator_base.py:185
+    P.parity0 = nf & 1;  // multiplier (-1)^sum(T), bs_submatrices_permanent_calculator_base.py:185
+    P.fx = a.fx;
     P.has_base = 0;
-    P.all_pow1 = all1;
-    P.n_chunks = ls.n_chunks;
-    P.item_off = ls.item_off;
-    P.n_items = ls.n_items;
+    P.out_idx = j;
+    P.n_codes = ls.n_codes;
+    P.thread_begin = ls.thread_begin;
+    P.n_threads = ls.n_threads;
     P.mat_off = ls.pool_off;
     P.base_off = 0;
     P.part_off = ls.part_off;
-    P.code_off = 0;
-    P.out_idx = j;
-    P.reserved = 0;
     P.scale = 1.0;
+    P.reserved = 0.0;
   }
 }
 
 // ---------------------------------------------------------------------------
-// Host orchestration
+// Host orchestration: prepare (schedule, upload, capture) / launch / collect.
 // ---------------------------------------------------------------------------
-struct GccbGraphCache {
-  cudaGraphExec_t exec = nullptr;
+struct GccbRun {
+  int N = 0, m = 0, n = 0, Lmax = 0;
+  std::vector<int> order;
+  size_t h2d_bytes = 0, d2h_bytes = 0;
+  uint8_t* dT = nullptr;
+  int* derr = nullptr;
+  int kernels = 0, sweeps = 0;
+  double sweep_flops = 0.0;  // algorithmic flops of all sweep launches
+  std::vector<cudaEvent_t> ev;  // 2 per sweep level when timing
 };
-static GccbGraphCache g_graph;
+static cudaGraphExec_t g_gccb_exec = nullptr;
 
-static int run_gccb(Context* cx, const double* matrix, int m, int n, int N, const std::vector<int32_t>& L,
-                    const std::vector<uint8_t>& add, const std::vector<double>& uni, int32_t* samples_out) {
-  if (N == 0) return kOk;
-  std::vector<int> order(N);
-  std::iota(order.begin(), order.end(), 0);
-  std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return L[x] > L[y]; });
+static void destroy_events(GccbRun& R) {
+  for (auto e : R.ev) cudaEventDestroy(e);
+  R.ev.clear();
+}
+
+static int gccb_prepare(Context* cx, const double* matrix, int m, int n, int N, const std::vector<int32_t>& L,
+                        const std::vector<uint8_t>& add, const std::vector<double>& uni, bool timing, GccbRun& R) {
+  R.N = N;
+  R.m = m;
+  R.n = n;
+  R.order.resize(N);
+  std::iota(R.order.begin(), R.order.end(), 0);
+  std::stable_sort(R.order.begin(), R.order.end(), [&](int x, int y) { return L[x] > L[y]; });
+  const std::vector<int>& order = R.order;
   const int Lmax = L[order[0]];
+  R.Lmax = Lmax;
   std::vector<int> A(Lmax + 2, 0);
   for (int s = 0; s < N; ++s)
     for (int k = 1; k <= L[s]; ++k) A[k]++;
+  // fixed point: |row sum| <= n * max |component of U|
+  double umax = 0.0;
+  for (size_t i = 0; i < (size_t)2 * m * m; ++i) umax = std::max(umax, std::fabs(matrix[i]));
+  int ex = 0;
+  std::frexp(std::max(umax, 1e-300) * std::max(n, 1), &ex);
+  const int fx = std::max(-900, std::min(61 - ex, 200));
   // Per-level layout (levels 2..Lmax need sweeps).
-  const int64_t resident_warps = (int64_t)cx->sm_count * 12;
   std::vector<std::vector<LevelSample>> tab(Lmax + 2);
-  std::vector<int64_t> lvl_items(Lmax + 2, 0), lvl_parts(Lmax + 2, 0), lvl_pool(Lmax + 2, 0);
-  std::vector<int> lvl_c(Lmax + 2, 0);
+  std::vector<int64_t> lvl_threads(Lmax + 2, 0), lvl_parts(Lmax + 2, 0), lvl_pool(Lmax + 2, 0);
   std::vector<uint8_t> occ(m);
+  R.sweep_flops = 0.0;
   for (int k = 2; k <= Lmax; ++k) {
     const int Ak = A[k];
     std::vector<uint64_t> codes(Ak);
-    std::vector<int> ndv(Ak), nbv(Ak);
-    uint64_t total = 0;
-    int min_nb = 64;
+    std::vector<int> ndv(Ak);
     for (int jj = 0; jj < Ak; ++jj) {
       const int s = order[jj];
       std::fill(occ.begin(), occ.end(), 0);
       for (int q = 0; q < k; ++q) occ[add[(size_t)s * n + q]]++;
       uint64_t c = 1;
-      int nd = 0, nb = 0;
+      int nd = 0;
       for (int i = 0; i < m; ++i)
         if (occ[i]) {
           ++nd;
-          if (occ[i] == 1) ++nb;
           c *= (uint64_t)occ[i] + 1;
         }
       codes[jj] = c;
       ndv[jj] = nd;
-      nbv[jj] = nb;
-      total += c;
-      min_nb = std::min(min_nb, nb);
+      // algorithmic flops of theboss's all-minors sweep per code: (k-1) complex
+      // adds, (k-2) complex products, one sign, k/2 real-weighted adds = 9k - 12
+      R.sweep_flops += (double)c * (9.0 * k - 12.0);
     }
-    int c = 0;
-    {
-      const uint64_t per = total / (uint64_t)(32 * 8 * resident_warps);
-      while (c < 12 && (1ull << (c + 1)) <= per) ++c;
-      c = std::min(c, min_nb);
-    }
-    lvl_c[k] = c;
+    std::vector<int64_t> nthr;
+    partition_threads(codes, sweep_resident_threads(k - 1, SweepOp::kMinors, cx->sm_count), nthr);
     auto& t = tab[k];
     t.resize(Ak);
-    int64_t items = 0, parts = 0, pool = 0;
+    int64_t threads = 0, parts = 0, pool = 0;
     for (int jj = 0; jj < Ak; ++jj) {
       LevelSample ls;
-      ls.c = c;
-      ls.n_chunks = (int64_t)(codes[jj] >> c);
-      ls.n_items = (int32_t)((ls.n_chunks + 31) / 32);
-      ls.item_off = items;
+      ls.n_codes = (int64_t)codes[jj];
+      ls.thread_begin = threads;
+      ls.n_threads = nthr[jj];
       ls.part_off = parts;
       ls.pool_off = pool;
-      items += ls.n_items;
-      parts += (int64_t)ls.n_items * ndv[jj];
+      threads += nthr[jj];
+      parts += nthr[jj] * ndv[jj];
       pool += (int64_t)ndv[jj] * (k - 1);
       t[jj] = ls;
     }
-    lvl_items[k] = items;
+    lvl_threads[k] = threads;
     lvl_parts[k] = parts;
     lvl_pool[k] = pool;
   }
@@ -410,25 +418,27 @@ static int run_gccb(Context* cx, const double* matrix, int m, int n, int N, cons
     max_parts = std::max(max_parts, lvl_parts[k]);
     max_pool = std::max(max_pool, lvl_pool[k]);
   }
-  // Arena (one H2D copy): counters | err | level tables | add | uniforms | U
+  // Arena (one H2D copy): err | level tables | add | uniforms | U | U fixed-point
   auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
   size_t off = 0;
-  const size_t o_cnt = off; off = al(off + sizeof(unsigned long long) * (Lmax + 2));
   const size_t o_err = off; off = al(off + sizeof(int));
   std::vector<size_t> o_tab(Lmax + 2, 0);
   for (int k = 2; k <= Lmax; ++k) { o_tab[k] = off; off = al(off + sizeof(LevelSample) * tab[k].size()); }
   const size_t o_add = off; off = al(off + (size_t)N * n);
   const size_t o_uni = off; off = al(off + sizeof(double) * (size_t)N * n);
   const size_t o_U = off; off = al(off + sizeof(double2) * (size_t)m * m);
+  const size_t o_Ufx = off; off = al(off + sizeof(longlong2) * (size_t)m * m);
   const size_t arena = off;
+  R.h2d_bytes = arena;
+  R.d2h_bytes = (size_t)N * m + sizeof(int);
   int st;
   if ((st = ensure(cx->gccb[0], arena))) return st;
-  if ((st = ensure(cx->gccb[1], (size_t)N * m * 2))) return st;                       // S | T
-  if ((st = ensure(cx->gccb[2], sizeof(SweepPlan) * (size_t)A[1] * 2 + 512))) return st;  // plans x2
-  if ((st = ensure(cx->gccb[3], (size_t)A[1] * 32 * 2))) return st;                   // dmode x2
-  if ((st = ensure(cx->gccb[4], sizeof(double2) * (size_t)max_pool * 2 + 512))) return st;  // pool x2
-  if ((st = ensure(cx->gccb[5], sizeof(double2) * (size_t)max_parts))) return st;    // partials
-  if ((st = ensure_pinned(cx, std::max(arena, (size_t)N * m)))) return st;
+  if ((st = ensure(cx->gccb[1], (size_t)N * m * 2))) return st;                              // S | T
+  if ((st = ensure(cx->gccb[2], sizeof(SweepProblem) * (size_t)A[1] * 2 + 512))) return st;  // problems x2
+  if ((st = ensure(cx->gccb[3], (size_t)A[1] * 32 * 2))) return st;                          // digit modes x2
+  if ((st = ensure(cx->gccb[4], sizeof(longlong2) * (size_t)max_pool * 2 + 512))) return st;  // rows x2
+  if ((st = ensure(cx->gccb[5], sizeof(double2) * (size_t)max_parts))) return st;            // partials
+  if ((st = ensure_pinned(cx, std::max(arena, al((size_t)N * m) + 256)))) return st;
   char* h = (char*)cx->pinned;
   memset(h, 0, o_add);
   for (int k = 2; k <= Lmax; ++k) memcpy(h + o_tab[k], tab[k].data(), sizeof(LevelSample) * tab[k].size());
@@ -439,36 +449,52 @@ static int run_gccb(Context* cx, const double* matrix, int m, int n, int N, cons
     memcpy(huni + (size_t)jj * n, &uni[(size_t)order[jj] * n], sizeof(double) * n);
   }
   memcpy(h + o_U, matrix, sizeof(double2) * (size_t)m * m);
+  longlong2* hfx = (longlong2*)(h + o_Ufx);
+  for (size_t i = 0; i < (size_t)m * m; ++i) {
+    hfx[i].x = std::llrint(std::ldexp(matrix[2 * i], fx));
+    hfx[i].y = std::llrint(std::ldexp(matrix[2 * i + 1], fx));
+  }
   char* d = (char*)cx->gccb[0].ptr;
   uint8_t* dS = (uint8_t*)cx->gccb[1].ptr;
-  uint8_t* dT = dS + (size_t)N * m;
-  SweepPlan* plans[2] = {(SweepPlan*)cx->gccb[2].ptr, (SweepPlan*)cx->gccb[2].ptr + A[1]};
+  R.dT = dS + (size_t)N * m;
+  R.derr = (int*)(d + o_err);
+  SweepProblem* probs[2] = {(SweepProblem*)cx->gccb[2].ptr, (SweepProblem*)cx->gccb[2].ptr + A[1]};
   uint8_t* dmode[2] = {(uint8_t*)cx->gccb[3].ptr, (uint8_t*)cx->gccb[3].ptr + (size_t)A[1] * 32};
-  double2* pool[2] = {(double2*)cx->gccb[4].ptr, (double2*)cx->gccb[4].ptr + max_pool};
+  longlong2* pool[2] = {(longlong2*)cx->gccb[4].ptr, (longlong2*)cx->gccb[4].ptr + max_pool};
   double2* partials = (double2*)cx->gccb[5].ptr;
   cudaStream_t s = cx->stream;
   cudaError_t e = cudaMemcpyAsync(d, h, arena, cudaMemcpyHostToDevice, s);
   if (e != cudaSuccess) return fail_cuda(e, "H2D sampler arena");
-
+  destroy_events(R);
+  if (timing) {
+    R.ev.resize(2 * (size_t)std::max(Lmax - 1, 0));
+    for (auto& ev : R.ev)
+      if ((e = cudaEventCreate(&ev)) != cudaSuccess) return fail_cuda(e, "event create");
+  }
   // Capture the level loop into one graph.
+  cudaGetLastError();
   cudaGraph_t graph = nullptr;
   e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
   if (e != cudaSuccess) return fail_cuda(e, "begin capture");
+  R.kernels = 0;
+  R.sweeps = 0;
   cudaError_t le = cudaMemsetAsync(dS, 0, (size_t)N * m * 2, s);
   for (int k = 1; k <= Lmax && le == cudaSuccess; ++k) {
     const int cur = k & 1, nxt = (k + 1) & 1;
     if (k >= 2) {
       SweepLaunch SL;
-      SL.plans = plans[cur];
-      SL.n_plans = A[k];
+      SL.probs = probs[cur];
+      SL.n_probs = A[k];
       SL.pool = pool[cur];
-      SL.total_items = lvl_items[k];
-      SL.counter = (unsigned long long*)(d + o_cnt) + k;
+      SL.total_threads = lvl_threads[k];
       SL.partials = partials;
-      SL.max_nc = k - 1;
-      SL.grid = (int)std::max<int64_t>(1, std::min<int64_t>((int64_t)cx->sm_count * 8, (lvl_items[k] + 3) / 4));
-      le = launch_minors_sweep(SL, s);
+      SL.grid = (int)((lvl_threads[k] + 127) / 128);
+      if (timing) le = cudaEventRecordWithFlags(R.ev[2 * (k - 2)], s, cudaEventRecordExternal);
+      if (le == cudaSuccess) le = launch_sweep(k - 1, SweepOp::kMinors, SL, s);
+      if (timing && le == cudaSuccess) le = cudaEventRecordWithFlags(R.ev[2 * (k - 2) + 1], s, cudaEventRecordExternal);
       if (le != cudaSuccess) break;
+      ++R.kernels;
+      ++R.sweeps;
     }
     FinalizeArgs fa;
     fa.k = k;
@@ -476,21 +502,24 @@ static int run_gccb(Context* cx, const double* matrix, int m, int n, int N, cons
     fa.A_next = (k < Lmax) ? A[k + 1] : 0;
     fa.m = m;
     fa.n = n;
+    fa.fx = fx;
     fa.U = (const double2*)(d + o_U);
+    fa.Ufx = (const longlong2*)(d + o_Ufx);
     fa.S = dS;
-    fa.T = dT;
+    fa.T = R.dT;
     fa.add = (const uint8_t*)(d + o_add);
     fa.uni = (const double*)(d + o_uni);
-    fa.plans_cur = plans[cur];
+    fa.probs_cur = probs[cur];
     fa.dmode_cur = dmode[cur];
     fa.partials = partials;
-    fa.plans_next = plans[nxt];
+    fa.probs_next = probs[nxt];
     fa.dmode_next = dmode[nxt];
     fa.pool_next = pool[nxt];
     fa.next_tab = (k < Lmax) ? (const LevelSample*)(d + o_tab[k + 1]) : nullptr;
-    fa.err = (int*)(d + o_err);
+    fa.err = R.derr;
     gccb_finalize_kernel<<<(A[k] + kFinWarps - 1) / kFinWarps, kFinWarps * 32, 0, s>>>(fa);
     le = cudaGetLastError();
+    ++R.kernels;
   }
   e = cudaStreamEndCapture(s, &graph);
   if (le != cudaSuccess) {
@@ -499,43 +528,64 @@ static int run_gccb(Context* cx, const double* matrix, int m, int n, int N, cons
   }
   if (e != cudaSuccess) return fail_cuda(e, "end capture");
   bool updated = false;
-  if (g_graph.exec) {
+  if (g_gccb_exec) {
     cudaGraphExecUpdateResultInfo info;
-    if (cudaGraphExecUpdate(g_graph.exec, graph, &info) == cudaSuccess) updated = true;
-    else {
+    if (cudaGraphExecUpdate(g_gccb_exec, graph, &info) == cudaSuccess) {
+      updated = true;
+    } else {
       cudaGetLastError();
-      cudaGraphExecDestroy(g_graph.exec);
-      g_graph.exec = nullptr;
+      cudaGraphExecDestroy(g_gccb_exec);
+      g_gccb_exec = nullptr;
     }
   }
   if (!updated) {
-    e = cudaGraphInstantiate(&g_graph.exec, graph, 0);
+    e = cudaGraphInstantiate(&g_gccb_exec, graph, 0);
     if (e != cudaSuccess) {
       cudaGraphDestroy(graph);
-      g_graph.exec = nullptr;
+      g_gccb_exec = nullptr;
       return fail_cuda(e, "graph instantiate");
     }
   }
   cudaGraphDestroy(graph);
-  e = cudaGraphLaunch(g_graph.exec, s);
-  if (e != cudaSuccess) return fail_cuda(e, "graph launch");
-  e = cudaMemcpyAsync(h, dT, (size_t)N * m, cudaMemcpyDeviceToHost, s);
+  return kOk;
+}
+
+static int gccb_launch(Context* cx) {
+  cudaError_t e = cudaGraphLaunch(g_gccb_exec, cx->stream);
+  return e == cudaSuccess ? kOk : fail_cuda(e, "graph launch");
+}
+
+static int gccb_collect(Context* cx, GccbRun& R, int32_t* samples_out) {
+  cudaStream_t s = cx->stream;
+  cudaError_t e = cudaMemcpyAsync(cx->pinned, R.dT, (size_t)R.N * R.m, cudaMemcpyDeviceToHost, s);
   if (e != cudaSuccess) return fail_cuda(e, "D2H samples");
-  int herr = 0;
-  e = cudaMemcpyAsync(&herr, d + o_err, sizeof(int), cudaMemcpyDeviceToHost, s);
+  int* herr = (int*)((char*)cx->pinned + (((size_t)R.N * R.m + 255) & ~(size_t)255));
+  e = cudaMemcpyAsync(herr, R.derr, sizeof(int), cudaMemcpyDeviceToHost, s);
   if (e != cudaSuccess) return fail_cuda(e, "D2H status");
   e = cudaStreamSynchronize(s);
   if (e != cudaSuccess) return fail_cuda(e, "sampler");
-  if (herr) {
+  if (*herr) {
     set_error("probabilities contain NaN (a pmf summed to zero or a non-finite value)");
     return kErrPmf;
   }
-  const uint8_t* hT = (const uint8_t*)h;
-  for (int jj = 0; jj < N; ++jj) {
-    int32_t* row = samples_out + (size_t)order[jj] * m;
-    for (int i = 0; i < m; ++i) row[i] = hT[(size_t)jj * m + i];
+  if (samples_out) {
+    const uint8_t* hT = (const uint8_t*)cx->pinned;
+    for (int jj = 0; jj < R.N; ++jj) {
+      int32_t* row = samples_out + (size_t)R.order[jj] * R.m;
+      for (int i = 0; i < R.m; ++i) row[i] = hT[(size_t)jj * R.m + i];
+    }
   }
   return kOk;
+}
+
+static int run_gccb(Context* cx, const double* matrix, int m, int n, int N, const std::vector<int32_t>& L,
+                    const std::vector<uint8_t>& add, const std::vector<double>& uni, int32_t* samples_out) {
+  if (N == 0) return kOk;
+  GccbRun R;
+  int st = gccb_prepare(cx, matrix, m, n, N, L, add, uni, false, R);
+  if (st) return st;
+  if ((st = gccb_launch(cx))) return st;
+  return gccb_collect(cx, R, samples_out);
 }
 
 }  // namespace boss
@@ -614,6 +664,85 @@ int boss_gccb_sample(const double* matrix, int32_t m, const int32_t* input_state
     st = run_gccb(cx, matrix, m, std::max(n, 1), n_samples, L, add, u, samples);
     if (st) return st;
   }
+  memcpy(mt_key, mt.key, sizeof(mt.key));
+  *mt_pos = mt.pos;
+  return kOk;
+}
+
+int boss_gccb_bench(const double* matrix, int32_t m, const int32_t* input_state, const double* particle_weights,
+                    int32_t n_weights, uint32_t* mt_key, int32_t* mt_pos, int32_t n_samples, int32_t n_warmup,
+                    int32_t n_steps, int64_t flush_bytes, double* step_ms, double* sweep_ms, double* info,
+                    int32_t* samples) {
+  if (!matrix || !input_state || m <= 0 || n_samples <= 0 || n_steps <= 0 || !step_ms || !sweep_ms || !info) {
+    set_error("null pointer or bad size");
+    return kErrArg;
+  }
+  if (m > 256) {
+    set_error("the batched sampler supports at most 256 modes");
+    return kErrLimit;
+  }
+  std::lock_guard<std::mutex> lk(g_api_mutex);
+  MT19937 mt;
+  int st = load_mt(mt, mt_key, mt_pos);
+  if (st) return st;
+  std::vector<int32_t> L;
+  std::vector<uint8_t> add;
+  std::vector<double> u;
+  int n = 0;
+  st = predraw(input_state, m, particle_weights, particle_weights ? n_weights : 0, mt, n_samples, L, add, u, n);
+  if (st) return st;
+  if (n > kMaxMinorDigits || n < 1) {
+    set_error("the batched sampler benchmark needs 1..32 input particles");
+    return kErrLimit;
+  }
+  if (!std::any_of(L.begin(), L.end(), [](int32_t l) { return l > 0; })) {
+    set_error("no sample keeps a particle");
+    return kErrArg;
+  }
+  Context* cx = context(&st);
+  if (!cx) return st;
+  GccbRun R;
+  if ((st = gccb_prepare(cx, matrix, m, n, n_samples, L, add, u, true, R))) return st;
+  if (flush_bytes > 0 && (st = ensure(cx->misc, (size_t)flush_bytes))) return st;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  cudaError_t e = cudaSuccess;
+  for (int it = 0; it < n_warmup + n_steps && e == cudaSuccess; ++it) {
+    if (flush_bytes > 0) e = cudaMemsetAsync(cx->misc.ptr, it & 0xff, (size_t)flush_bytes, cx->stream);
+    cudaEventRecord(e0, cx->stream);
+    if ((st = gccb_launch(cx))) break;
+    cudaEventRecord(e1, cx->stream);
+    e = cudaEventSynchronize(e1);
+    if (e != cudaSuccess) break;
+    if (it >= n_warmup) {
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, e0, e1);
+      step_ms[it - n_warmup] = ms;
+      double sw = 0.0;
+      for (int k = 0; k + 1 < (int)R.ev.size(); k += 2) {
+        float x = 0.f;
+        if (cudaEventElapsedTime(&x, R.ev[k], R.ev[k + 1]) != cudaSuccess) {
+          cudaGetLastError();
+          x = 0.f;
+        }
+        sw += x;
+      }
+      sweep_ms[it - n_warmup] = sw;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (!st && e != cudaSuccess) st = fail_cuda(e, "bench");
+  if (!st) st = gccb_collect(cx, R, samples);
+  destroy_events(R);
+  if (st) return st;
+  info[0] = R.sweep_flops;
+  info[1] = (double)R.h2d_bytes;
+  info[2] = (double)R.d2h_bytes;
+  info[3] = (double)R.kernels;
+  info[4] = (double)R.sweeps;
+  info[5] = (double)R.Lmax;
   memcpy(mt_key, mt.key, sizeof(mt.key));
   *mt_pos = mt.pos;
   return kOk;

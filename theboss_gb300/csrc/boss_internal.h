@@ -11,38 +11,45 @@
 
 namespace boss {
 
+enum class SweepOp { kPerm = 0, kMinors = 1 };
+
 // Everything one sweep launch needs (device pointers).
 struct SweepLaunch {
-  const SweepPlan* plans = nullptr;
-  int n_plans = 0;
-  const double2* pool = nullptr;
-  int64_t total_items = 0;
-  unsigned long long* counter = nullptr;  // zeroed before the launch
+  const SweepProblem* probs = nullptr;
+  int n_probs = 0;
+  const longlong2* pool = nullptr;
+  int64_t total_threads = 0;
   double2* partials = nullptr;
-  int max_nc = 1;
   int grid = 1;
 };
 
+// Sets kernel attributes and records occupancy (once per process, outside any capture).
 cudaError_t prepare_sweep_kernels();
-cudaError_t launch_perm_sweep(const SweepLaunch& L, cudaStream_t st);
-cudaError_t launch_minors_sweep(const SweepLaunch& L, cudaStream_t st);
-cudaError_t launch_perm_reduce(const SweepPlan* plans, const int32_t* out_plans, const int32_t* out_begin, int n_out,
-                               const double2* partials, double2* out, cudaStream_t st);
-cudaError_t launch_minors_reduce(const SweepPlan* plans, const int32_t* out_plans, const int32_t* out_begin,
-                                 int n_out, const double2* partials, double2* out, int nd_max, cudaStream_t st);
+// Resident threads of one full wave of the sweep kernel for `nf` factors.
+int64_t sweep_resident_threads(int nf, SweepOp op, int sm_count);
+cudaError_t launch_sweep(int nf, SweepOp op, const SweepLaunch& L, cudaStream_t st);
+cudaError_t launch_perm_reduce(const SweepProblem* probs, int n_probs, const double2* partials, double2* out,
+                               cudaStream_t st);
+cudaError_t launch_minors_reduce(const SweepProblem* probs, int n_probs, const double2* partials, double2* out,
+                                 int nd_max, cudaStream_t st);
+
+// Splits `n_codes` codes over at most `resident` threads, proportionally, at
+// least one thread per sweep and at least kMinCodesPerThread codes per thread.
+constexpr int64_t kMinCodesPerThread = 32;
+void partition_threads(const std::vector<uint64_t>& n_codes, int64_t resident, std::vector<int64_t>& n_threads);
 
 // ---------------------------------------------------------------------------
-// Host-side sweep description before it is cut into segments.
+// Host-side sweep description.
 // ---------------------------------------------------------------------------
 struct HostSweep {
   int kind = kRyser;
   int parity0 = 0;
-  int nd = 0, nb = 0, nc = 0;
+  int nd = 0, nb = 0, nf = 0;
   int has_base = 0;
+  int fx = 56;
   uint8_t mult[kMaxDigits] = {};
-  uint8_t pw[kMaxCols] = {};
-  std::vector<double2> D;     // nd x nc
-  std::vector<double2> base;  // nc (has_base)
+  std::vector<longlong2> D;     // nd x nf
+  std::vector<longlong2> base;  // nf (has_base)
   double scale = 1.0;
   uint64_t total_codes = 1;
   int digit_mode[kMaxDigits] = {};  // digit -> mode (all-minors results)
@@ -81,8 +88,9 @@ Context* context(int* status);
 int ensure(DeviceBuffer& b, size_t bytes);
 int ensure_pinned(Context* cx, size_t bytes);
 
-// Builds the segments of a list of sweeps into device plan arrays and launches
-// sweep + reduction.  results: n_out complex (perms) or n_out x nd_max (minors).
+// Uploads a list of sweeps (all with the same factor count), launches the sweep
+// and the reduction, copies the results back.  results: one complex per sweep
+// (perms) or nd_max complex per sweep (all-minors).
 int run_sweeps(Context* cx, const std::vector<HostSweep>& sweeps, bool minors, int nd_max, double2* results_host);
 
 }  // namespace boss

@@ -1,138 +1,154 @@
 // boss_sweep.cuh -- device-side building blocks of the permanent sweeps.
 //
 // Every permanent in theboss's hot path is a signed, binomially weighted sum over
-// the codes r of a reflected mixed-radix Gray ("Guan") code of
-//     prod_l ( base_l + sgn * sum_i r_i * D_il ) ^ pw_l
+// the codes r of a reflected mixed-radix Gray ("Guan") code of a product of
+// row sums:
+//     sum_r  sign(r) * prod_i C(mult_i, r_i) * prod_f s_f(r),
+//     s_f(r) = base_f + sum_i r_i * D_if
 // where i runs over the iterated side's distinct modes ("digits", multiplicity
-// mult_i, r_i in [0, mult_i]) and l over the product side's distinct modes
-// ("columns", power pw_l):
-//   * Ryser   (ryser_permanent_calculator.py:45-64): base = 0, sgn = +1, D = U,
-//               sign (-1)^(n + |r|);
+// mult_i, r_i in [0, mult_i]) and f over the product side's particles ("factors":
+// a mode occupied p times contributes p identical factors, which is theboss's
+// pow(sum, p)):
+//   * Ryser (ryser_permanent_calculator.py:45-64): base = 0, D = U,
+//     sign (-1)^(n + |r|);
 //   * Glynn / Chin-Huh (chin_huh_permanent_calculator.py:38-59,
-//     glynn_gray_permanent_calculator.py:41-84): base_l = sum_i mult_i U_il,
-//               sgn = -1, D = 2U, sign (-1)^|r|, scale 2^-n.
-// The weight is prod_i C(mult_i, r_i) (bs_permanent_calculator_base.py:151-164).
+//     glynn_gray_permanent_calculator.py:41-84): base_f = sum_i mult_i U_if,
+//     D = -2U, sign (-1)^|r|, scale 2^-n.
+// The binomial weight follows bs_permanent_calculator_base.py:151-164.
 //
-// GPU layout of one sweep: the digits are ordered binary-first (mult 1), then
-// multi-valued.  The code range is cut into chunks of 2^c codes that only move
-// the lowest c (binary) digits, so inside a chunk the flip sequence is the
-// binary-reflected Gray code (step t flips digit ctz(t)) for every thread at
-// once, the multi-valued digits and the binomial weight are constant, and each
-// thread decodes its chunk's start code in closed form.  A warp owns 32
-// consecutive chunks (one per lane) = one "work item"; sums stay in registers,
-// the delta rows are warp-broadcast loads.
+// GB300 mapping.  The FP64 pipe issues 2 lanes/clk/SM, 1/64 of FP32, so only the
+// products use it:
+//   * the row sums are exact 64-bit fixed-point integers (value = int * 2^-fx),
+//     updated with integer adds and converted to FP64 with integer instructions
+//     (fx_to_double), so the 2 adds per factor and code leave the FP64 pipe and
+//     the sums never drift;
+//   * the last multiply of every product is fused into the accumulation (4 DFMA);
+//   * sign flips are integer XORs on the sign bit.
+// That leaves 4*(nf - 1) FP64 instructions per code.
+//
+// Work split: the codes of a sweep are cut into one contiguous range per thread
+// (lengths differ by at most one), each thread decodes its start code in closed
+// form and walks the Gray code: step t flips binary digit ctz(t); when ctz(t)
+// reaches a multi-valued digit the thread re-decodes.  Binary digits are ordered
+// first so that happens once per 2^nb codes.
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
 
 namespace boss {
 
-constexpr int kMaxDigits = 64;      // distinct modes on the iterated side
-constexpr int kMaxCols = 32;        // distinct modes on the product side
-constexpr int kMaxMinorDigits = 32; // digits of an all-minors sweep
-constexpr int kMaxChunkLog = 20;
+constexpr int kMaxDigits = 64;       // distinct modes on the iterated side
+constexpr int kMaxFactors = 32;      // particles on the product side
+constexpr int kMaxMinorDigits = 32;  // digits of an all-minors sweep
+constexpr int kSegLog = 16;          // all-minors bookkeeping is settled every 2^16 codes
 
 enum SweepKind : int32_t { kRyser = 0, kGlynn = 1 };
 
-// One sweep (one permanent, or one all-minors problem), built on the host or by
-// the sampler's device-side planner.  Plain old data; lives in device memory.
-struct SweepPlan {
-  int32_t nd;        // digits (iterated side), binary ones first
-  int32_t nb;        // number of leading binary digits
-  int32_t c;         // log2(codes per chunk); c <= nb
-  int32_t nc;        // product columns (0 < nc <= kMaxCols)
+// One sweep (a permanent or an all-minors problem).  Plain old data in device
+// memory; built by the host planner or by the sampler's device-side planner.
+struct SweepProblem {
+  int32_t nd;        // digits, binary ones first
+  int32_t nb;        // leading binary digits
+  int32_t nf;        // product factors
   int32_t kind;      // SweepKind
   int32_t parity0;   // sign parity of the r = 0 code
-  int32_t has_base;  // Glynn/Chin-Huh: base sums present at base_off
-  int32_t all_pow1;  // every column power is 1
-  int64_t n_chunks;  // total codes >> c
-  int64_t item_off;  // first work item of this sweep in the flat item space
-  int64_t n_items;   // ceil(n_chunks / 32)
-  int64_t mat_off;   // delta rows D: nd x nc complex, row-major, at pool + mat_off
-  int64_t base_off;  // nc complex base sums (has_base)
-  int64_t part_off;  // partial-result slot: perms use 1 complex / item, minors nd / item
-  int64_t code_off;  // first code of this segment (a sweep may be cut into segments)
-  int32_t out_idx;   // result this segment contributes to
-  int32_t reserved;
+  int32_t fx;        // fixed-point fraction bits of the row sums
+  int32_t has_base;  // base sums present
+  int32_t out_idx;   // result index
+  int64_t n_codes;       // codes in the sweep
+  int64_t thread_begin;  // first global thread of this sweep
+  int64_t n_threads;     // threads working on it
+  int64_t mat_off;   // D: nd x nf fixed-point complex (longlong2), row-major
+  int64_t base_off;  // nf fixed-point complex
+  int64_t part_off;  // partials: n_threads complex (perms) or n_threads x nd (all-minors)
   double scale;      // final real scale
+  double reserved;
   uint8_t mult[kMaxDigits];
-  uint8_t pw[kMaxCols];
 };
 
 // ---------------------------------------------------------------------------
-// FP64 helpers.  The GB300 FP64 pipe issues ~2 lanes/clk/SM, 1/64 of FP32, so
-// everything that is not FP64 arithmetic (sign handling, index math, loads) is
-// kept on the integer / load pipes.
+// Integer-pipe helpers
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ double xor_sign(double x, uint32_t neg_mask) {
-  // neg_mask is 0 or 0x80000000: flips the sign bit with one integer LOP.
   return __hiloint2double(__double2hiint(x) ^ (int)neg_mask, __double2loint(x));
 }
 
-__device__ __forceinline__ void cmul_acc(double& pr, double& pi, double br, double bi) {
-  // (pr + i pi) *= (br + i bi): 2 DMUL + 2 DFMA.
-  const double t_re = fma(pr, br, -(pi * bi));
-  const double t_im = fma(pr, bi, pi * br);
-  pr = t_re;
-  pi = t_im;
+// x * 2^-fx as a double, rounded to nearest (ties away from zero), using integer
+// instructions only.  bias_exp = 1023 + 63 - fx.  Requires the result to be a
+// normal double or zero.
+__device__ __forceinline__ double fx_to_double(long long x, int bias_exp) {
+  const unsigned long long sgn = (unsigned long long)(x >> 63);
+  const unsigned long long ax = ((unsigned long long)x ^ sgn) - sgn;
+  const int lz = __clzll((long long)ax);
+  const unsigned long long y = ax << (lz & 63);
+  const unsigned long long yr = y + 0x400ull;
+  const unsigned long long carry = (yr < y) ? 1ull : 0ull;
+  const unsigned long long mant = (yr >> 11) & 0xFFFFFFFFFFFFFull;
+  const unsigned long long e = (unsigned long long)(bias_exp - lz) + carry;
+  const unsigned long long bits = (sgn << 63) | (e << 52) | mant;
+  return __longlong_as_double(ax ? (long long)bits : 0ll);
 }
 
 __device__ __forceinline__ double binom_small(int n, int k) {
-  // C(n, k) for n <= 255; exact in double for the multiplicities a sweep allows.
   double r = 1.0;
   for (int i = 1; i <= k; ++i) r = r * (double)(n - k + i) / (double)i;
   return r;
 }
 
-// Decodes the start code of a chunk (code number t0, low c bits zero) into the
-// sweep state: starting sums, the sign parity, the binomial weight of the
-// multi-valued digits, and the Gray bits of the low c digits.  The digit value
-// is the closed form of the reflected mixed-radix code: digit i of code t is d_i
-// (the plain mixed-radix digit) when the number of completed cycles of digits
-// 0..i is even and mult_i - d_i otherwise; for binary digits that is
+// Digit value of code t: digit i is the plain mixed-radix digit d_i when the
+// number of completed cycles of digits 0..i is even, mult_i - d_i when odd (the
+// closed form of the reflected mixed-radix code); binary digits reduce to
 // bit_i(t) ^ bit_(i+1)(t).
-template <int NC>
-__device__ __forceinline__ void decode_chunk_start(const SweepPlan& P, const double2* __restrict__ D,
-                                                   const double2* __restrict__ base, uint64_t t0,
-                                                   double (&sr)[NC], double (&si)[NC], uint32_t& parity,
-                                                   double& weight, uint32_t& gray_low) {
-  const int nc = P.nc;
+__device__ __forceinline__ uint32_t digit_value(const SweepProblem& P, uint64_t t, int i) {
+  if (i < P.nb) return (uint32_t)(((t >> i) ^ (t >> (i + 1))) & 1ull);
+  uint64_t th = t >> P.nb;
+  uint32_t r = 0;
+  for (int j = P.nb; j <= i; ++j) {
+    const uint32_t mu = P.mult[j];
+    const uint64_t b = (uint64_t)mu + 1ull;
+    const uint64_t q = th / b;
+    const uint32_t dgt = (uint32_t)(th - q * b);
+    th = q;
+    r = (q & 1ull) ? (mu - dgt) : dgt;
+  }
+  return r;
+}
+
+// Full state at code t: fixed-point sums, sign parity, binomial weight of the
+// multi-valued digits, and the bits of the binary digits.
+template <int NF>
+__device__ __forceinline__ void decode_code(const SweepProblem& P, const longlong2* __restrict__ D,
+                                            const longlong2* __restrict__ base, uint64_t t, long long (&sr)[NF],
+                                            long long (&si)[NF], uint64_t& gbits, uint32_t& parity, double& weight) {
 #pragma unroll
-  for (int l = 0; l < NC; ++l) {
-    if (l < nc) {
-      if (P.has_base) {
-        const double2 b = base[l];
-        sr[l] = b.x;
-        si[l] = b.y;
-      } else {
-        sr[l] = 0.0;
-        si[l] = 0.0;
-      }
+  for (int f = 0; f < NF; ++f) {
+    if (P.has_base) {
+      const longlong2 b = base[f];
+      sr[f] = b.x;
+      si[f] = b.y;
     } else {
-      sr[l] = 0.0;
-      si[l] = 0.0;
+      sr[f] = 0;
+      si[f] = 0;
     }
   }
   parity = (uint32_t)P.parity0;
   weight = 1.0;
-  // Ryser adds r_i * D_i, Glynn subtracts it.
-  const uint32_t sub_mask = (P.kind == kGlynn) ? 0x80000000u : 0u;
-  for (int i = 0; i < P.nb; ++i) {
-    const uint32_t r = (uint32_t)(((t0 >> i) ^ (t0 >> (i + 1))) & 1ull);
-    if (r) {
-      parity ^= 1u;
-      const double2* row = D + (size_t)i * nc;
+  gbits = (t ^ (t >> 1));
+  if (P.nb < 64) gbits &= (1ull << P.nb) - 1ull;
+  uint64_t bits = gbits;
+  while (bits) {
+    const int i = __ffsll((long long)bits) - 1;
+    bits &= bits - 1ull;
+    parity ^= 1u;
+    const longlong2* row = D + (size_t)i * NF;
 #pragma unroll
-      for (int l = 0; l < NC; ++l) {
-        if (l < nc) {
-          const double2 d = row[l];
-          sr[l] += xor_sign(d.x, sub_mask);
-          si[l] += xor_sign(d.y, sub_mask);
-        }
-      }
+    for (int f = 0; f < NF; ++f) {
+      const longlong2 d = row[f];
+      sr[f] += d.x;
+      si[f] += d.y;
     }
   }
-  uint64_t th = t0 >> P.nb;
+  uint64_t th = t >> P.nb;
   for (int i = P.nb; i < P.nd; ++i) {
     const uint32_t mu = P.mult[i];
     const uint64_t b = (uint64_t)mu + 1ull;
@@ -143,68 +159,84 @@ __device__ __forceinline__ void decode_chunk_start(const SweepPlan& P, const dou
     if (r) {
       parity ^= (r & 1u);
       weight *= binom_small((int)mu, (int)r);
-      const double coef = (P.kind == kGlynn) ? -(double)r : (double)r;
-      const double2* row = D + (size_t)i * nc;
+      const longlong2* row = D + (size_t)i * NF;
 #pragma unroll
-      for (int l = 0; l < NC; ++l) {
-        if (l < nc) {
-          const double2 d = row[l];
-          sr[l] = fma(coef, d.x, sr[l]);
-          si[l] = fma(coef, d.y, si[l]);
-        }
+      for (int f = 0; f < NF; ++f) {
+        const longlong2 d = row[f];
+        sr[f] += (long long)r * d.x;
+        si[f] += (long long)r * d.y;
       }
     }
   }
-  const int c = P.c;
-  gray_low = (c > 0) ? (uint32_t)((t0 >> c) & 1ull) << (c - 1) : 0u;
 }
 
-// prod_l s_l^pw_l.  nc >= 1.
-template <int NC>
-__device__ __forceinline__ void column_product(const SweepPlan& P, const double (&sr)[NC], const double (&si)[NC],
-                                               double& pr, double& pi) {
-  const int nc = P.nc;
-  pr = sr[0];
-  pi = si[0];
-  if (P.all_pow1) {
+// Binary digit i moves from `bit` to 1 - bit: sums +/-= D_i.
+template <int NF>
+__device__ __forceinline__ void flip_binary(const longlong2* __restrict__ D, int i, uint32_t bit, long long (&sr)[NF],
+                                            long long (&si)[NF]) {
+  const longlong2* row = D + (size_t)i * NF;
+  if (bit) {
 #pragma unroll
-    for (int l = 1; l < NC; ++l)
-      if (l < nc) cmul_acc(pr, pi, sr[l], si[l]);
+    for (int f = 0; f < NF; ++f) {
+      const longlong2 d = row[f];
+      sr[f] -= d.x;
+      si[f] -= d.y;
+    }
   } else {
-    for (int q = 1; q < P.pw[0]; ++q) cmul_acc(pr, pi, sr[0], si[0]);
 #pragma unroll
-    for (int l = 1; l < NC; ++l) {
-      if (l < nc) {
-        const int p = P.pw[l];
-        for (int q = 0; q < p; ++q) cmul_acc(pr, pi, sr[l], si[l]);
-      }
+    for (int f = 0; f < NF; ++f) {
+      const longlong2 d = row[f];
+      sr[f] += d.x;
+      si[f] += d.y;
     }
   }
 }
 
-// Moves digit i (a low, binary digit) from r_i = bit to 1 - bit.
-template <int NC>
-__device__ __forceinline__ void flip_digit(const SweepPlan& P, const double2* __restrict__ D, int i, uint32_t bit,
-                                           double (&sr)[NC], double (&si)[NC]) {
-  // Ryser: sums += (bit ? -D_i : +D_i).  Glynn: sums += (bit ? +D_i : -D_i).
-  const uint32_t neg = ((bit ^ (uint32_t)(P.kind == kGlynn)) & 1u) ? 0x80000000u : 0u;
-  const int nc = P.nc;
-  const double2* row = D + (size_t)i * nc;
-#pragma unroll
-  for (int l = 0; l < NC; ++l) {
-    if (l < nc) {
-      const double2 d = row[l];
-      sr[l] += xor_sign(d.x, neg);
-      si[l] += xor_sign(d.y, neg);
-    }
+// acc += sign * prod_f s_f : (NF - 2) complex products (4 FP64 instructions each)
+// plus 4 DFMA for the last factor fused with the accumulation.
+template <int NF>
+__device__ __forceinline__ void accumulate_product(const long long (&sr)[NF], const long long (&si)[NF], int bias_exp,
+                                                   uint32_t neg_mask, double& ar, double& ai) {
+  if (NF == 1) {
+    ar += xor_sign(fx_to_double(sr[0], bias_exp), neg_mask);
+    ai += xor_sign(fx_to_double(si[0], bias_exp), neg_mask);
+    return;
   }
+  double pr = fx_to_double(sr[0], bias_exp);
+  double pi = fx_to_double(si[0], bias_exp);
+#pragma unroll
+  for (int f = 1; f < NF - 1; ++f) {
+    const double br = fx_to_double(sr[f], bias_exp);
+    const double bi = fx_to_double(si[f], bias_exp);
+    const double t_re = fma(pr, br, -(pi * bi));
+    const double t_im = fma(pr, bi, pi * br);
+    pr = t_re;
+    pi = t_im;
+  }
+  pr = xor_sign(pr, neg_mask);
+  pi = xor_sign(pi, neg_mask);
+  const double br = fx_to_double(sr[NF - 1], bias_exp);
+  const double bi = fx_to_double(si[NF - 1], bias_exp);
+  ar = fma(pr, br, ar);
+  ar = fma(-pi, bi, ar);
+  ai = fma(pr, bi, ai);
+  ai = fma(pi, br, ai);
 }
 
-__device__ __forceinline__ double warp_sum(double v) {
-  // Fixed butterfly order: every lane ends with the same, run-to-run identical sum.
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-  return v;
+// This thread's code range inside its sweep: lengths differ by at most one.
+__device__ __forceinline__ void thread_range(const SweepProblem& P, int64_t q, int64_t& a, int64_t& len) {
+  const int64_t per = P.n_codes / P.n_threads, rem = P.n_codes % P.n_threads;
+  a = q * per + (q < rem ? q : rem);
+  len = per + (q < rem ? 1 : 0);
+}
+
+__device__ __forceinline__ int find_problem(const SweepProblem* __restrict__ probs, int n, int64_t gt) {
+  int lo = 0, hi = n - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (probs[mid].thread_begin <= gt) lo = mid; else hi = mid - 1;
+  }
+  return lo;
 }
 
 }  // namespace boss

@@ -1,0 +1,4 @@
+// Instantiates the sweep kernels for NF = 1 .. 8 (see boss_sweep_kernels.cuh).
+#include "boss_sweep_kernels.cuh"
+
+BOSS_SWEEP_RANGE(sweep_nf_a, 1)
