@@ -170,6 +170,33 @@ BOSS_API int boss_gccb_bench(const double* matrix, int32_t m, const int32_t* inp
                              double* step_ms, double* sweep_ms, double* info, int32_t* samples);
 
 /*
+ * Allocation-free form of boss_perm_batch, for callers that cannot let a library
+ * call cudaMalloc: processes that give the GPU's memory to their own pool
+ * allocator and must account for every byte, services under a hard memory cap,
+ * and latency-sensitive loops that avoid cudaMalloc's implicit device
+ * synchronisation.  This entry point has no counterpart in theboss.
+ *   - It allocates nothing: its scratch (sweep descriptors, fixed-point rows and
+ *     per-thread partial sums) is one static 8 MiB device array that every GPU
+ *     loading the library holds until the process exits.  A request needing
+ *     more scratch is rejected with BOSS_ERR_LIMIT (split the batch).
+ *   - matrix and the occupation vectors are host pointers (the sweep is planned
+ *     on the host); results_device is a device buffer of `count` complex128 owned
+ *     by the caller; work is queued on `stream` (a cudaStream_t, 0 for the
+ *     default stream) and the call returns without waiting for it: synchronise
+ *     the stream before reading the results.
+ *   - The first call on each device does a one-time set-up on the current
+ *     device (looks up the scratch array's device address and sets kernel
+ *     attributes).
+ *   - Every call shares the scratch array, which keeps the last call's contents;
+ *     nothing in it has to start at zero.  Calls on the same stream are ordered;
+ *     calls whose work overlaps on the GPU (different streams or threads) race on
+ *     the scratch and must not be issued.
+ */
+BOSS_API int boss_perm_batch_noalloc(const double* matrix, int32_t m, const int32_t* input_states,
+                                     const int32_t* output_states, int32_t len, int32_t count, int32_t variant,
+                                     double* results_device, void* stream);
+
+/*
  * FP64 throughput of the current GPU: a dependency-free DFMA stream on every SM,
  * timed with CUDA events.  Writes TFLOP/s (an FMA counts 2 flops) and the kernel
  * time.  No reference counterpart: it is the denominator of the FP64 roofline.

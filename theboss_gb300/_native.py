@@ -57,6 +57,9 @@ def load() -> ctypes.CDLL:
             f = getattr(L, name)
             f.restype = ctypes.c_int
             f.argtypes = [dp, ctypes.c_int32, ip, ip, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, dp]
+        L.boss_perm_batch_noalloc.restype = ctypes.c_int
+        L.boss_perm_batch_noalloc.argtypes = [dp, ctypes.c_int32, ip, ip, ctypes.c_int32, ctypes.c_int32,
+                                              ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p]
         L.boss_fp64_peak.restype = ctypes.c_int
         L.boss_fp64_peak.argtypes = [dp, dp]
         up = ctypes.POINTER(ctypes.c_uint32)
@@ -138,6 +141,17 @@ def submatrices_batch(U: np.ndarray, S: np.ndarray, T: np.ndarray, variant: int)
     check(L.boss_submatrices_batch(_dp(U.view(np.float64)), U.shape[0], _ip(S), _ip(T), n, count, variant,
                                    _dp(out.view(np.float64))))
     return out
+
+
+def perm_batch_noalloc(U: np.ndarray, S: np.ndarray, T: np.ndarray, variant: int, results_device_ptr: int,
+                       stream_ptr: int = 0) -> None:
+    """Queues the permanents of U[T_k, S_k] into a caller-owned device buffer of
+    count complex128 without any GPU allocation (boss_perm_batch_noalloc).  The
+    caller synchronises the stream before reading the buffer."""
+    L = load()
+    count, n = S.shape
+    check(L.boss_perm_batch_noalloc(_dp(U.view(np.float64)), U.shape[0], _ip(S), _ip(T), n, count, variant,
+                                    ctypes.c_void_p(int(results_device_ptr)), ctypes.c_void_p(int(stream_ptr))))
 
 
 def fp64_peak():

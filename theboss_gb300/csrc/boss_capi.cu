@@ -648,3 +648,157 @@ int boss_perm_bench(const double* matrix, int32_t m, const int32_t* input_states
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Allocation-free permanents.
+//
+// Some callers cannot let a library call cudaMalloc: processes that hand all of
+// the GPU's memory to their own pool allocator up front and must account for
+// every byte, services running under a hard memory cap where a surprise
+// allocation can fail or fragment the pool, and latency-sensitive loops that
+// avoid cudaMalloc's implicit device synchronisation.  For them
+// boss_perm_batch_noalloc runs the same permanent sweep as boss_perm_batch with
+// all of its scratch (sweep descriptors, fixed-point rows, per-thread partial
+// sums) in one statically sized device array, g_noalloc_scratch below, and
+// writes the results into a device buffer the caller owns.
+// ---------------------------------------------------------------------------
+namespace boss {
+
+constexpr size_t kNoAllocScratchBytes = (size_t)8 << 20;  // 8 MiB, held by every GPU that loads the library
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+alignas(256) static unsigned char g_noalloc_staging[kNoAllocScratchBytes];  // host-side copy source
+
+struct NoAllocDevice {
+  bool ready = false;
+  int sm_count = 0;
+  unsigned char* scratch = nullptr;  // device address of g_noalloc_scratch on this device
+};
+constexpr int kNoAllocMaxDevices = 64;
+static NoAllocDevice g_noalloc_dev[kNoAllocMaxDevices];
+
+// Once per device, with that device current: the device address of the scratch
+// array (its host-side name is only a stand-in) and the kernel attributes.
+static int noalloc_setup(int device, NoAllocDevice*& out) {
+  if (device < 0 || device >= kNoAllocMaxDevices) {
+    set_error("device index out of range");
+    return kErrArg;
+  }
+  NoAllocDevice& d = g_noalloc_dev[device];
+  if (!d.ready) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess) return fail_cuda(e, "cudaGetSymbolAddress(g_noalloc_scratch)");
+    if ((e = cudaDeviceGetAttribute(&d.sm_count, cudaDevAttrMultiProcessorCount, device)) != cudaSuccess)
+      return fail_cuda(e, "cudaDeviceGetAttribute");
+    if ((e = prepare_sweep_kernels()) != cudaSuccess) return fail_cuda(e, "kernel attributes");
+    d.scratch = (unsigned char*)p;
+    d.ready = true;
+  }
+  out = &d;
+  return kOk;
+}
+
+}  // namespace boss
+
+extern "C" int boss_perm_batch_noalloc(const double* matrix, int32_t m, const int32_t* input_states,
+                                       const int32_t* output_states, int32_t len, int32_t count, int32_t variant,
+                                       double* results_device, void* stream) {
+  if (!matrix || !input_states || !output_states || !results_device || m <= 0 || count < 0) {
+    set_error("null pointer or bad size");
+    return kErrArg;
+  }
+  std::lock_guard<std::mutex> lk(g_api_mutex);
+  int device = 0;
+  cudaError_t e = cudaGetDevice(&device);
+  if (e != cudaSuccess) return fail_cuda(e, "cudaGetDevice");
+  NoAllocDevice* dev = nullptr;
+  int st = noalloc_setup(device, dev);
+  if (st) return st;
+  cudaStream_t s = (cudaStream_t)stream;
+  double2* out = (double2*)results_device;
+  std::vector<HostSweep> by_nf[kMaxFactors + 1];
+  std::vector<int> which[kMaxFactors + 1];
+  for (int k = 0; k < count; ++k) {
+    HostSweep hs;
+    bool need = false;
+    double2 v = make_double2(0.0, 0.0);
+    st = plan_permanent(matrix, m, input_states + (size_t)k * len, output_states + (size_t)k * len, len, variant, hs,
+                        need, v);
+    if (st) return st;
+    if (need) {
+      which[hs.nf].push_back(k);
+      by_nf[hs.nf].push_back(std::move(hs));
+    } else {  // a permanent theboss defines without a sweep (empty states): one small copy
+      if ((e = cudaMemcpyAsync(out + k, &v, sizeof(double2), cudaMemcpyHostToDevice, s)) != cudaSuccess)
+        return fail_cuda(e, "H2D direct result");
+    }
+  }
+  // One sweep launch per product size; each reuses the scratch from its start
+  // (stream order keeps a group's copy behind the previous group's kernels).
+  for (int nf = 1; nf <= kMaxFactors; ++nf) {
+    const std::vector<HostSweep>& sw = by_nf[nf];
+    const int n = (int)sw.size();
+    if (n == 0) continue;
+    std::vector<uint64_t> codes(n);
+    for (int p = 0; p < n; ++p) codes[p] = sw[p].total_codes;
+    std::vector<int64_t> nthr;
+    partition_threads(codes, sweep_resident_threads(nf, SweepOp::kPerm, dev->sm_count), nthr);
+    int64_t pool_n = 0, threads = 0;
+    for (int p = 0; p < n; ++p) {
+      pool_n += (int64_t)(sw[p].D.size() + sw[p].base.size());
+      threads += nthr[p];
+    }
+    const size_t o_probs = 0;
+    const size_t o_pool = align_up(o_probs + sizeof(SweepProblem) * n, 256);
+    const size_t o_part = align_up(o_pool + sizeof(longlong2) * (size_t)std::max<int64_t>(pool_n, 1), 256);
+    const size_t need_bytes = o_part + sizeof(double2) * (size_t)threads;
+    if (need_bytes > kNoAllocScratchBytes) {
+      set_error("request needs " + std::to_string(need_bytes) + " bytes of scratch; the allocation-free entry "
+                "point has " + std::to_string(kNoAllocScratchBytes) + " (split the batch)");
+      return kErrLimit;
+    }
+    SweepProblem* hp = (SweepProblem*)(g_noalloc_staging + o_probs);
+    longlong2* hpool = (longlong2*)(g_noalloc_staging + o_pool);
+    int64_t pool_at = 0, thread_at = 0;
+    for (int p = 0; p < n; ++p) {
+      const HostSweep& h = sw[p];
+      SweepProblem& P = hp[p];
+      memset(&P, 0, sizeof(P));
+      P.nd = h.nd;
+      P.nb = h.nb;
+      P.nf = h.nf;
+      P.kind = h.kind;
+      P.parity0 = h.parity0;
+      P.fx = h.fx;
+      P.has_base = h.has_base;
+      P.out_idx = which[nf][p];  // the reduction writes straight into the caller's buffer
+      P.n_codes = (int64_t)h.total_codes;
+      P.thread_begin = thread_at;
+      P.n_threads = nthr[p];
+      P.mat_off = pool_at;
+      std::copy(h.D.begin(), h.D.end(), hpool + pool_at);
+      pool_at += (int64_t)h.D.size();
+      P.base_off = pool_at;
+      std::copy(h.base.begin(), h.base.end(), hpool + pool_at);
+      pool_at += (int64_t)h.base.size();
+      P.part_off = thread_at;
+      P.scale = h.scale;
+      for (int i = 0; i < h.nd; ++i) P.mult[i] = h.mult[i];
+      thread_at += nthr[p];
+    }
+    // Pageable source: the copy is staged before this call returns, so the host
+    // staging array can be refilled by the next group.
+    if ((e = cudaMemcpyAsync(dev->scratch, g_noalloc_staging, o_part, cudaMemcpyHostToDevice, s)) != cudaSuccess)
+      return fail_cuda(e, "H2D sweeps");
+    SweepLaunch L;
+    L.probs = (const SweepProblem*)(dev->scratch + o_probs);
+    L.n_probs = n;
+    L.pool = (const longlong2*)(dev->scratch + o_pool);
+    L.total_threads = threads;
+    L.partials = (double2*)(dev->scratch + o_part);
+    L.grid = (int)((threads + 127) / 128);
+    if ((e = launch_sweep(nf, SweepOp::kPerm, L, s)) != cudaSuccess) return fail_cuda(e, "sweep launch");
+    if ((e = launch_perm_reduce(L.probs, n, L.partials, out, s)) != cudaSuccess) return fail_cuda(e, "reduce launch");
+  }
+  return kOk;
+}
