@@ -190,6 +190,68 @@ def single_permanents(peak_tflops, seed):
     return res
 
 
+def adjoint_section(seed):
+    """C4: log-likelihood of 256 seeded output patterns (n=12, m=24, doubles
+    allowed) under a 24-mode Clements mesh of 276 (theta, phi) phases;
+    forward = mesh + permanents + log-likelihood, backward = torch autograd
+    through the adjoint kernel and the mesh.  Plus 64 n=24 gradients in m=48."""
+    import torch
+
+    from theboss_gb300 import _native
+    from theboss_gb300.adjoint import clements_unitary, log_likelihood
+    from theboss_gb300.utilities import haar_unitary
+
+    def patterns(m, n, count, s, maxm=2):
+        rng = np.random.default_rng(s)
+        out = np.zeros((count, m), dtype=np.int32)
+        for k in range(count):
+            c = 0
+            while c < n:
+                i = int(rng.integers(0, m))
+                if out[k, i] < maxm:
+                    out[k, i] += 1
+                    c += 1
+        return out
+
+    m, n = 24, 12
+    g = torch.Generator().manual_seed(seed)
+    theta = (torch.rand(276, generator=g, dtype=torch.float64) * 2 * np.pi).requires_grad_(True)
+    phi = (torch.rand(276, generator=g, dtype=torch.float64) * 2 * np.pi).requires_grad_(True)
+    S = np.zeros((256, m), dtype=np.int32)
+    S[:, :n] = 1
+    T = patterns(m, n, 256, seed)
+    fw, bw = [], []
+    for it in range(6):
+        theta.grad = None
+        phi.grad = None
+        t0 = time.perf_counter()
+        L = log_likelihood(clements_unitary(theta, phi), S, T)
+        t1 = time.perf_counter()
+        L.backward()
+        t2 = time.perf_counter()
+        if it >= 2:
+            fw.append(t1 - t0)
+            bw.append(t2 - t1)
+    c4 = {"forward_ms": 1e3 * float(np.median(fw)), "backward_ms": 1e3 * float(np.median(bw)),
+          "backward_over_forward": float(np.median(bw) / np.median(fw)), "patterns": 256, "n": n, "m": m,
+          "phases": 276, "log_likelihood": float(L.item())}
+    # kernel-level: permanents vs permanents + all n^2 derivatives, n = 24
+    m2, n2 = 48, 24
+    U = haar_unitary(m2, seed + 1)
+    S2 = np.zeros((64, m2), dtype=np.int32)
+    S2[:, :n2] = 1
+    T2 = patterns(m2, n2, 64, seed + 2)
+    _native.perm_batch(U, S2, T2, _native.GLYNN)
+    t0 = time.perf_counter()
+    _native.perm_batch(U, S2, T2, _native.GLYNN)
+    t1 = time.perf_counter()
+    _native.perm_grad_batch(U, S2, T2)
+    t2 = time.perf_counter()
+    c5 = {"forward_ms": 1e3 * (t1 - t0), "gradient_ms": 1e3 * (t2 - t1), "gradient_over_forward": (t2 - t1) / (t1 - t0),
+          "patterns": 64, "n": n2, "m": m2}
+    return {"clements_log_likelihood_n12_m24": c4, "gradients_n24_m48": c5}
+
+
 def run_ours(args, rank, world):
     from theboss_gb300 import _native
     from theboss_gb300.simulation_strategies import GCCBPlainDriver
@@ -249,6 +311,7 @@ def run_ours(args, rank, world):
         line["plain_gpu"] = {"value": plain, "unit": "samples/s", "samples": n_plain}
         line["batched_vs_plain"] = {"device": value / world / plain, "e2e": e2e["value"] / plain}
         line["single_permanents"] = single_permanents(peak, args.seed)
+        line["adjoint"] = adjoint_section(args.seed)
     if rank == 0:
         line["cpu_baseline"] = cpu_baseline(U, inp, w, args.seed)
         print(json.dumps(line), flush=True)

@@ -100,6 +100,20 @@ BOSS_API int boss_submatrices_batch(const double* matrix, int32_t m, const int32
                            double* results);
 
 /*
+ * Permanents and their gradients with respect to the matrix.  For each k,
+ * perms[k] = perm(U[T_k, S_k]) and grads[k][j][i] = d perm / d U[j][i]
+ * = T_k[j] * S_k[i] * perm(U[T_k - e_j, S_k - e_i]) (zero where either mode is
+ * empty), all from one Glynn sweep per permanent.  theboss has no derivative;
+ * its per-minor counterpart is BSCCRyserSubmatricesPermanentCalculator.compute_permanents
+ * (bs_cc_ryser_submatrices_permanent_calculator.py:16-119) called once per removed
+ * output particle.  Requires sum(S_k) == sum(T_k).
+ *   perms : count complex128;  grads : count x len x len complex128 (row = output mode)
+ */
+BOSS_API int boss_perm_grad_batch(const double* matrix, int32_t m, const int32_t* input_states,
+                                  const int32_t* output_states, int32_t len, int32_t count, double* perms,
+                                  double* grads);
+
+/*
  * Benchmark form of boss_perm_batch for `count` permanents with the same number
  * of product-side particles: planned and uploaded once, then the sweep kernel and
  * its reduction run n_warmup + n_steps times (an L2-evicting memset of

@@ -60,6 +60,8 @@ def load() -> ctypes.CDLL:
         L.boss_perm_batch_noalloc.restype = ctypes.c_int
         L.boss_perm_batch_noalloc.argtypes = [dp, ctypes.c_int32, ip, ip, ctypes.c_int32, ctypes.c_int32,
                                               ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p]
+        L.boss_perm_grad_batch.restype = ctypes.c_int
+        L.boss_perm_grad_batch.argtypes = [dp, ctypes.c_int32, ip, ip, ctypes.c_int32, ctypes.c_int32, dp, dp]
         L.boss_fp64_peak.restype = ctypes.c_int
         L.boss_fp64_peak.argtypes = [dp, dp]
         up = ctypes.POINTER(ctypes.c_uint32)
@@ -129,6 +131,19 @@ def perm_batch(U: np.ndarray, S: np.ndarray, T: np.ndarray, variant: int) -> np.
     check(L.boss_perm_batch(_dp(U.view(np.float64)), U.shape[0], _ip(S), _ip(T), n, count, variant,
                             _dp(out.view(np.float64))))
     return out
+
+
+def perm_grad_batch(U: np.ndarray, S: np.ndarray, T: np.ndarray):
+    """Permanents of U[T_k, S_k] and d perm_k / d U[j][i] (count x len x len)."""
+    L = load()
+    count, n = S.shape
+    perms = np.empty(count, dtype=np.complex128)
+    grads = np.empty((count, n, n), dtype=np.complex128)
+    if count == 0:
+        return perms, grads
+    check(L.boss_perm_grad_batch(_dp(U.view(np.float64)), U.shape[0], _ip(S), _ip(T), n, count,
+                                 _dp(perms.view(np.float64)), _dp(grads.view(np.float64))))
+    return perms, grads
 
 
 def submatrices_batch(U: np.ndarray, S: np.ndarray, T: np.ndarray, variant: int) -> np.ndarray:

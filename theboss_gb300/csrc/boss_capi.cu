@@ -250,6 +250,8 @@ static int fill_sweep(HostSweep& hs, const Side& dig, const Side& col, int kind,
   for (size_t l = 0; l < col.modes.size(); ++l)
     for (int k = 0; k < col.mult[l]; ++k) fmode.push_back(col.modes[l]);
   hs.nf = (int)fmode.size();
+  hs.fixed_mode = (drop >= 0) ? dig.modes[drop] : -1;
+  for (int f = 0; f < (int)fmode.size() && f < kMaxFactors; ++f) hs.factor_mode[f] = fmode[f];
   if (hs.nd > kMaxDigits || hs.nf > kMaxFactors || hs.nf < 1) {
     set_error("sweep exceeds 64 distinct iterated modes or 32 product-side particles");
     return kErrLimit;
@@ -367,15 +369,14 @@ static int plan_permanent(const double* U, int m, const int32_t* S, const int32_
       const uint64_t ci = in.nb ? in.codes / 2 : in.codes;
       const uint64_t co = out.nb ? out.codes / 2 : out.codes;
       int st;
-      if (co < ci)
-        st = fill_sweep(hs, out, in, kGlynn, true, entry_out_in);
-      else
-        st = fill_sweep(hs, in, out, kGlynn, true, entry_in_out);
+      bool outs = co < ci;
+      st = outs ? fill_sweep(hs, out, in, kGlynn, true, entry_out_in) : fill_sweep(hs, in, out, kGlynn, true, entry_in_out);
       if (st == kErrLimit) {  // try the other orientation
-        if (co < ci) st = fill_sweep(hs, in, out, kGlynn, true, entry_in_out);
-        else st = fill_sweep(hs, out, in, kGlynn, true, entry_out_in);
+        outs = !outs;
+        st = outs ? fill_sweep(hs, out, in, kGlynn, true, entry_out_in) : fill_sweep(hs, in, out, kGlynn, true, entry_in_out);
       }
       if (st) return st;
+      hs.digits_are_outputs = outs;
       if (hs.nd == 0) {  // a single code
         // fall through to the sweep anyway: nd = 0 is a one-code sweep
       }
@@ -571,6 +572,150 @@ int boss_submatrices_batch(const double* matrix, int32_t m, const int32_t* input
       const HostSweep& hs = by_nf[nf][a];
       double2* row = res + (size_t)which[nf][a] * len;
       for (int d = 0; d < hs.nd; ++d) row[hs.digit_mode[d]] = out[a * nd_max + d];
+    }
+  }
+  return kOk;
+}
+
+int boss_perm_grad_batch(const double* matrix, int32_t m, const int32_t* input_states,
+                         const int32_t* output_states, int32_t len, int32_t count, double* perms, double* grads) {
+  if (!matrix || !input_states || !output_states || !perms || !grads || m <= 0 || count < 0 || len <= 0) {
+    set_error("null pointer or bad size");
+    return kErrArg;
+  }
+  std::lock_guard<std::mutex> lk(g_api_mutex);
+  double2* P2 = (double2*)perms;
+  double2* G2 = (double2*)grads;
+  std::fill(G2, G2 + (size_t)count * len * len, make_double2(0.0, 0.0));
+  std::vector<HostSweep> by_nf[kMaxFactors + 1];
+  std::vector<int> which[kMaxFactors + 1];
+  bool any = false;
+  for (int k = 0; k < count; ++k) {
+    HostSweep hs;
+    bool need = false;
+    double2 v = make_double2(0.0, 0.0);
+    const int32_t* S = input_states + (size_t)k * len;
+    const int32_t* T = output_states + (size_t)k * len;
+    int st = plan_permanent(matrix, m, S, T, len, BOSS_GLYNN, hs, need, v);
+    if (st) return st;
+    if (!need) {  // no particles: perm = 1, gradient 0
+      P2[k] = v;
+      continue;
+    }
+    if (hs.nd + 1 > kMaxDigits) {
+      set_error("gradient sweep exceeds the digit limit");
+      return kErrLimit;
+    }
+    which[hs.nf].push_back(k);
+    by_nf[hs.nf].push_back(std::move(hs));
+    any = true;
+  }
+  if (!any) return kOk;
+  int st;
+  Context* cx = context(&st);
+  if (!cx) return st;
+  for (int nf = 1; nf <= kMaxFactors; ++nf) {
+    const std::vector<HostSweep>& sw = by_nf[nf];
+    const int n = (int)sw.size();
+    if (n == 0) continue;
+    // at least 32 codes per thread (each thread also writes a (nd+1) x nf slice)
+    std::vector<uint64_t> codes(n);
+    double total = 0.0;
+    for (int p = 0; p < n; ++p) {
+      codes[p] = sw[p].total_codes;
+      total += (double)codes[p];
+    }
+    const int64_t resident = sweep_resident_threads(nf, SweepOp::kGrad, cx->sm_count);
+    const int64_t want = std::max<int64_t>(n, std::min<int64_t>(resident, (int64_t)(total / 32.0)));
+    std::vector<int64_t> nthr(n);
+    for (int p = 0; p < n; ++p)
+      nthr[p] = std::max<int64_t>(1, std::min<int64_t>((int64_t)codes[p],
+                                                       (int64_t)std::floor(want * (double)codes[p] / total)));
+    std::vector<SweepProblem> probs(n);
+    int64_t pool_n = 0, threads = 0, gparts = 0;
+    int row = 0;
+    for (int p = 0; p < n; ++p) row = std::max(row, (sw[p].nd + 1) * nf);
+    for (int p = 0; p < n; ++p) {
+      const HostSweep& h = sw[p];
+      SweepProblem& Pp = probs[p];
+      memset(&Pp, 0, sizeof(Pp));
+      Pp.nd = h.nd;
+      Pp.nb = h.nb;
+      Pp.nf = h.nf;
+      Pp.kind = h.kind;
+      Pp.parity0 = h.parity0;
+      Pp.fx = h.fx;
+      Pp.has_base = h.has_base;
+      Pp.out_idx = p;
+      Pp.n_codes = (int64_t)h.total_codes;
+      Pp.thread_begin = threads;
+      Pp.n_threads = nthr[p];
+      Pp.mat_off = pool_n;
+      pool_n += (int64_t)h.D.size();
+      Pp.base_off = pool_n;
+      pool_n += (int64_t)h.base.size();
+      Pp.fixed_digit = (h.fixed_mode >= 0) ? 1 : 0;
+      Pp.part_off = gparts;
+      Pp.scale = h.scale;
+      for (int i = 0; i < h.nd; ++i) Pp.mult[i] = h.mult[i];
+      threads += nthr[p];
+      gparts += nthr[p] * (int64_t)(h.nd + Pp.fixed_digit) * nf;
+    }
+    size_t off = 0;
+    const size_t o_probs = off; off = align_up(off + sizeof(SweepProblem) * n, 256);
+    const size_t o_pool = off; off = align_up(off + sizeof(longlong2) * std::max<int64_t>(pool_n, 1), 256);
+    const size_t arena_bytes = off;
+    const size_t out_g = (size_t)n * row, out_p = (size_t)n;
+    if ((st = ensure(cx->plans, arena_bytes))) return st;
+    if ((st = ensure(cx->gpart, sizeof(double2) * std::max<int64_t>(gparts, 1)))) return st;
+    if ((st = ensure(cx->pperm, sizeof(double2) * std::max<int64_t>(threads, 1)))) return st;
+    if ((st = ensure(cx->out, sizeof(double2) * (out_g + out_p)))) return st;
+    if ((st = ensure_pinned(cx, std::max(arena_bytes, sizeof(double2) * (out_g + out_p))))) return st;
+    char* h = (char*)cx->pinned;
+    memcpy(h + o_probs, probs.data(), sizeof(SweepProblem) * n);
+    longlong2* hp = (longlong2*)(h + o_pool);
+    for (int p = 0; p < n; ++p) {
+      std::copy(sw[p].D.begin(), sw[p].D.end(), hp + probs[p].mat_off);
+      std::copy(sw[p].base.begin(), sw[p].base.end(), hp + probs[p].base_off);
+    }
+    char* d = (char*)cx->plans.ptr;
+    cudaError_t e = cudaMemcpyAsync(d, h, arena_bytes, cudaMemcpyHostToDevice, cx->stream);
+    if (e != cudaSuccess) return fail_cuda(e, "H2D gradient sweeps");
+    SweepLaunch L;
+    L.probs = (const SweepProblem*)(d + o_probs);
+    L.n_probs = n;
+    L.pool = (const longlong2*)(d + o_pool);
+    L.total_threads = threads;
+    L.partials = (double2*)cx->gpart.ptr;
+    L.partials2 = (double2*)cx->pperm.ptr;
+    L.grid = (int)((threads + 63) / 64);
+    if ((e = launch_sweep(nf, SweepOp::kGrad, L, cx->stream)) != cudaSuccess) return fail_cuda(e, "gradient sweep");
+    double2* dout = (double2*)cx->out.ptr;
+    if ((e = launch_grad_reduce(L.probs, n, L.partials, L.partials2, dout, dout + out_g, row, cx->stream)) !=
+        cudaSuccess)
+      return fail_cuda(e, "gradient reduce");
+    e = cudaMemcpyAsync(cx->pinned, dout, sizeof(double2) * (out_g + out_p), cudaMemcpyDeviceToHost, cx->stream);
+    if (e != cudaSuccess) return fail_cuda(e, "D2H gradients");
+    if ((e = cudaStreamSynchronize(cx->stream)) != cudaSuccess) return fail_cuda(e, "gradient sweep");
+    const double2* hg = (const double2*)cx->pinned;
+    const double2* hpm = hg + out_g;
+    for (int p = 0; p < n; ++p) {
+      const HostSweep& hs = sw[p];
+      const int k = which[nf][p];
+      P2[k] = hpm[p];
+      double2* gk = G2 + (size_t)k * len * len;
+      const int ndt = hs.nd + (hs.fixed_mode >= 0 ? 1 : 0);
+      for (int b = 0; b < ndt; ++b) {
+        const int bmode = (b < hs.nd) ? hs.digit_mode[b] : hs.fixed_mode;
+        for (int f = 0; f < nf; ++f) {
+          const int fmode = hs.factor_mode[f];
+          const int j = hs.digits_are_outputs ? bmode : fmode;  // output mode
+          const int i = hs.digits_are_outputs ? fmode : bmode;  // input mode
+          const double2 v = hg[(size_t)p * row + (size_t)b * nf + f];
+          gk[(size_t)j * len + i].x += v.x;
+          gk[(size_t)j * len + i].y += v.y;
+        }
+      }
     }
   }
   return kOk;

@@ -207,46 +207,83 @@ __global__ void __launch_bounds__(kFinWarps * 32) gccb_finalize_kernel(FinalizeA
   __syncwarp();
   // Laplace expansion perm(T + e_o) = sum_i S_i sub_i U[o][i]
   // (generalized_cliffords_b_simulation_strategy.py:82-89), then |.|^2.
+  if (lane < nd) {
+    const double mu = (double)mult_s[w][lane];
+    const double2 sv = sub_s[w][lane];
+    sub_s[w][lane] = make_double2(mu * sv.x, mu * sv.y);
+  }
+  __syncwarp();
   for (int o = lane; o < m; o += 32) {
     double re = 0.0, im = 0.0;
+    const double2* Urow = a.U + (size_t)o * m;
     for (int d = 0; d < nd; ++d) {
-      const double2 sv = sub_s[w][d];
-      const double mu = (double)mult_s[w][d];
-      const double2 u = a.U[(size_t)o * m + dm_s[w][d]];
-      const double cr = mu * sv.x, ci = mu * sv.y;
-      re = fma(cr, u.x, fma(-ci, u.y, re));
-      im = fma(cr, u.y, fma(ci, u.x, im));
+      const double2 c = sub_s[w][d];
+      const double2 u = Urow[dm_s[w][d]];
+      re = fma(c.x, u.x, fma(-c.y, u.y, re));
+      im = fma(c.x, u.y, fma(c.y, u.x, im));
     }
     pmf_s[w][o] = fma(re, re, im * im);
   }
   __syncwarp();
-  // Normalise with a sequential sum (Python's sum over the list), then
-  // numpy.random.choice: cdf = cumsum(p); cdf /= cdf[-1]; searchsorted(cdf, u, 'right').
-  double total = 0.0;
-  if (lane == 0)
-    for (int o = 0; o < m; ++o) total += pmf_s[w][o];
-  total = __shfl_sync(0xffffffffu, total, 0);
+  // theboss normalises with Python's sequential sum, and numpy.random.choice then
+  // takes cdf = cumsum(p), cdf /= cdf[-1], searchsorted(cdf, u, 'right')
+  // (generalized_cliffords_b_simulation_strategy.py:91-92, 107-110).  Fast path:
+  // the same quantities from a warp scan and a reciprocal, whose rounding differs
+  // from the sequential evaluation by far less than 1e-12 relative; whenever some
+  // cdf entry lies within 1e-12 of the uniform the sequential evaluation decides.
+  const double uu = a.uni[(size_t)j * a.n + (a.k - 1)];
+  const int K = (m + 31) >> 5;  // contiguous outputs per lane
+  const int o0 = lane * K;
+  double local = 0.0;
+  for (int q = 0; q < K; ++q)
+    if (o0 + q < m) local += pmf_s[w][o0 + q];
+  double incl = local;
+#pragma unroll
+  for (int off = 1; off < 32; off <<= 1) {
+    const double y = __shfl_up_sync(0xffffffffu, incl, off);
+    if (lane >= off) incl += y;
+  }
+  const double total_fast = __shfl_sync(0xffffffffu, incl, 31);
   int idx = 0;
-  if (!(total > 0.0) || !isfinite(total)) {
+  if (!(total_fast > 0.0) || !isfinite(total_fast)) {
     if (lane == 0) atomicOr(a.err, 1);
   } else {
-    for (int o = lane; o < m; o += 32) pmf_s[w][o] = pmf_s[w][o] / total;
-    __syncwarp();
-    if (lane == 0) {
-      double c = 0.0;
-      for (int o = 0; o < m; ++o) {
-        c += pmf_s[w][o];
-        pmf_s[w][o] = c;
-      }
-    }
-    __syncwarp();
-    const double last = pmf_s[w][m - 1];
-    const double uu = a.uni[(size_t)j * a.n + (a.k - 1)];
+    const double inv = 1.0 / total_fast;
+    double c = (incl - local) * inv;
     int cnt = 0;
-    for (int o = lane; o < m; o += 32) cnt += (pmf_s[w][o] / last <= uu) ? 1 : 0;
+    bool near = false;
+    for (int q = 0; q < K; ++q) {
+      if (o0 + q >= m) break;
+      c += pmf_s[w][o0 + q] * inv;  // ~ cdf / cdf[-1] (the last entry is ~1)
+      const double d = c - uu;
+      near |= (o0 + q < m - 1) && (fabs(d) <= 1e-12 * fmax(c, uu));
+      cnt += (d <= 0.0) ? 1 : 0;
+    }
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) cnt += __shfl_xor_sync(0xffffffffu, cnt, off);
     idx = cnt < m ? cnt : m - 1;
+    if (__any_sync(0xffffffffu, near)) {  // exact sequential evaluation
+      double total = 0.0;
+      if (lane == 0)
+        for (int o = 0; o < m; ++o) total += pmf_s[w][o];
+      total = __shfl_sync(0xffffffffu, total, 0);
+      for (int o = lane; o < m; o += 32) pmf_s[w][o] = pmf_s[w][o] / total;
+      __syncwarp();
+      if (lane == 0) {
+        double acc = 0.0;
+        for (int o = 0; o < m; ++o) {
+          acc += pmf_s[w][o];
+          pmf_s[w][o] = acc;
+        }
+      }
+      __syncwarp();
+      const double last = pmf_s[w][m - 1];
+      int cnt2 = 0;
+      for (int o = lane; o < m; o += 32) cnt2 += (pmf_s[w][o] / last <= uu) ? 1 : 0;
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) cnt2 += __shfl_xor_sync(0xffffffffu, cnt2, off);
+      idx = cnt2 < m ? cnt2 : m - 1;
+    }
   }
   if (lane == 0) T[idx] = (uint8_t)(T[idx] + 1);
   __syncwarp();
@@ -322,7 +359,8 @@ __global__ void __launch_bounds__(kFinWarps * 32) gccb_finalize_kernel(FinalizeA
     P.base_off = 0;
     P.part_off = ls.part_off;
     P.scale = 1.0;
-    P.reserved = 0.0;
+    P.fixed_digit = 0;
+    P.reserved = 0;
   }
 }
 
@@ -369,29 +407,42 @@ static int gccb_prepare(Context* cx, const double* matrix, int m, int n, int N, 
   // Per-level layout (levels 2..Lmax need sweeps).
   std::vector<std::vector<LevelSample>> tab(Lmax + 2);
   std::vector<int64_t> lvl_threads(Lmax + 2, 0), lvl_parts(Lmax + 2, 0), lvl_pool(Lmax + 2, 0);
-  std::vector<uint8_t> occ(m);
-  R.sweep_flops = 0.0;
+  // Code count and digit count of every (level, active sample), walked
+  // incrementally per sample: adding a particle to mode a multiplies the code
+  // count by (occ_a + 2) / (occ_a + 1).
+  std::vector<std::vector<uint64_t>> lvl_codes(Lmax + 2);
+  std::vector<std::vector<int>> lvl_nd(Lmax + 2);
   for (int k = 2; k <= Lmax; ++k) {
-    const int Ak = A[k];
-    std::vector<uint64_t> codes(Ak);
-    std::vector<int> ndv(Ak);
-    for (int jj = 0; jj < Ak; ++jj) {
+    lvl_codes[k].resize(A[k]);
+    lvl_nd[k].resize(A[k]);
+  }
+  R.sweep_flops = 0.0;
+  {
+    std::vector<uint8_t> occ(m, 0);
+    for (int jj = 0; jj < A[1]; ++jj) {
       const int s = order[jj];
-      std::fill(occ.begin(), occ.end(), 0);
-      for (int q = 0; q < k; ++q) occ[add[(size_t)s * n + q]]++;
       uint64_t c = 1;
       int nd = 0;
-      for (int i = 0; i < m; ++i)
-        if (occ[i]) {
-          ++nd;
-          c *= (uint64_t)occ[i] + 1;
+      for (int k = 1; k <= L[s]; ++k) {
+        const int md = add[(size_t)s * n + (k - 1)];
+        c = c / ((uint64_t)occ[md] + 1) * ((uint64_t)occ[md] + 2);
+        if (occ[md] == 0) ++nd;
+        occ[md]++;
+        if (k >= 2) {
+          lvl_codes[k][jj] = c;
+          lvl_nd[k][jj] = nd;
+          // algorithmic flops of theboss's all-minors sweep per code: (k-1) complex
+          // adds, (k-2) complex products, one sign, k/2 real-weighted adds = 9k - 12
+          R.sweep_flops += (double)c * (9.0 * k - 12.0);
         }
-      codes[jj] = c;
-      ndv[jj] = nd;
-      // algorithmic flops of theboss's all-minors sweep per code: (k-1) complex
-      // adds, (k-2) complex products, one sign, k/2 real-weighted adds = 9k - 12
-      R.sweep_flops += (double)c * (9.0 * k - 12.0);
+      }
+      for (int k = 0; k < L[s]; ++k) occ[add[(size_t)s * n + k]] = 0;
     }
+  }
+  for (int k = 2; k <= Lmax; ++k) {
+    const int Ak = A[k];
+    const std::vector<uint64_t>& codes = lvl_codes[k];
+    const std::vector<int>& ndv = lvl_nd[k];
     std::vector<int64_t> nthr;
     partition_threads(codes, sweep_resident_threads(k - 1, SweepOp::kMinors, cx->sm_count), nthr);
     auto& t = tab[k];

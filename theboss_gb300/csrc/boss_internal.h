@@ -11,7 +11,7 @@
 
 namespace boss {
 
-enum class SweepOp { kPerm = 0, kMinors = 1 };
+enum class SweepOp { kPerm = 0, kMinors = 1, kGrad = 2 };
 
 // Everything one sweep launch needs (device pointers).
 struct SweepLaunch {
@@ -20,6 +20,7 @@ struct SweepLaunch {
   const longlong2* pool = nullptr;
   int64_t total_threads = 0;
   double2* partials = nullptr;
+  double2* partials2 = nullptr;  // gradients: per-thread permanent partials
   int grid = 1;
 };
 
@@ -30,6 +31,8 @@ int64_t sweep_resident_threads(int nf, SweepOp op, int sm_count);
 cudaError_t launch_sweep(int nf, SweepOp op, const SweepLaunch& L, cudaStream_t st);
 cudaError_t launch_perm_reduce(const SweepProblem* probs, int n_probs, const double2* partials, double2* out,
                                cudaStream_t st);
+cudaError_t launch_grad_reduce(const SweepProblem* probs, int n_probs, const double2* gpart, const double2* ppart,
+                               double2* grad_out, double2* perm_out, int row_stride, cudaStream_t st);
 cudaError_t launch_minors_reduce(const SweepProblem* probs, int n_probs, const double2* partials, double2* out,
                                  int nd_max, cudaStream_t st);
 
@@ -53,6 +56,9 @@ struct HostSweep {
   double scale = 1.0;
   uint64_t total_codes = 1;
   int digit_mode[kMaxDigits] = {};  // digit -> mode (all-minors results)
+  int factor_mode[kMaxFactors] = {};  // factor -> mode (gradients)
+  int fixed_mode = -1;                // mode of the digit held at r = 0 (Glynn halving), or -1
+  bool digits_are_outputs = false;    // orientation of the sweep
 };
 
 // Status codes of the C ABI (include/boss.h repeats them).
@@ -79,7 +85,7 @@ struct Context {
   int device = 0;
   int sm_count = 0;
   cudaStream_t stream = nullptr;
-  DeviceBuffer plans, pool, partials, out, counter, index, misc;
+  DeviceBuffer plans, pool, partials, out, counter, index, misc, gpart, pperm;
   DeviceBuffer gccb[16];
   void* pinned = nullptr;
   size_t pinned_bytes = 0;

@@ -16,6 +16,11 @@ cudaError_t sweep_nf_b_prepare(int* perm_occ, int* minors_occ);
 cudaError_t sweep_nf_c_prepare(int* perm_occ, int* minors_occ);
 cudaError_t sweep_nf_d_prepare(int* perm_occ, int* minors_occ);
 
+cudaError_t sweep_nf_a_grad_occupancy(int nf, int* occ);
+cudaError_t sweep_nf_b_grad_occupancy(int nf, int* occ);
+cudaError_t sweep_nf_c_grad_occupancy(int nf, int* occ);
+cudaError_t sweep_nf_d_grad_occupancy(int nf, int* occ);
+
 static int g_perm_occ[kMaxFactors + 1];
 static int g_minors_occ[kMaxFactors + 1];
 
@@ -29,6 +34,18 @@ cudaError_t prepare_sweep_kernels() {
 
 int64_t sweep_resident_threads(int nf, SweepOp op, int sm_count) {
   if (nf < 1 || nf > kMaxFactors) return 128;
+  if (op == SweepOp::kGrad) {
+    int occ = 1;
+    cudaError_t e = (nf <= 8)    ? sweep_nf_a_grad_occupancy(nf, &occ)
+                    : (nf <= 16) ? sweep_nf_b_grad_occupancy(nf, &occ)
+                    : (nf <= 24) ? sweep_nf_c_grad_occupancy(nf, &occ)
+                                 : sweep_nf_d_grad_occupancy(nf, &occ);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      occ = 1;
+    }
+    return (int64_t)std::max(occ, 1) * sm_count * 64;
+  }
   const int occ = std::max(1, op == SweepOp::kPerm ? g_perm_occ[nf] : g_minors_occ[nf]);
   return (int64_t)occ * sm_count * 128;
 }
@@ -110,6 +127,50 @@ __global__ void minors_reduce_kernel(const SweepProblem* __restrict__ probs, con
     if (threadIdx.x == 0) out[(size_t)P.out_idx * nd_max + j] = make_double2(sr[0] * P.scale, si[0] * P.scale);
     __syncthreads();
   }
+}
+
+// One block per gradient sweep: every (digit, factor) entry of the per-thread
+// gradient slices and the per-thread permanents, summed over the sweep's threads
+// in a fixed order.  grad_out row = (nd + fixed) x nf entries.
+__global__ void grad_reduce_kernel(const SweepProblem* __restrict__ probs, const double2* __restrict__ gpart,
+                                   const double2* __restrict__ ppart, double2* __restrict__ grad_out,
+                                   double2* __restrict__ perm_out, int row_stride) {
+  __shared__ double sr[256], si[256];
+  const SweepProblem& P = probs[blockIdx.x];
+  const int ne = (P.nd + P.fixed_digit) * P.nf;
+  for (int e = threadIdx.x; e < ne; e += blockDim.x) {
+    double ar = 0.0, ai = 0.0;
+    for (int64_t q = 0; q < P.n_threads; ++q) {
+      const double2 v = gpart[P.part_off + q * ne + e];
+      ar += v.x;
+      ai += v.y;
+    }
+    grad_out[(size_t)P.out_idx * row_stride + e] = make_double2(ar * P.scale, ai * P.scale);
+  }
+  double ar = 0.0, ai = 0.0;
+  for (int64_t q = threadIdx.x; q < P.n_threads; q += blockDim.x) {
+    const double2 v = ppart[P.thread_begin + q];
+    ar += v.x;
+    ai += v.y;
+  }
+  sr[threadIdx.x] = ar;
+  si[threadIdx.x] = ai;
+  __syncthreads();
+  for (int s = blockDim.x >> 1; s > 0; s >>= 1) {
+    if ((int)threadIdx.x < s) {
+      sr[threadIdx.x] += sr[threadIdx.x + s];
+      si[threadIdx.x] += si[threadIdx.x + s];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) perm_out[P.out_idx] = make_double2(sr[0] * P.scale, si[0] * P.scale);
+}
+
+cudaError_t launch_grad_reduce(const SweepProblem* probs, int n_probs, const double2* gpart, const double2* ppart,
+                               double2* grad_out, double2* perm_out, int row_stride, cudaStream_t st) {
+  if (n_probs <= 0) return cudaSuccess;
+  grad_reduce_kernel<<<n_probs, 256, 0, st>>>(probs, gpart, ppart, grad_out, perm_out, row_stride);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_perm_reduce(const SweepProblem* probs, int n_probs, const double2* partials, double2* out,

@@ -62,7 +62,8 @@ struct SweepProblem {
   int64_t base_off;  // nf fixed-point complex
   int64_t part_off;  // partials: n_threads complex (perms) or n_threads x nd (all-minors)
   double scale;      // final real scale
-  double reserved;
+  int32_t fixed_digit;  // gradients: a binary digit held at r = 0 (Glynn halving) adds one weight-1 column
+  int32_t reserved;
   uint8_t mult[kMaxDigits];
 };
 
@@ -88,6 +89,10 @@ __device__ __forceinline__ double fx_to_double(long long x, int bias_exp) {
   const unsigned long long bits = (sgn << 63) | (e << 52) | mant;
   return __longlong_as_double(ax ? (long long)bits : 0ll);
 }
+
+// Compiler-only barrier: keeps the scheduler from hoisting all of a row's loads
+// at once (at large NF that alone would exhaust the register file).
+__device__ __forceinline__ void load_fence() { asm volatile("" ::: "memory"); }
 
 __device__ __forceinline__ double binom_small(int n, int k) {
   double r = 1.0;
@@ -143,6 +148,7 @@ __device__ __forceinline__ void decode_code(const SweepProblem& P, const longlon
     const longlong2* row = D + (size_t)i * NF;
 #pragma unroll
     for (int f = 0; f < NF; ++f) {
+      if (f > 0 && (f & 7) == 0) load_fence();
       const longlong2 d = row[f];
       sr[f] += d.x;
       si[f] += d.y;
@@ -175,20 +181,13 @@ template <int NF>
 __device__ __forceinline__ void flip_binary(const longlong2* __restrict__ D, int i, uint32_t bit, long long (&sr)[NF],
                                             long long (&si)[NF]) {
   const longlong2* row = D + (size_t)i * NF;
-  if (bit) {
+  const long long sgn = bit ? -1ll : 0ll;  // x ^ -1 - (-1) = -x
 #pragma unroll
-    for (int f = 0; f < NF; ++f) {
-      const longlong2 d = row[f];
-      sr[f] -= d.x;
-      si[f] -= d.y;
-    }
-  } else {
-#pragma unroll
-    for (int f = 0; f < NF; ++f) {
-      const longlong2 d = row[f];
-      sr[f] += d.x;
-      si[f] += d.y;
-    }
+  for (int f = 0; f < NF; ++f) {
+    if (f > 0 && (f & 7) == 0) load_fence();
+    const longlong2 d = row[f];
+    sr[f] += (d.x ^ sgn) - sgn;
+    si[f] += (d.y ^ sgn) - sgn;
   }
 }
 

@@ -156,10 +156,192 @@ __global__ void __launch_bounds__(128) minors_sweep_kernel(const SweepProblem* _
   for (int j = 0; j < nd; ++j) out[j] = M[j * 128];
 }
 
+
+// Gradient sweep (Glynn / Chin-Huh kind).  With s_f the factor sums and
+// w_b = mult_b - 2 r_b the weight of digit b, d perm / d U[mode f][mode b] is
+// scale * sum over the copies f of the mode of
+//     G_{b,f} = sum_r sign(r) prod C(mult, r) w_b(r) L_f(r),  L_f = prod_{f' != f} s_f'
+// (the derivative of the Chin-Huh sum; mult_b * copies(f) * minor once summed).
+// Per code the leave-one-out products come from a prefix array in registers and
+// a running suffix, and sign * L_f is added to a running total R_f (shared
+// memory).  w_b only changes when digit b flips, so G is settled at flips:
+// G_{b,.} += (w_b(before) - w_b(after)) * R_. , and at the end of each segment
+// G_{b,.} += w_b * R_. for every digit.  A halved (fixed) digit has w = 1.
+// The permanent itself is accumulated alongside (one fused product per code).
+// Per-thread G lives in global scratch: (nd + fixed) x NF complex, row = digit.
+template <int NF>
+__global__ void __launch_bounds__(64) grad_sweep_kernel(const SweepProblem* __restrict__ probs, int n_probs,
+                                                        const longlong2* __restrict__ pool, int64_t total_threads,
+                                                        double2* __restrict__ gpart, double2* __restrict__ ppart) {
+  extern __shared__ double2 grad_smem[];
+  const int64_t gt = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (gt >= total_threads) return;
+  const SweepProblem& P = probs[find_problem(probs, n_probs, gt)];
+  const int64_t q = gt - P.thread_begin;
+  const int nd = P.nd, ndt = P.nd + P.fixed_digit;
+  double2* R = grad_smem + threadIdx.x;             // running sign * L_f, R[f * 64]
+  double2* Pp = grad_smem + NF * 64 + threadIdx.x;  // prefix products, Pp[f * 64]
+  double2* Bf = grad_smem + 2 * NF * 64 + threadIdx.x;  // this code's factors, Bf[f * 64]
+  double2* G = gpart + P.part_off + q * (int64_t)(ndt * NF);
+  uint64_t touched = 0;  // rows of G written so far (the first write of a row stores, later ones add)
+  double totr = 0.0, toti = 0.0;  // weighted permanent over finished segments
+  int64_t a, len;
+  thread_range(P, q, a, len);
+  const longlong2* D = pool + P.mat_off;
+  const longlong2* base = pool + P.base_off;
+  const int bias = 1023 + 63 - P.fx;
+  const int nb = P.nb;
+  const uint64_t end = (uint64_t)(a + len);
+  const uint64_t block = (nb < 64) ? (1ull << nb) : 0ull;  // multi-valued digits change every 2^nb codes
+  // Segments: runs of codes over which every multi-valued digit is constant.
+  for (uint64_t seg = (uint64_t)a; seg < end;) {
+    const uint64_t seg_end = block ? ((seg / block + 1) * block < end ? (seg / block + 1) * block : end) : end;
+    long long sr[NF], si[NF];
+    uint64_t g;
+    uint32_t parity;
+    double w;
+    decode_code<NF>(P, D, base, seg, sr, si, g, parity, w);
+#pragma unroll
+    for (int f = 0; f < NF; ++f) R[f * 64] = make_double2(0.0, 0.0);
+    double permr = 0.0, permi = 0.0;
+    for (uint64_t t = seg;; ++t) {
+      // ---- this code: leave-one-out products into R, the full product into perm ----
+      const uint32_t neg = parity << 31;
+      if (NF == 1) {
+        double2 v = R[0];
+        v.x += xor_sign(1.0, neg);
+        R[0] = v;
+        permr += xor_sign(fx_to_double(sr[0], bias), neg);
+        permi += xor_sign(fx_to_double(si[0], bias), neg);
+      } else {
+        // the factors as doubles, once, into shared memory
+#pragma unroll
+        for (int f = 0; f < NF; ++f) {
+          if (f > 0 && (f & 7) == 0) load_fence();
+          Bf[f * 64] = make_double2(fx_to_double(sr[f], bias), fx_to_double(si[f], bias));
+        }
+        load_fence();
+        // prefix products P_f = B_0 ... B_f (f <= NF - 2)
+        double2 pv = Bf[0];
+        Pp[0] = pv;
+#pragma unroll
+        for (int f = 1; f < NF - 1; ++f) {
+          const double2 bv = Bf[f * 64];
+          const double t_re = fma(pv.x, bv.x, -(pv.y * bv.y));
+          const double t_im = fma(pv.x, bv.y, pv.y * bv.x);
+          pv = make_double2(t_re, t_im);
+          Pp[f * 64] = pv;
+        }
+        load_fence();
+        double2 qv = Bf[(NF - 1) * 64];
+        const double pnr = xor_sign(pv.x, neg), pni = xor_sign(pv.y, neg);
+        permr = fma(pnr, qv.x, permr);
+        permr = fma(-pni, qv.y, permr);
+        permi = fma(pnr, qv.y, permi);
+        permi = fma(pni, qv.x, permi);
+        {
+          double2 v = R[(NF - 1) * 64];
+          v.x += pnr;
+          v.y += pni;
+          R[(NF - 1) * 64] = v;
+        }
+#pragma unroll
+        for (int f = NF - 2; f >= 1; --f) {
+          const double2 Pv = Pp[(f - 1) * 64];
+          const double lr = xor_sign(Pv.x, neg), li = xor_sign(Pv.y, neg);
+          double2 v = R[f * 64];
+          v.x = fma(lr, qv.x, v.x);
+          v.x = fma(-li, qv.y, v.x);
+          v.y = fma(lr, qv.y, v.y);
+          v.y = fma(li, qv.x, v.y);
+          R[f * 64] = v;
+          const double2 bv = Bf[f * 64];
+          const double nqr = fma(qv.x, bv.x, -(qv.y * bv.y));
+          const double nqi = fma(qv.x, bv.y, qv.y * bv.x);
+          qv = make_double2(nqr, nqi);
+        }
+        double2 v = R[0];
+        v.x += xor_sign(qv.x, neg);
+        v.y += xor_sign(qv.y, neg);
+        R[0] = v;
+        load_fence();
+      }
+      if (t + 1 >= seg_end) break;
+      // ---- step to code t + 1: a binary digit flips ----
+      const int i = __ffsll((long long)(t + 1)) - 1;
+      const uint32_t bit = (uint32_t)(g >> i) & 1u;
+      // its weight goes 1 - 2 bit -> 2 bit - 1: G_i += 2 (1 - 2 bit) w R
+      const double cc = (bit ? -2.0 : 2.0) * w;
+      double2* Gi = G + (size_t)i * NF;
+      if ((touched >> i) & 1ull) {
+#pragma unroll
+        for (int f = 0; f < NF; ++f) {
+          if (f > 0 && (f & 7) == 0) load_fence();
+          const double2 r = R[f * 64];
+          double2 gv = Gi[f];
+          gv.x = fma(cc, r.x, gv.x);
+          gv.y = fma(cc, r.y, gv.y);
+          Gi[f] = gv;
+        }
+      } else {
+        touched |= 1ull << i;
+#pragma unroll
+        for (int f = 0; f < NF; ++f) {
+          const double2 r = R[f * 64];
+          Gi[f] = make_double2(cc * r.x, cc * r.y);
+        }
+      }
+      g ^= 1ull << i;
+      flip_binary<NF>(D, i, bit, sr, si);
+      parity ^= 1u;
+    }
+    // settle the segment: every digit receives its current weight times R
+    for (int bd = 0; bd < ndt; ++bd) {
+      double wb;
+      if (bd < nb) wb = ((g >> bd) & 1ull) ? -1.0 : 1.0;
+      else if (bd < nd) wb = (double)P.mult[bd] - 2.0 * (double)digit_value(P, seg, bd);
+      else wb = 1.0;
+      wb *= w;
+      double2* Gb = G + (size_t)bd * NF;
+      if ((touched >> bd) & 1ull) {
+#pragma unroll
+        for (int f = 0; f < NF; ++f) {
+          if (f > 0 && (f & 7) == 0) load_fence();
+          const double2 r = R[f * 64];
+          double2 gv = Gb[f];
+          gv.x = fma(wb, r.x, gv.x);
+          gv.y = fma(wb, r.y, gv.y);
+          Gb[f] = gv;
+        }
+      } else {
+        touched |= 1ull << bd;
+#pragma unroll
+        for (int f = 0; f < NF; ++f) {
+          const double2 r = R[f * 64];
+          Gb[f] = make_double2(wb * r.x, wb * r.y);
+        }
+      }
+    }
+    totr = fma(w, permr, totr);
+    toti = fma(w, permi, toti);
+    seg = seg_end;
+  }
+  for (int bd = 0; bd < ndt; ++bd)
+    if (!((touched >> bd) & 1ull))
+      for (int f = 0; f < NF; ++f) G[(size_t)bd * NF + f] = make_double2(0.0, 0.0);
+  ppart[gt] = make_double2(totr, toti);
+}
+
 constexpr size_t kMinorsSmem = (size_t)kMaxMinorDigits * 128 * sizeof(double2);
+constexpr size_t kGradSmem = (size_t)(3 * kMaxFactors) * 64 * sizeof(double2);
 
 template <int NF>
 cudaError_t sweep_launch_t(SweepOp op, const SweepLaunch& L, cudaStream_t st) {
+  if (op == SweepOp::kGrad) {
+    grad_sweep_kernel<NF><<<L.grid, 64, (size_t)(3 * NF) * 64 * sizeof(double2), st>>>(
+        L.probs, L.n_probs, L.pool, L.total_threads, L.partials, L.partials2);
+    return cudaGetLastError();
+  }
   if (op == SweepOp::kPerm) {
     perm_sweep_kernel<NF><<<L.grid, 128, 0, st>>>(L.probs, L.n_probs, L.pool, L.total_threads, L.partials);
   } else {
@@ -170,9 +352,17 @@ cudaError_t sweep_launch_t(SweepOp op, const SweepLaunch& L, cudaStream_t st) {
 }
 
 template <int NF>
+cudaError_t grad_occupancy_t(int* blocks_per_sm) {
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, grad_sweep_kernel<NF>, 64,
+                                                       (size_t)(3 * NF) * 64 * sizeof(double2));
+}
+
+template <int NF>
 cudaError_t sweep_prepare_t(int* perm_blocks_per_sm, int* minors_blocks_per_sm) {
   cudaError_t e = cudaFuncSetAttribute(minors_sweep_kernel<NF>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)kMinorsSmem);
+  if (e != cudaSuccess) return e;
+  e = cudaFuncSetAttribute(grad_sweep_kernel<NF>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kGradSmem);
   if (e != cudaSuccess) return e;
   e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(perm_blocks_per_sm, perm_sweep_kernel<NF>, 128, 0);
   if (e != cudaSuccess) return e;
@@ -195,6 +385,19 @@ cudaError_t sweep_prepare_t(int* perm_blocks_per_sm, int* minors_blocks_per_sm) 
       case 5: return sweep_launch_t<(LO) + 5>(op, L, st);                                                \
       case 6: return sweep_launch_t<(LO) + 6>(op, L, st);                                                \
       case 7: return sweep_launch_t<(LO) + 7>(op, L, st);                                                \
+      default: return cudaErrorInvalidValue;                                                             \
+    }                                                                                                    \
+  }                                                                                                      \
+  cudaError_t NAME##_grad_occupancy(int nf, int* occ) {                                                  \
+    switch (nf - (LO)) {                                                                                 \
+      case 0: return grad_occupancy_t<(LO) + 0>(occ);                                                    \
+      case 1: return grad_occupancy_t<(LO) + 1>(occ);                                                    \
+      case 2: return grad_occupancy_t<(LO) + 2>(occ);                                                    \
+      case 3: return grad_occupancy_t<(LO) + 3>(occ);                                                    \
+      case 4: return grad_occupancy_t<(LO) + 4>(occ);                                                    \
+      case 5: return grad_occupancy_t<(LO) + 5>(occ);                                                    \
+      case 6: return grad_occupancy_t<(LO) + 6>(occ);                                                    \
+      case 7: return grad_occupancy_t<(LO) + 7>(occ);                                                    \
       default: return cudaErrorInvalidValue;                                                             \
     }                                                                                                    \
   }                                                                                                      \
