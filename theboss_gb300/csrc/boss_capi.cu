@@ -627,10 +627,13 @@ int boss_perm_grad_batch(const double* matrix, int32_t m, const int32_t* input_s
     }
     const int64_t resident = sweep_resident_threads(nf, SweepOp::kGrad, cx->sm_count);
     const int64_t want = std::max<int64_t>(n, std::min<int64_t>(resident, (int64_t)(total / 32.0)));
+    // whole groups of 32 threads per sweep (the gradient slices interleave by lane),
+    // rounded down so the launch stays within one wave of resident threads
     std::vector<int64_t> nthr(n);
-    for (int p = 0; p < n; ++p)
-      nthr[p] = std::max<int64_t>(1, std::min<int64_t>((int64_t)codes[p],
-                                                       (int64_t)std::floor(want * (double)codes[p] / total)));
+    for (int p = 0; p < n; ++p) {
+      const int64_t t = (int64_t)std::floor(want * (double)codes[p] / total);
+      nthr[p] = std::max<int64_t>(32, t / 32 * 32);
+    }
     std::vector<SweepProblem> probs(n);
     int64_t pool_n = 0, threads = 0, gparts = 0;
     int row = 0;
@@ -659,7 +662,7 @@ int boss_perm_grad_batch(const double* matrix, int32_t m, const int32_t* input_s
       Pp.scale = h.scale;
       for (int i = 0; i < h.nd; ++i) Pp.mult[i] = h.mult[i];
       threads += nthr[p];
-      gparts += nthr[p] * (int64_t)(h.nd + Pp.fixed_digit) * nf;
+      gparts += nthr[p] * (int64_t)(h.nd + Pp.fixed_digit) * nf;  // nthr is a multiple of 32
     }
     size_t off = 0;
     const size_t o_probs = off; off = align_up(off + sizeof(SweepProblem) * n, 256);

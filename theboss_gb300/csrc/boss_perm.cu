@@ -141,7 +141,7 @@ __global__ void grad_reduce_kernel(const SweepProblem* __restrict__ probs, const
   for (int e = threadIdx.x; e < ne; e += blockDim.x) {
     double ar = 0.0, ai = 0.0;
     for (int64_t q = 0; q < P.n_threads; ++q) {
-      const double2 v = gpart[P.part_off + q * ne + e];
+      const double2 v = gpart[P.part_off + ((q >> 5) * ne + e) * 32 + (q & 31)];
       ar += v.x;
       ai += v.y;
     }

@@ -182,7 +182,9 @@ __global__ void __launch_bounds__(64) grad_sweep_kernel(const SweepProblem* __re
   double2* R = grad_smem + threadIdx.x;             // running sign * L_f, R[f * 64]
   double2* Pp = grad_smem + NF * 64 + threadIdx.x;  // prefix products, Pp[f * 64]
   double2* Bf = grad_smem + 2 * NF * 64 + threadIdx.x;  // this code's factors, Bf[f * 64]
-  double2* G = gpart + P.part_off + q * (int64_t)(ndt * NF);
+  // Per-thread gradient slices are interleaved by lane within each group of 32
+  // threads ([group][row][factor][lane]) so a warp's row updates coalesce.
+  double2* G = gpart + P.part_off + (q >> 5) * (int64_t)(ndt * NF) * 32 + (q & 31);
   uint64_t touched = 0;  // rows of G written so far (the first write of a row stores, later ones add)
   double totr = 0.0, toti = 0.0;  // weighted permanent over finished segments
   int64_t a, len;
@@ -272,23 +274,23 @@ __global__ void __launch_bounds__(64) grad_sweep_kernel(const SweepProblem* __re
       const uint32_t bit = (uint32_t)(g >> i) & 1u;
       // its weight goes 1 - 2 bit -> 2 bit - 1: G_i += 2 (1 - 2 bit) w R
       const double cc = (bit ? -2.0 : 2.0) * w;
-      double2* Gi = G + (size_t)i * NF;
+      double2* Gi = G + (size_t)i * NF * 32;
       if ((touched >> i) & 1ull) {
 #pragma unroll
         for (int f = 0; f < NF; ++f) {
           if (f > 0 && (f & 7) == 0) load_fence();
           const double2 r = R[f * 64];
-          double2 gv = Gi[f];
+          double2 gv = Gi[f * 32];
           gv.x = fma(cc, r.x, gv.x);
           gv.y = fma(cc, r.y, gv.y);
-          Gi[f] = gv;
+          Gi[f * 32] = gv;
         }
       } else {
         touched |= 1ull << i;
 #pragma unroll
         for (int f = 0; f < NF; ++f) {
           const double2 r = R[f * 64];
-          Gi[f] = make_double2(cc * r.x, cc * r.y);
+          Gi[f * 32] = make_double2(cc * r.x, cc * r.y);
         }
       }
       g ^= 1ull << i;
@@ -302,23 +304,23 @@ __global__ void __launch_bounds__(64) grad_sweep_kernel(const SweepProblem* __re
       else if (bd < nd) wb = (double)P.mult[bd] - 2.0 * (double)digit_value(P, seg, bd);
       else wb = 1.0;
       wb *= w;
-      double2* Gb = G + (size_t)bd * NF;
+      double2* Gb = G + (size_t)bd * NF * 32;
       if ((touched >> bd) & 1ull) {
 #pragma unroll
         for (int f = 0; f < NF; ++f) {
           if (f > 0 && (f & 7) == 0) load_fence();
           const double2 r = R[f * 64];
-          double2 gv = Gb[f];
+          double2 gv = Gb[f * 32];
           gv.x = fma(wb, r.x, gv.x);
           gv.y = fma(wb, r.y, gv.y);
-          Gb[f] = gv;
+          Gb[f * 32] = gv;
         }
       } else {
         touched |= 1ull << bd;
 #pragma unroll
         for (int f = 0; f < NF; ++f) {
           const double2 r = R[f * 64];
-          Gb[f] = make_double2(wb * r.x, wb * r.y);
+          Gb[f * 32] = make_double2(wb * r.x, wb * r.y);
         }
       }
     }
@@ -328,7 +330,7 @@ __global__ void __launch_bounds__(64) grad_sweep_kernel(const SweepProblem* __re
   }
   for (int bd = 0; bd < ndt; ++bd)
     if (!((touched >> bd) & 1ull))
-      for (int f = 0; f < NF; ++f) G[(size_t)bd * NF + f] = make_double2(0.0, 0.0);
+      for (int f = 0; f < NF; ++f) G[((size_t)bd * NF + f) * 32] = make_double2(0.0, 0.0);
   ppart[gt] = make_double2(totr, toti);
 }
 

@@ -149,10 +149,14 @@ class GCCBPlainDriver(GeneralizedCliffordsBUniformLossesSimulationStrategy):
 
 
 class GeneralizedCliffordsSimulationStrategy(SimulationStrategyInterface):
-    """Plain (A-version) generalized C&C: per new output prefix, every output's
-    probability is a weighted sum of |perm|^2 over the input's sub-multisets; all
-    permanents of one layer go to the GPU in one batched launch.  Layers are
-    memoised per prefix and sampling follows generalized_cliffords_simulation_strategy.py:249-266."""
+    """Plain (A-version) generalized C&C (generalized_cliffords_simulation_strategy.py:20-266).
+
+    Per new output prefix r, every output r + e_j gets the probability
+    sum_S w_S |perm(U[r + e_j, S])|^2 / (prod S! |S|!) over the input's
+    sub-multisets S with |r| + 1 particles; layers are memoised per prefix.  theboss
+    draws exactly one numpy random() per sampling step, so the whole stream is drawn
+    up front (same calls, same order) and all samples advance together step by
+    step: each step's new prefixes become one batched GPU permanent launch."""
 
     def __init__(self, bs_permanent_calculator: BSPermanentCalculatorInterface) -> None:
         self.r_sample: List[int] = []
@@ -169,15 +173,17 @@ class GeneralizedCliffordsSimulationStrategy(SimulationStrategyInterface):
         self._bs_permanent_calculator.matrix = new_matrix
 
     def simulate(self, input_state, samples_number: int = 1):
+        self._initialize(input_state)
+        n = self.number_of_input_photons
+        steps = [n] * int(samples_number)
+        uniforms = np.random.random(n * int(samples_number)) if n > 0 else np.zeros(0)
+        return [tuple(r) for r in self._run(steps, uniforms, len(input_state))]
+
+    def _initialize(self, input_state) -> None:
         self.input_state = input_state
         self.number_of_input_photons = int(sum(input_state))
         self._get_sorted_possible_states()
         self.pmfs = dict()
-        samples = []
-        while len(samples) < samples_number:
-            self._fill_r_sample()
-            samples.append(tuple(self.r_sample))
-        return samples
 
     def _get_sorted_possible_states(self) -> None:
         states = [()]
@@ -187,16 +193,47 @@ class GeneralizedCliffordsSimulationStrategy(SimulationStrategyInterface):
         for s in states:
             self._labeled_states[sum(s)].append(np.array(s, dtype=np.int64))
 
-    def _fill_r_sample(self) -> None:
-        self.r_sample = [0 for _ in self.input_state]
-        self.current_key = tuple(self.r_sample)
-        self.current_sample_probability = 1
-        while self.number_of_input_photons > sum(self.r_sample):
-            if self.current_key not in self.pmfs:
-                self._calculate_new_layer_of_pmfs()
-            self._sample_from_latest_pmf()
+    def _run(self, steps, uniforms, width: int) -> List[List[int]]:
+        """Advances every sample step by step; steps[s] sampling steps for sample s,
+        uniforms consumed in sample-major order (theboss's order)."""
+        N = len(steps)
+        offsets = np.concatenate([[0], np.cumsum(steps)]).astype(np.int64)
+        r = [[0] * width for _ in range(N)]
+        for k in range(max(steps, default=0)):
+            active = [sidx for sidx in range(N) if steps[sidx] > k]
+            missing = []
+            seen = set()
+            for sidx in active:
+                key = tuple(r[sidx])
+                if key not in self.pmfs and key not in seen:
+                    seen.add(key)
+                    missing.append(list(key))
+            if missing:
+                self._calculate_layers(missing)
+            for sidx in active:
+                key = tuple(r[sidx])
+                r[sidx] = self._sample(key, uniforms[offsets[sidx] + k])
+        if N:
+            self.r_sample = r[-1]
+            self.current_key = tuple(self.r_sample)
+        return r
+
+    def _sample(self, key, u: float) -> List[int]:
+        """generalized_cliffords_simulation_strategy.py:249-266."""
+        pmf = self.pmfs[key]
+        idx = 0
+        rv = u * sum(pmf)
+        acc = 0
+        for p in pmf:
+            acc += p
+            if acc > rv:
+                break
+            idx += 1
+        self.current_sample_probability = pmf[idx]
+        return self.possible_outputs[key][idx]
 
     def _weights(self, k_vectors) -> np.ndarray:
+        """generalized_cliffords_simulation_strategy.py:173-205."""
         from scipy.special import binom
 
         n = int(sum(self.input_state))
@@ -209,90 +246,68 @@ class GeneralizedCliffordsSimulationStrategy(SimulationStrategyInterface):
             out.append(w)
         return np.asarray(out, dtype=np.float64)
 
-    def _layer_probabilities(self, inputs, outputs) -> np.ndarray:
-        """|perm(U[out, in])|^2 / prod(in!) / |in|! for every (output, input) pair,
-        as one batched GPU call.  Returns (len(outputs), len(inputs))."""
-        n_in = len(inputs)
+    def _calculate_layers(self, prefixes: List[List[int]]) -> None:
+        """Layers of every prefix in `prefixes` (all with the same particle count):
+        one batched permanent launch for all (prefix, output, input) triples."""
+        k = sum(prefixes[0]) + 1
+        inputs = self._labeled_states[k]
+        weights = self._weights([[self.input_state[i] - st[i] for i in range(len(st))] for st in inputs])
+        weights /= sum(weights)
+        m = len(prefixes[0])
+        outs = []
+        for pre in prefixes:
+            layer = []
+            for j in range(m):
+                o = list(pre)
+                o[j] += 1
+                layer.append(o)
+            outs.append(layer)
+        P, C = len(prefixes), len(inputs)
         L = len(self.input_state)
-        S = np.repeat(np.asarray(inputs, dtype=np.int32).reshape(1, n_in, L), len(outputs), axis=0).reshape(-1, L)
-        T = np.repeat(np.asarray(outputs, dtype=np.int32), n_in, axis=0)
+        T = np.repeat(np.asarray(outs, dtype=np.int32).reshape(P * m, 1, m), C, axis=1).reshape(-1, m)
+        S = np.tile(np.asarray(inputs, dtype=np.int32).reshape(1, C, L), (P * m, 1, 1)).reshape(-1, L)
         calc = self._bs_permanent_calculator
         variant = getattr(calc, "_VARIANT", _native.RYSER)
-        perms = _native.perm_batch(_native.as_matrix(calc.matrix), np.ascontiguousarray(S), np.ascontiguousarray(T),
-                                   variant)
-        prob = (np.abs(perms) ** 2).reshape(len(outputs), n_in)
-        # generalized_cliffords_simulation_strategy.py:240-245: one division per mode, then by |S|!
-        for i, s in enumerate(inputs):
-            for v in s:
-                prob[:, i] /= factorial(int(v))
-            prob[:, i] /= factorial(int(sum(s)))
-        return prob
-
-    def _calculate_new_layer_of_pmfs(self) -> None:
-        k = sum(self.r_sample) + 1
-        inputs = self._labeled_states[k]
-        weights = self._weights([[self.input_state[i] - s[i] for i in range(len(s))] for s in inputs])
-        weights /= sum(weights)
-        outputs = self._generate_possible_output_states()
-        self.possible_outputs[self.current_key] = outputs
-        probs = self._layer_probabilities(inputs, outputs)
-        pmf = []
-        for o in range(len(outputs)):
-            acc = 0
-            for i in range(len(inputs)):
-                acc += probs[o, i] * weights[i]
-            pmf.append(acc)
-        self.pmfs[self.current_key] = pmf
-
-    def _generate_possible_output_states(self) -> List[List[int]]:
-        out = []
-        for i in range(len(self.r_sample)):
-            new = copy(self.r_sample)
-            new[i] += 1
-            out.append(new)
-        return out
-
-    def _sample_from_latest_pmf(self) -> None:
-        pmf = self.pmfs[self.current_key]
-        idx = 0
-        rv = np.random.random() * sum(pmf)
-        acc = 0
-        for p in pmf:
-            acc += p
-            if acc > rv:
-                break
-            idx += 1
-        self.current_sample_probability = pmf[idx]
-        self.r_sample = self.possible_outputs[self.current_key][idx]
-        self.current_key = tuple(self.r_sample)
+        perms = _native.perm_batch(_native.as_matrix(calc.matrix), np.ascontiguousarray(S),
+                                   np.ascontiguousarray(T), variant)
+        prob = (np.abs(perms) ** 2).reshape(P, m, C)
+        # generalized_cliffords_simulation_strategy.py:240-245: one division per
+        # occupied mode factorial, then by |S|!
+        for i, st in enumerate(inputs):
+            for v in st:
+                prob[:, :, i] /= factorial(int(v))
+            prob[:, :, i] /= factorial(int(sum(st)))
+        pmf = np.zeros((P, m))
+        for i in range(C):  # :160-169, sequential over the inputs
+            pmf += prob[:, :, i] * weights[i]
+        for p_idx, pre in enumerate(prefixes):
+            key = tuple(pre)
+            self.possible_outputs[key] = outs[p_idx]
+            self.pmfs[key] = list(pmf[p_idx])
 
 
 class GeneralizedCliffordsUniformLossesSimulationStrategy(GeneralizedCliffordsSimulationStrategy):
-    """A-version with per-photon uniform losses drawn from Python's ``random``
-    module (generalized_cliffords_uniform_losses_simulation_strategy.py:125-138)."""
+    """A-version with per-photon uniform losses: each photon survives when Python's
+    random.random() < transmissivity (generalized_cliffords_uniform_losses_simulation_strategy.py:125-138),
+    then one numpy random() per surviving photon.  The two generators are
+    independent, so both streams are drawn up front in theboss's order."""
 
     def __init__(self, bs_permanent_calculator: BSPermanentCalculatorInterface, transmissivity: float = 0) -> None:
         self._transmissivity = transmissivity
         super().__init__(bs_permanent_calculator)
 
     def simulate(self, input_state, samples_number: int = 1) -> List[np.ndarray]:
-        self.input_state = input_state
-        self.number_of_input_photons = int(sum(input_state))
-        self._get_sorted_possible_states()
-        self.pmfs = dict()
-        samples = []
-        while len(samples) < samples_number:
-            self._fill_r_sample()
-            samples.append(np.array(self.r_sample, dtype=np.int64))
-        return samples
-
-    def _fill_r_sample(self) -> None:
-        self.r_sample = [0 for _ in self._bs_permanent_calculator.matrix]
-        self.current_key = tuple(self.r_sample)
-        self.current_sample_probability = 1
-        for _ in range(self.number_of_input_photons):
-            if _stdlib_random.random() >= self._transmissivity:
-                continue
-            if self.current_key not in self.pmfs:
-                self._calculate_new_layer_of_pmfs()
-            self._sample_from_latest_pmf()
+        self._initialize(input_state)
+        n = self.number_of_input_photons
+        N = int(samples_number)
+        kept = []
+        for _ in range(N):
+            c = 0
+            for _photon in range(n):
+                if _stdlib_random.random() >= self._transmissivity:
+                    continue
+                c += 1
+            kept.append(c)
+        uniforms = np.random.random(sum(kept)) if sum(kept) else np.zeros(0)
+        width = len(self._bs_permanent_calculator.matrix)
+        return [np.array(r, dtype=np.int64) for r in self._run(kept, uniforms, width)]
