@@ -41,13 +41,20 @@ struct MT19937 {
 
   void twist() {
     const uint32_t upper = 0x80000000u, lower = 0x7fffffffu, a = 0x9908b0dfu;
-    for (int i = 0; i < 624; ++i) {
-      const uint32_t y = (key[i] & upper) | (key[(i + 1) % 624] & lower);
-      key[i] = key[(i + 397) % 624] ^ (y >> 1) ^ ((y & 1u) ? a : 0u);
+    int i = 0;
+    for (; i < 624 - 397; ++i) {
+      const uint32_t y = (key[i] & upper) | (key[i + 1] & lower);
+      key[i] = key[i + 397] ^ (y >> 1) ^ ((0u - (y & 1u)) & a);
     }
+    for (; i < 623; ++i) {
+      const uint32_t y = (key[i] & upper) | (key[i + 1] & lower);
+      key[i] = key[i + 397 - 624] ^ (y >> 1) ^ ((0u - (y & 1u)) & a);
+    }
+    const uint32_t y = (key[623] & upper) | (key[0] & lower);
+    key[623] = key[396] ^ (y >> 1) ^ ((0u - (y & 1u)) & a);
     pos = 0;
   }
-  uint32_t next32() {
+  inline uint32_t next32() {
     if (pos >= 624) twist();
     uint32_t y = key[pos++];
     y ^= y >> 11;
@@ -57,27 +64,31 @@ struct MT19937 {
     return y;
   }
   // 53-bit uniform in [0, 1): numpy.random.random / random_sample.
-  double next_double() {
+  inline double next_double() {
     const uint32_t a = next32() >> 5, b = next32() >> 6;
     return (a * 67108864.0 + b) / 9007199254740992.0;
   }
-  // numpy.random.randint(0, n) for 1 <= n <= 2^32: masked rejection sampling on
-  // 32-bit draws; n == 1 draws nothing.
-  uint32_t bounded(uint64_t n) {
-    const uint64_t rng = n - 1;
+  // numpy.random.randint(0, n) for 1 <= n: masked rejection sampling on 32-bit
+  // draws with mask = the smallest 2^k - 1 >= n - 1; n == 1 draws nothing.
+  inline uint32_t bounded(uint32_t n, uint32_t mask) {
+    const uint32_t rng = n - 1;
     if (rng == 0) return 0;
-    uint32_t mask = (uint32_t)rng;
-    mask |= mask >> 1;
-    mask |= mask >> 2;
-    mask |= mask >> 4;
-    mask |= mask >> 8;
-    mask |= mask >> 16;
     uint32_t v;
     while ((v = (next32() & mask)) > rng) {
     }
     return v;
   }
 };
+
+static inline uint32_t mask_for(uint32_t n) {
+  uint32_t m = n - 1;
+  m |= m >> 1;
+  m |= m >> 2;
+  m |= m >> 4;
+  m |= m >> 8;
+  m |= m >> 16;
+  return m;
+}
 
 // The whole random stream of `n_samples` GC&C-B samples, in theboss's draw order.
 static int predraw(const int32_t* input_state, int m, const double* weights, int n_weights, MT19937& mt,
@@ -97,10 +108,16 @@ static int predraw(const int32_t* input_state, int m, const double* weights, int
     set_error("particle-number weights must have n + 1 entries");
     return kErrArg;
   }
+  if (n > 255) {
+    set_error("at most 255 input particles");
+    return kErrLimit;
+  }
   L.assign(n_samples, 0);
   add.assign((size_t)n_samples * std::max(n, 1), 0);
   u.assign((size_t)n_samples * std::max(n, 1), 0.0);
-  std::vector<int> work;
+  uint32_t masks[257];
+  for (int r = 1; r <= n; ++r) masks[r] = mask_for((uint32_t)r);
+  uint8_t work[256];
   for (int s = 0; s < n_samples; ++s) {
     int l = n;
     if (weights) {  // generalized_cliffords_b_uniform_losses_simulation_strategy.py:67-85
@@ -118,12 +135,16 @@ static int predraw(const int32_t* input_state, int m, const double* weights, int
       }
     }
     L[s] = l;
-    work.assign(particles.begin(), particles.end());
+    for (int k = 0; k < n; ++k) work[k] = (uint8_t)particles[k];
+    int remaining = n;
+    uint8_t* as = &add[(size_t)s * n];
+    double* us = &u[(size_t)s * n];
     for (int k = 0; k < l; ++k) {  // generalized_cliffords_b_simulation_strategy.py:97-110
-      const uint32_t idx = mt.bounded(work.size());
-      add[(size_t)s * n + k] = (uint8_t)work[idx];
-      work.erase(work.begin() + idx);
-      u[(size_t)s * n + k] = mt.next_double();
+      const uint32_t idx = mt.bounded((uint32_t)remaining, masks[remaining]);
+      as[k] = work[idx];
+      for (int q = (int)idx; q + 1 < remaining; ++q) work[q] = work[q + 1];
+      --remaining;
+      us[k] = mt.next_double();
     }
   }
   return kOk;
@@ -159,7 +180,9 @@ struct FinalizeArgs {
   SweepProblem* probs_next;
   uint8_t* dmode_next;
   longlong2* pool_next;
-  const LevelSample* next_tab;  // A_next entries
+  const LevelSample* next_tab;  // A_next entries, or null when the next level is uniform
+  LevelSample next_uni;         // uniform next level: n_codes, threads per sample and the per-sample
+                                // strides of partials (part_off) and rows (pool_off)
   int* err;
 };
 
@@ -333,7 +356,16 @@ __global__ void __launch_bounds__(kFinWarps * 32) gccb_finalize_kernel(FinalizeA
   }
   __syncwarp();
   nd = nb + nmul;
-  const LevelSample& ls = a.next_tab[j];
+  LevelSample ls;
+  if (a.next_tab) {
+    ls = a.next_tab[j];
+  } else {  // every sample of the next level has the same code count and layout
+    ls.n_codes = a.next_uni.n_codes;
+    ls.n_threads = a.next_uni.n_threads;
+    ls.thread_begin = (int64_t)j * a.next_uni.n_threads;
+    ls.part_off = (int64_t)j * a.next_uni.part_off;
+    ls.pool_off = (int64_t)j * a.next_uni.pool_off;
+  }
   longlong2* D = a.pool_next + ls.pool_off;
   for (int e = lane; e < nd * nf; e += 32) {
     const int d = e / nf, f = e - d * nf;
@@ -439,12 +471,32 @@ static int gccb_prepare(Context* cx, const double* matrix, int m, int n, int N, 
       for (int k = 0; k < L[s]; ++k) occ[add[(size_t)s * n + k]] = 0;
     }
   }
+  std::vector<char> uniform(Lmax + 2, 0);
+  std::vector<LevelSample> uni_lvl(Lmax + 2);
   for (int k = 2; k <= Lmax; ++k) {
     const int Ak = A[k];
     const std::vector<uint64_t>& codes = lvl_codes[k];
     const std::vector<int>& ndv = lvl_nd[k];
+    const int64_t resident = sweep_resident_threads(k - 1, SweepOp::kMinors, cx->sm_count);
+    bool same = true;
+    for (int jj = 1; jj < Ak && same; ++jj) same = (codes[jj] == codes[0] && ndv[jj] == ndv[0]);
+    if (same) {  // one small descriptor instead of a per-sample table
+      const double total = (double)codes[0] * Ak;
+      const double want = std::max<double>(Ak, std::min<double>((double)resident, total / kMinCodesPerThread));
+      const int64_t tps = std::max<int64_t>(1, std::min<int64_t>((int64_t)codes[0], (int64_t)(want / Ak)));
+      uniform[k] = 1;
+      uni_lvl[k].n_codes = (int64_t)codes[0];
+      uni_lvl[k].thread_begin = 0;
+      uni_lvl[k].n_threads = tps;
+      uni_lvl[k].part_off = tps * ndv[0];
+      uni_lvl[k].pool_off = (int64_t)ndv[0] * (k - 1);
+      lvl_threads[k] = tps * Ak;
+      lvl_parts[k] = tps * ndv[0] * Ak;
+      lvl_pool[k] = (int64_t)ndv[0] * (k - 1) * Ak;
+      continue;
+    }
     std::vector<int64_t> nthr;
-    partition_threads(codes, sweep_resident_threads(k - 1, SweepOp::kMinors, cx->sm_count), nthr);
+    partition_threads(codes, resident, nthr);
     auto& t = tab[k];
     t.resize(Ak);
     int64_t threads = 0, parts = 0, pool = 0;
@@ -566,7 +618,8 @@ static int gccb_prepare(Context* cx, const double* matrix, int m, int n, int N, 
     fa.probs_next = probs[nxt];
     fa.dmode_next = dmode[nxt];
     fa.pool_next = pool[nxt];
-    fa.next_tab = (k < Lmax) ? (const LevelSample*)(d + o_tab[k + 1]) : nullptr;
+    fa.next_tab = (k < Lmax && !uniform[k + 1]) ? (const LevelSample*)(d + o_tab[k + 1]) : nullptr;
+    fa.next_uni = (k < Lmax) ? uni_lvl[k + 1] : LevelSample{};
     fa.err = R.derr;
     gccb_finalize_kernel<<<(A[k] + kFinWarps - 1) / kFinWarps, kFinWarps * 32, 0, s>>>(fa);
     le = cudaGetLastError();
@@ -752,41 +805,52 @@ int boss_gccb_bench(const double* matrix, int32_t m, const int32_t* input_state,
   }
   Context* cx = context(&st);
   if (!cx) return st;
-  GccbRun R;
-  if ((st = gccb_prepare(cx, matrix, m, n, n_samples, L, add, u, true, R))) return st;
   if (flush_bytes > 0 && (st = ensure(cx->misc, (size_t)flush_bytes))) return st;
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
   cudaError_t e = cudaSuccess;
-  for (int it = 0; it < n_warmup + n_steps && e == cudaSuccess; ++it) {
-    if (flush_bytes > 0) e = cudaMemsetAsync(cx->misc.ptr, it & 0xff, (size_t)flush_bytes, cx->stream);
+  // (1) the plain graph, timed per step
+  GccbRun R;
+  st = gccb_prepare(cx, matrix, m, n, n_samples, L, add, u, false, R);
+  for (int it = 0; !st && it < n_warmup + n_steps; ++it) {
+    if (flush_bytes > 0 && (e = cudaMemsetAsync(cx->misc.ptr, it & 0xff, (size_t)flush_bytes, cx->stream)))
+      break;
     cudaEventRecord(e0, cx->stream);
     if ((st = gccb_launch(cx))) break;
     cudaEventRecord(e1, cx->stream);
-    e = cudaEventSynchronize(e1);
-    if (e != cudaSuccess) break;
+    if ((e = cudaEventSynchronize(e1)) != cudaSuccess) break;
     if (it >= n_warmup) {
       float ms = 0.f;
       cudaEventElapsedTime(&ms, e0, e1);
       step_ms[it - n_warmup] = ms;
-      double sw = 0.0;
-      for (int k = 0; k + 1 < (int)R.ev.size(); k += 2) {
-        float x = 0.f;
-        if (cudaEventElapsedTime(&x, R.ev[k], R.ev[k + 1]) != cudaSuccess) {
-          cudaGetLastError();
-          x = 0.f;
-        }
-        sw += x;
-      }
-      sweep_ms[it - n_warmup] = sw;
     }
+  }
+  if (!st && e == cudaSuccess) st = gccb_collect(cx, R, samples);
+  // (2) the same work with an event pair around every sweep launch: the sweep
+  // kernels' share of a step (event nodes cost time, so steps are not timed here)
+  GccbRun RT;
+  if (!st && e == cudaSuccess) st = gccb_prepare(cx, matrix, m, n, n_samples, L, add, u, true, RT);
+  for (int it = 0; !st && e == cudaSuccess && it < n_steps; ++it) {
+    if (flush_bytes > 0 && (e = cudaMemsetAsync(cx->misc.ptr, it & 0xff, (size_t)flush_bytes, cx->stream)))
+      break;
+    if ((st = gccb_launch(cx))) break;
+    if ((e = cudaStreamSynchronize(cx->stream)) != cudaSuccess) break;
+    double sw = 0.0;
+    for (int k = 0; k + 1 < (int)RT.ev.size(); k += 2) {
+      float x = 0.f;
+      if (cudaEventElapsedTime(&x, RT.ev[k], RT.ev[k + 1]) != cudaSuccess) {
+        cudaGetLastError();
+        x = 0.f;
+      }
+      sw += x;
+    }
+    sweep_ms[it] = sw;
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
+  destroy_events(RT);
   if (!st && e != cudaSuccess) st = fail_cuda(e, "bench");
-  if (!st) st = gccb_collect(cx, R, samples);
-  destroy_events(R);
   if (st) return st;
   info[0] = R.sweep_flops;
   info[1] = (double)R.h2d_bytes;
