@@ -116,3 +116,24 @@ def test_no_particles_gives_empty_samples():
 
     out = ss.GeneralizedCliffordsBSimulationStrategy(_calc(haar_unitary(4, 1))).simulate([0, 0, 0, 0], 5)
     assert out == [(0, 0, 0, 0)] * 5
+
+
+def test_lossy_network_sampling_in_expanded_120_modes(oracle):
+    """Non-uniform (network) losses at the large geometry: a 60-mode lossy matrix
+    U diag(sqrt(t)), t ~ U[0.3, 0.9], expanded to 120 modes; n = 12 photons keeps
+    the CPU oracle quick.  The GPU streams must equal the oracle's."""
+    from theboss_gb300 import _native
+    from theboss_gb300.utilities import haar_unitary, prepare_interferometer_matrix_in_expanded_space
+
+    m, n, N = 60, 12, 40
+    U = haar_unitary(m, 60)
+    t = np.random.default_rng(61).uniform(0.3, 0.9, m)
+    E = prepare_interferometer_matrix_in_expanded_space(U @ np.diag(np.sqrt(t)))
+    inp = [1] * n + [0] * (2 * m - n)
+    np.random.seed(62)
+    L, A, Uu = oracle.predraw_gccb(inp, N, None)
+    ref = oracle.gccb_run(E, L, A, Uu)
+    np.random.seed(62)
+    got = _native.gccb_sample(np.ascontiguousarray(E), np.array(inp, dtype=np.int32), None, N)
+    assert (got == ref).all()
+    assert (got[:, :m].sum(axis=1) <= n).all()

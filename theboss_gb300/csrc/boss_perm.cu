@@ -138,18 +138,19 @@ __global__ void grad_reduce_kernel(const SweepProblem* __restrict__ probs, const
   __shared__ double sr[256], si[256];
   const SweepProblem& P = probs[blockIdx.x];
   const int ne = (P.nd + P.fixed_digit) * P.nf;
+  const int64_t groups = P.n_threads >> 5;  // each group of 32 threads left one compact partial
   for (int e = threadIdx.x; e < ne; e += blockDim.x) {
     double ar = 0.0, ai = 0.0;
-    for (int64_t q = 0; q < P.n_threads; ++q) {
-      const double2 v = gpart[P.part_off + ((q >> 5) * ne + e) * 32 + (q & 31)];
+    for (int64_t g = 0; g < groups; ++g) {
+      const double2 v = gpart[P.part_off + g * (int64_t)ne * 32 + e];
       ar += v.x;
       ai += v.y;
     }
     grad_out[(size_t)P.out_idx * row_stride + e] = make_double2(ar * P.scale, ai * P.scale);
   }
   double ar = 0.0, ai = 0.0;
-  for (int64_t q = threadIdx.x; q < P.n_threads; q += blockDim.x) {
-    const double2 v = ppart[P.thread_begin + q];
+  for (int64_t q = threadIdx.x; q < groups; q += blockDim.x) {
+    const double2 v = ppart[(P.thread_begin >> 5) + q];
     ar += v.x;
     ai += v.y;
   }

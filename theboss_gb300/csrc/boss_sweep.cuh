@@ -222,6 +222,13 @@ __device__ __forceinline__ void accumulate_product(const long long (&sr)[NF], co
   ai = fma(pi, br, ai);
 }
 
+__device__ __forceinline__ double warp_sum(double v) {
+  // Fixed butterfly order: every lane ends with the same, run-to-run identical sum.
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
 // This thread's code range inside its sweep: lengths differ by at most one.
 __device__ __forceinline__ void thread_range(const SweepProblem& P, int64_t q, int64_t& a, int64_t& len) {
   const int64_t per = P.n_codes / P.n_threads, rem = P.n_codes % P.n_threads;

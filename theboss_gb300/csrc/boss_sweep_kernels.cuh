@@ -194,19 +194,19 @@ __global__ void __launch_bounds__(64) grad_sweep_kernel(const SweepProblem* __re
   const int bias = 1023 + 63 - P.fx;
   const int nb = P.nb;
   const uint64_t end = (uint64_t)(a + len);
-  const uint64_t block = (nb < 64) ? (1ull << nb) : 0ull;  // multi-valued digits change every 2^nb codes
-  // Segments: runs of codes over which every multi-valued digit is constant.
-  for (uint64_t seg = (uint64_t)a; seg < end;) {
-    const uint64_t seg_end = block ? ((seg / block + 1) * block < end ? (seg / block + 1) * block : end) : end;
+  // One walk over the thread's codes; a change of a multi-valued digit (every
+  // 2^nb codes) settles the segment and re-decodes inside the loop, so the lanes
+  // of a warp stay in step.
+  if (len > 0) {
     long long sr[NF], si[NF];
-    uint64_t g;
+    uint64_t g, seg = (uint64_t)a;
     uint32_t parity;
     double w;
     decode_code<NF>(P, D, base, seg, sr, si, g, parity, w);
 #pragma unroll
     for (int f = 0; f < NF; ++f) R[f * 64] = make_double2(0.0, 0.0);
     double permr = 0.0, permi = 0.0;
-    for (uint64_t t = seg;; ++t) {
+    for (uint64_t t = seg; t < end; ++t) {
       // ---- this code: leave-one-out products into R, the full product into perm ----
       const uint32_t neg = parity << 31;
       if (NF == 1) {
@@ -216,14 +216,12 @@ __global__ void __launch_bounds__(64) grad_sweep_kernel(const SweepProblem* __re
         permr += xor_sign(fx_to_double(sr[0], bias), neg);
         permi += xor_sign(fx_to_double(si[0], bias), neg);
       } else {
-        // the factors as doubles, once, into shared memory
 #pragma unroll
         for (int f = 0; f < NF; ++f) {
           if (f > 0 && (f & 7) == 0) load_fence();
           Bf[f * 64] = make_double2(fx_to_double(sr[f], bias), fx_to_double(si[f], bias));
         }
         load_fence();
-        // prefix products P_f = B_0 ... B_f (f <= NF - 2)
         double2 pv = Bf[0];
         Pp[0] = pv;
 #pragma unroll
@@ -268,70 +266,91 @@ __global__ void __launch_bounds__(64) grad_sweep_kernel(const SweepProblem* __re
         R[0] = v;
         load_fence();
       }
-      if (t + 1 >= seg_end) break;
-      // ---- step to code t + 1: a binary digit flips ----
-      const int i = __ffsll((long long)(t + 1)) - 1;
-      const uint32_t bit = (uint32_t)(g >> i) & 1u;
-      // its weight goes 1 - 2 bit -> 2 bit - 1: G_i += 2 (1 - 2 bit) w R
-      const double cc = (bit ? -2.0 : 2.0) * w;
-      double2* Gi = G + (size_t)i * NF * 32;
-      if ((touched >> i) & 1ull) {
+      const uint64_t tn = t + 1;
+      const bool last = (tn >= end);
+      const int i = __ffsll((long long)tn) - 1;
+      if (!last && i < nb) {
+        // ---- a binary digit flips: its weight goes 1 - 2 bit -> 2 bit - 1 ----
+        const uint32_t bit = (uint32_t)(g >> i) & 1u;
+        const double cc = (bit ? -2.0 : 2.0) * w;
+        double2* Gi = G + (size_t)i * NF * 32;
+        if ((touched >> i) & 1ull) {
 #pragma unroll
-        for (int f = 0; f < NF; ++f) {
-          if (f > 0 && (f & 7) == 0) load_fence();
-          const double2 r = R[f * 64];
-          double2 gv = Gi[f * 32];
-          gv.x = fma(cc, r.x, gv.x);
-          gv.y = fma(cc, r.y, gv.y);
-          Gi[f * 32] = gv;
+          for (int f = 0; f < NF; ++f) {
+            if (f > 0 && (f & 7) == 0) load_fence();
+            const double2 r = R[f * 64];
+            double2 gv = Gi[f * 32];
+            gv.x = fma(cc, r.x, gv.x);
+            gv.y = fma(cc, r.y, gv.y);
+            Gi[f * 32] = gv;
+          }
+        } else {
+          touched |= 1ull << i;
+#pragma unroll
+          for (int f = 0; f < NF; ++f) {
+            const double2 r = R[f * 64];
+            Gi[f * 32] = make_double2(cc * r.x, cc * r.y);
+          }
         }
+        g ^= 1ull << i;
+        flip_binary<NF>(D, i, bit, sr, si);
+        parity ^= 1u;
       } else {
-        touched |= 1ull << i;
-#pragma unroll
-        for (int f = 0; f < NF; ++f) {
-          const double2 r = R[f * 64];
-          Gi[f * 32] = make_double2(cc * r.x, cc * r.y);
+        // ---- end of a segment (or of the range): every digit receives its
+        // current weight times R ----
+        for (int bd = 0; bd < ndt; ++bd) {
+          double wb;
+          if (bd < nb) wb = ((g >> bd) & 1ull) ? -1.0 : 1.0;
+          else if (bd < nd) wb = (double)P.mult[bd] - 2.0 * (double)digit_value(P, seg, bd);
+          else wb = 1.0;
+          wb *= w;
+          double2* Gb = G + (size_t)bd * NF * 32;
+          if ((touched >> bd) & 1ull) {
+            for (int f = 0; f < NF; ++f) {
+              const double2 r = R[f * 64];
+              double2 gv = Gb[f * 32];
+              gv.x = fma(wb, r.x, gv.x);
+              gv.y = fma(wb, r.y, gv.y);
+              Gb[f * 32] = gv;
+            }
+          } else {
+            touched |= 1ull << bd;
+            for (int f = 0; f < NF; ++f) {
+              const double2 r = R[f * 64];
+              Gb[f * 32] = make_double2(wb * r.x, wb * r.y);
+            }
+          }
+        }
+        totr = fma(w, permr, totr);
+        toti = fma(w, permi, toti);
+        permr = 0.0;
+        permi = 0.0;
+        if (!last) {
+          for (int f = 0; f < NF; ++f) R[f * 64] = make_double2(0.0, 0.0);
+          seg = tn;
+          decode_code<NF>(P, D, base, tn, sr, si, g, parity, w);
         }
       }
-      g ^= 1ull << i;
-      flip_binary<NF>(D, i, bit, sr, si);
-      parity ^= 1u;
     }
-    // settle the segment: every digit receives its current weight times R
-    for (int bd = 0; bd < ndt; ++bd) {
-      double wb;
-      if (bd < nb) wb = ((g >> bd) & 1ull) ? -1.0 : 1.0;
-      else if (bd < nd) wb = (double)P.mult[bd] - 2.0 * (double)digit_value(P, seg, bd);
-      else wb = 1.0;
-      wb *= w;
-      double2* Gb = G + (size_t)bd * NF * 32;
-      if ((touched >> bd) & 1ull) {
-#pragma unroll
-        for (int f = 0; f < NF; ++f) {
-          if (f > 0 && (f & 7) == 0) load_fence();
-          const double2 r = R[f * 64];
-          double2 gv = Gb[f * 32];
-          gv.x = fma(wb, r.x, gv.x);
-          gv.y = fma(wb, r.y, gv.y);
-          Gb[f * 32] = gv;
-        }
-      } else {
-        touched |= 1ull << bd;
-#pragma unroll
-        for (int f = 0; f < NF; ++f) {
-          const double2 r = R[f * 64];
-          Gb[f * 32] = make_double2(wb * r.x, wb * r.y);
-        }
-      }
-    }
-    totr = fma(w, permr, totr);
-    toti = fma(w, permi, toti);
-    seg = seg_end;
   }
-  for (int bd = 0; bd < ndt; ++bd)
-    if (!((touched >> bd) & 1ull))
-      for (int f = 0; f < NF; ++f) G[((size_t)bd * NF + f) * 32] = make_double2(0.0, 0.0);
-  ppart[gt] = make_double2(totr, toti);
+  // Warp reduction of the 32 lanes' slices (the lane-interleaved layout makes
+  // every read coalesced); lane e % 32 stores entry e of the group's partial.
+  // Every lane of a warp belongs to the same sweep (thread counts are multiples of 32).
+  const int ne = ndt * NF;
+  const int lane = (int)(q & 31);
+  double2* W = gpart + P.part_off + (q >> 5) * (int64_t)ne * 32;  // the group's slices, reused for the result
+  for (int e = 0; e < ne; ++e) {
+    const int bd = e / NF;
+    double2 v = ((touched >> bd) & 1ull) ? G[(size_t)e * 32] : make_double2(0.0, 0.0);
+    v.x = warp_sum(v.x);
+    v.y = warp_sum(v.y);
+    __syncwarp();
+    if (lane == (e & 31)) W[e] = v;  // entry e of the group, compact at the start of its slices
+    __syncwarp();
+  }
+  totr = warp_sum(totr);
+  toti = warp_sum(toti);
+  if (lane == 0) ppart[gt >> 5] = make_double2(totr, toti);
 }
 
 constexpr size_t kMinorsSmem = (size_t)kMaxMinorDigits * 128 * sizeof(double2);
