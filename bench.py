@@ -56,7 +56,32 @@ def parse():
     ap.add_argument("--samples", type=int, default=10000)
     ap.add_argument("--seed", type=int, default=2026)
     ap.add_argument("--quick", action="store_true", help="skip the single-permanent and plain-driver sections")
+    ap.add_argument("--case", choices=["perm", "grad"],
+                    help="run one small kernel case instead of the bench (for profiler captures): "
+                         "Glynn permanents or permanents with all n^2 derivatives, n photons in 2n modes")
+    ap.add_argument("--n", type=int, default=24, help="photons of --case")
+    ap.add_argument("--patterns", type=int, default=16, help="output patterns of --case")
     return ap.parse_args()
+
+
+def run_case(args):
+    """One warm-up call and one timed call of a single kernel case; prints a
+    short JSON line (not a bench line)."""
+    from theboss_gb300 import _native
+    from theboss_gb300.utilities import haar_unitary
+
+    m = 2 * args.n
+    U = haar_unitary(m, args.seed + args.n)
+    T = c2_patterns(args.n, args.patterns, args.seed + args.n)
+    S = np.zeros_like(T)
+    S[:, :args.n] = 1
+    call = ((lambda: _native.perm_batch(U, S, T, _native.GLYNN)) if args.case == "perm"
+            else (lambda: _native.perm_grad_batch(U, S, T)))
+    call()
+    t = time.perf_counter()
+    call()
+    dt = time.perf_counter() - t
+    print(json.dumps({"case": args.case, "n": args.n, "m": m, "patterns": args.patterns, "ms": dt * 1e3}), flush=True)
 
 
 def workload(seed):
@@ -97,10 +122,18 @@ class Clocks:
             os.close(fd)
             self.f = open(self.path, "w")
             self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
-                                          "-lms", "200", "-i", str(self.idx)], stdout=self.f,
+                                          "-lms", "20", "-i", str(self.idx)], stdout=self.f,
                                          stderr=subprocess.DEVNULL)
         except Exception:
             self.proc = None
+            return
+        # nvidia-smi needs a moment to start: wait (at most 5 s) for its first sample
+        # so that the region it watches is covered from the start
+        t0 = time.time()
+        while time.time() - t0 < 5.0 and self.proc.poll() is None:
+            if os.path.getsize(self.path) > 0:
+                break
+            time.sleep(0.02)
 
     def stop(self):
         if self.proc is None:
@@ -262,11 +295,10 @@ def run_ours(args, rank, world):
     clocks = Clocks(int(os.environ.get("LOCAL_RANK", "0")))
     np.random.seed(args.seed + rank)
     _barrier(world)
-    clocks.start()
+    clocks.start()  # sampled over the device-timed steps and the e2e steps below
     t_wall = time.perf_counter()
     b = _native.gccb_bench(U, inp, w, args.samples, args.warmup, args.steps)
     t_wall = time.perf_counter() - t_wall
-    clk = clocks.stop()
     _barrier(world)
     total_ms = float(np.sum(b["step_ms"]))
     total_ms = _max_over_ranks(total_ms, world)
@@ -287,6 +319,7 @@ def run_ours(args, rank, world):
         t = time.perf_counter()
         out = _native.gccb_sample(U, inp, w, args.samples)
         e2e_t.append(time.perf_counter() - t)
+    clk = clocks.stop()
     if not np.array_equal(out, b["samples"]):
         raise SystemExit("e2e samples differ from the device-timed run")
     e2e = {"value": args.samples * args.steps / sum(e2e_t), "unit": "samples/s",
@@ -387,7 +420,10 @@ def main():
         from theboss_gb300 import _native
 
         _native.select_device(int(os.environ.get("LOCAL_RANK", "0")))
-        run_ours(args, rank, world)
+        if args.case:
+            run_case(args)
+        else:
+            run_ours(args, rank, world)
     if world > 1:
         import torch.distributed as dist
 

@@ -181,7 +181,6 @@ __global__ void __launch_bounds__(64) grad_sweep_kernel(const SweepProblem* __re
   const int nd = P.nd, ndt = P.nd + P.fixed_digit;
   double2* R = grad_smem + threadIdx.x;             // running sign * L_f, R[f * 64]
   double2* Pp = grad_smem + NF * 64 + threadIdx.x;  // prefix products, Pp[f * 64]
-  double2* Bf = grad_smem + 2 * NF * 64 + threadIdx.x;  // this code's factors, Bf[f * 64]
   // Per-thread gradient slices are interleaved by lane within each group of 32
   // threads ([group][row][factor][lane]) so a warp's row updates coalesce.
   double2* G = gpart + P.part_off + (q >> 5) * (int64_t)(ndt * NF) * 32 + (q & 31);
@@ -216,24 +215,20 @@ __global__ void __launch_bounds__(64) grad_sweep_kernel(const SweepProblem* __re
         permr += xor_sign(fx_to_double(sr[0], bias), neg);
         permi += xor_sign(fx_to_double(si[0], bias), neg);
       } else {
-#pragma unroll
-        for (int f = 0; f < NF; ++f) {
-          if (f > 0 && (f & 7) == 0) load_fence();
-          Bf[f * 64] = make_double2(fx_to_double(sr[f], bias), fx_to_double(si[f], bias));
-        }
-        load_fence();
-        double2 pv = Bf[0];
+        // The factors are converted from the fixed-point sums twice (prefix and
+        // suffix pass): integer work, cheaper than staging them in shared memory.
+        double2 pv = make_double2(fx_to_double(sr[0], bias), fx_to_double(si[0], bias));
         Pp[0] = pv;
 #pragma unroll
         for (int f = 1; f < NF - 1; ++f) {
-          const double2 bv = Bf[f * 64];
+          const double2 bv = make_double2(fx_to_double(sr[f], bias), fx_to_double(si[f], bias));
           const double t_re = fma(pv.x, bv.x, -(pv.y * bv.y));
           const double t_im = fma(pv.x, bv.y, pv.y * bv.x);
           pv = make_double2(t_re, t_im);
           Pp[f * 64] = pv;
         }
         load_fence();
-        double2 qv = Bf[(NF - 1) * 64];
+        double2 qv = make_double2(fx_to_double(sr[NF - 1], bias), fx_to_double(si[NF - 1], bias));
         const double pnr = xor_sign(pv.x, neg), pni = xor_sign(pv.y, neg);
         permr = fma(pnr, qv.x, permr);
         permr = fma(-pni, qv.y, permr);
@@ -255,7 +250,7 @@ __global__ void __launch_bounds__(64) grad_sweep_kernel(const SweepProblem* __re
           v.y = fma(lr, qv.y, v.y);
           v.y = fma(li, qv.x, v.y);
           R[f * 64] = v;
-          const double2 bv = Bf[f * 64];
+          const double2 bv = make_double2(fx_to_double(sr[f], bias), fx_to_double(si[f], bias));
           const double nqr = fma(qv.x, bv.x, -(qv.y * bv.y));
           const double nqi = fma(qv.x, bv.y, qv.y * bv.x);
           qv = make_double2(nqr, nqi);
@@ -354,12 +349,12 @@ __global__ void __launch_bounds__(64) grad_sweep_kernel(const SweepProblem* __re
 }
 
 constexpr size_t kMinorsSmem = (size_t)kMaxMinorDigits * 128 * sizeof(double2);
-constexpr size_t kGradSmem = (size_t)(3 * kMaxFactors) * 64 * sizeof(double2);
+constexpr size_t kGradSmem = (size_t)(2 * kMaxFactors) * 64 * sizeof(double2);
 
 template <int NF>
 cudaError_t sweep_launch_t(SweepOp op, const SweepLaunch& L, cudaStream_t st) {
   if (op == SweepOp::kGrad) {
-    grad_sweep_kernel<NF><<<L.grid, 64, (size_t)(3 * NF) * 64 * sizeof(double2), st>>>(
+    grad_sweep_kernel<NF><<<L.grid, 64, (size_t)(2 * NF) * 64 * sizeof(double2), st>>>(
         L.probs, L.n_probs, L.pool, L.total_threads, L.partials, L.partials2);
     return cudaGetLastError();
   }
@@ -375,7 +370,7 @@ cudaError_t sweep_launch_t(SweepOp op, const SweepLaunch& L, cudaStream_t st) {
 template <int NF>
 cudaError_t grad_occupancy_t(int* blocks_per_sm) {
   return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, grad_sweep_kernel<NF>, 64,
-                                                       (size_t)(3 * NF) * 64 * sizeof(double2));
+                                                       (size_t)(2 * NF) * 64 * sizeof(double2));
 }
 
 template <int NF>
