@@ -90,34 +90,73 @@ static inline uint32_t mask_for(uint32_t n) {
   return m;
 }
 
+// The random numbers of a batch of samples.  theboss keeps its input particles in
+// a list ordered by mode and pops a uniformly chosen one per step
+// (generalized_cliffords_b_simulation_strategy.py:97-105); `idx` holds the
+// randint results, i.e. positions in the list of the particles not yet popped.
+struct Draws {
+  int n = 0;                       // input particles
+  bool binned = false;             // some input mode holds more than one particle
+  std::vector<uint8_t> particles;  // particle -> mode (ascending)
+  std::vector<int32_t> L;          // [sample] particles kept
+  std::vector<uint8_t> idx;        // [sample][n] randint results
+  std::vector<double> u;           // [sample][n] uniforms of numpy.random.choice
+  std::vector<uint8_t> modes;      // [sample][n] popped modes (host copy, filled on demand)
+};
+
+// The popped modes from the randint results: remove the idx-th remaining particle.
+static void modes_from_draws(Draws& D) {
+  const int n = D.n, N = (int)D.L.size();
+  D.modes.assign((size_t)N * std::max(n, 1), 0);
+  uint8_t work[257];
+  for (int s = 0; s < N; ++s) {
+    for (int k = 0; k < n; ++k) work[k] = D.particles[k];
+    const uint8_t* is = &D.idx[(size_t)s * n];
+    uint8_t* ms = &D.modes[(size_t)s * n];
+    for (int k = 0; k < D.L[s]; ++k) {
+      const int i = is[k];
+      ms[k] = work[i];
+      for (int q = 0; q < n - 1; ++q) work[q] = (q >= i) ? work[q + 1] : work[q];  // fixed trip count
+    }
+  }
+}
+
 // The whole random stream of `n_samples` GC&C-B samples, in theboss's draw order.
 static int predraw(const int32_t* input_state, int m, const double* weights, int n_weights, MT19937& mt,
-                   int n_samples, std::vector<int32_t>& L, std::vector<uint8_t>& add, std::vector<double>& u,
-                   int& n_particles) {
-  std::vector<int> particles;
+                   int n_samples, Draws& D) {
+  if (m > 256) {
+    set_error("the sampler supports at most 256 modes");
+    return kErrLimit;
+  }
+  int n = 0;
+  D.binned = false;
   for (int i = 0; i < m; ++i) {
     if (input_state[i] < 0 || input_state[i] > 255) {
       set_error("input occupations must be in [0, 255]");
       return kErrArg;
     }
-    for (int k = 0; k < input_state[i]; ++k) particles.push_back(i);
-  }
-  const int n = (int)particles.size();
-  n_particles = n;
-  if (weights && n_weights != n + 1) {
-    set_error("particle-number weights must have n + 1 entries");
-    return kErrArg;
+    if (input_state[i] > 1) D.binned = true;
+    n += input_state[i];
   }
   if (n > 255) {
     set_error("at most 255 input particles");
     return kErrLimit;
   }
+  D.n = n;
+  D.particles.clear();
+  for (int i = 0; i < m; ++i)
+    for (int k = 0; k < input_state[i]; ++k) D.particles.push_back((uint8_t)i);
+  if (weights && n_weights != n + 1) {
+    set_error("particle-number weights must have n + 1 entries");
+    return kErrArg;
+  }
+  std::vector<int32_t>& L = D.L;
   L.assign(n_samples, 0);
-  add.assign((size_t)n_samples * std::max(n, 1), 0);
-  u.assign((size_t)n_samples * std::max(n, 1), 0.0);
+  D.idx.assign((size_t)n_samples * std::max(n, 1), 0);
+  D.u.assign((size_t)n_samples * std::max(n, 1), 0.0);
+  D.modes.clear();
   uint32_t masks[257];
   for (int r = 1; r <= n; ++r) masks[r] = mask_for((uint32_t)r);
-  uint8_t work[256];
   for (int s = 0; s < n_samples; ++s) {
     int l = n;
     if (weights) {  // generalized_cliffords_b_uniform_losses_simulation_strategy.py:67-85
@@ -135,14 +174,11 @@ static int predraw(const int32_t* input_state, int m, const double* weights, int
       }
     }
     L[s] = l;
-    for (int k = 0; k < n; ++k) work[k] = (uint8_t)particles[k];
     int remaining = n;
-    uint8_t* as = &add[(size_t)s * n];
-    double* us = &u[(size_t)s * n];
+    uint8_t* is = &D.idx[(size_t)s * n];
+    double* us = &D.u[(size_t)s * n];
     for (int k = 0; k < l; ++k) {  // generalized_cliffords_b_simulation_strategy.py:97-110
-      const uint32_t idx = mt.bounded((uint32_t)remaining, masks[remaining]);
-      as[k] = work[idx];
-      for (int q = (int)idx; q + 1 < remaining; ++q) work[q] = work[q + 1];
+      is[k] = (uint8_t)mt.bounded((uint32_t)remaining, masks[remaining]);
       --remaining;
       us[k] = mt.next_double();
     }
@@ -166,13 +202,15 @@ struct FinalizeArgs {
   int A;       // active samples at this level
   int A_next;  // active samples at level k + 1
   int m;
-  int n;       // row stride of add / uni
+  int n;       // row stride of idx / uni
   int fx;      // fixed-point fraction bits of the sweep rows
   const double2* U;       // m x m
   const longlong2* Ufx;   // m x m, U * 2^fx rounded
   uint8_t* S;             // [sample][m] current input occupations
   uint8_t* T;             // [sample][m] output occupations
-  const uint8_t* add;     // [sample][n] popped input modes
+  const uint8_t* idx;     // [sample][n] randint results (position among the particles left)
+  const uint8_t* pmode;   // [n] particle -> input mode
+  uint32_t* rem;          // [sample][8] particles not yet popped, as bits
   const double* uni;      // [sample][n] uniforms
   const SweepProblem* probs_cur;
   const uint8_t* dmode_cur;  // [sample][32]
@@ -183,10 +221,37 @@ struct FinalizeArgs {
   const LevelSample* next_tab;  // A_next entries, or null when the next level is uniform
   LevelSample next_uni;         // uniform next level: n_codes, threads per sample and the per-sample
                                 // strides of partials (part_off) and rows (pool_off)
+  int next_group;               // uniform next level: threads per summed group of minors
   int* err;
 };
 
 constexpr int kFinWarps = 4;
+
+// Removes and returns the r-th (0-based) particle still in the 256-bit set `rem`
+// (r is below the number of set bits: the host drew it with randint(0, remaining)).
+__device__ __forceinline__ int pop_particle(uint32_t* rem, int r) {
+  int q = 0;
+  for (; q < 7; ++q) {
+    const int c = __popc(rem[q]);
+    if (r < c) break;
+    r -= c;
+  }
+  uint32_t x = rem[q];
+  int pos = 0;
+  for (int s = 16; s > 0; s >>= 1) {  // binary search for the bit
+    const uint32_t lo = x & ((1u << s) - 1u);
+    const int c = __popc(lo);
+    if (r >= c) {
+      r -= c;
+      x >>= s;
+      pos += s;
+    } else {
+      x = lo;
+    }
+  }
+  rem[q] &= ~(1u << pos);
+  return q * 32 + pos;
+}
 
 __global__ void __launch_bounds__(kFinWarps * 32) gccb_finalize_kernel(FinalizeArgs a) {
   __shared__ double2 sub_s[kFinWarps][32];
@@ -204,8 +269,14 @@ __global__ void __launch_bounds__(kFinWarps * 32) gccb_finalize_kernel(FinalizeA
   if (a.k == 1) {
     // one particle: the minors are the input occupations themselves
     // (bs_submatrices_permanent_calculator_base.py:157-158)
-    const int mode = a.add[(size_t)j * a.n];
+    int mode = 0;
     if (lane == 0) {
+      uint32_t* rem = a.rem + (size_t)j * 8;
+      for (int q = 0; q < 8; ++q) {
+        const int lo = q * 32;
+        rem[q] = (a.n >= lo + 32) ? 0xffffffffu : (a.n > lo ? ((1u << (a.n - lo)) - 1u) : 0u);
+      }
+      mode = a.pmode[pop_particle(rem, a.idx[(size_t)j * a.n])];
       S[mode] = 1;
       sub_s[w][0] = make_double2(1.0, 0.0);
       dm_s[w][0] = (uint8_t)mode;
@@ -215,14 +286,31 @@ __global__ void __launch_bounds__(kFinWarps * 32) gccb_finalize_kernel(FinalizeA
   } else {
     const SweepProblem& P = a.probs_cur[j];
     nd = P.nd;
-    if (lane < nd) {
-      double sx = 0.0, sy = 0.0;
-      for (int64_t q = 0; q < P.n_threads; ++q) {
-        const double2 v = a.partials[P.part_off + q * nd + lane];
-        sx += v.x;
-        sy += v.y;
+    const int64_t parts = P.n_threads / P.group;
+    if (parts <= 64) {  // lane d sums digit d's partials
+      if (lane < nd) {
+        double sx = 0.0, sy = 0.0;
+        for (int64_t q = 0; q < parts; ++q) {
+          const double2 v = a.partials[P.part_off + q * nd + lane];
+          sx += v.x;
+          sy += v.y;
+        }
+        sub_s[w][lane] = make_double2(sx * P.scale, sy * P.scale);
       }
-      sub_s[w][lane] = make_double2(sx * P.scale, sy * P.scale);
+    } else {  // many partials: the lanes stripe over them, then a fixed-order warp sum
+      for (int d = 0; d < nd; ++d) {
+        double sx = 0.0, sy = 0.0;
+        for (int64_t q = lane; q < parts; q += 32) {
+          const double2 v = a.partials[P.part_off + q * nd + d];
+          sx += v.x;
+          sy += v.y;
+        }
+        sx = warp_sum(sx);
+        sy = warp_sum(sy);
+        if (lane == d) sub_s[w][d] = make_double2(sx * P.scale, sy * P.scale);
+      }
+    }
+    if (lane < nd) {
       dm_s[w][lane] = a.dmode_cur[(size_t)j * 32 + lane];
       mult_s[w][lane] = P.mult[lane];
     }
@@ -236,7 +324,10 @@ __global__ void __launch_bounds__(kFinWarps * 32) gccb_finalize_kernel(FinalizeA
     sub_s[w][lane] = make_double2(mu * sv.x, mu * sv.y);
   }
   __syncwarp();
-  for (int o = lane; o < m; o += 32) {
+  // FP64 instructions cost the same whatever the number of active lanes, so the
+  // outputs that do not fill a warp split their digits over several lanes.
+  const int full = m & ~31;
+  for (int o = lane; o < full; o += 32) {
     double re = 0.0, im = 0.0;
     const double2* Urow = a.U + (size_t)o * m;
     for (int d = 0; d < nd; ++d) {
@@ -246,6 +337,27 @@ __global__ void __launch_bounds__(kFinWarps * 32) gccb_finalize_kernel(FinalizeA
       im = fma(c.x, u.y, fma(c.y, u.x, im));
     }
     pmf_s[w][o] = fma(re, re, im * im);
+  }
+  if (m > full) {
+    const int r = m - full;
+    int s = 1;  // lanes per remaining output (a power of two, r * s <= 32)
+    while (r * (s << 1) <= 32) s <<= 1;
+    const int oi = lane / s, c0 = lane & (s - 1);
+    double re = 0.0, im = 0.0;
+    if (oi < r) {
+      const double2* Urow = a.U + (size_t)(full + oi) * m;
+      for (int d = c0; d < nd; d += s) {
+        const double2 c = sub_s[w][d];
+        const double2 u = Urow[dm_s[w][d]];
+        re = fma(c.x, u.x, fma(-c.y, u.y, re));
+        im = fma(c.x, u.y, fma(c.y, u.x, im));
+      }
+    }
+    for (int off = s >> 1; off > 0; off >>= 1) {
+      re += __shfl_xor_sync(0xffffffffu, re, off);
+      im += __shfl_xor_sync(0xffffffffu, im, off);
+    }
+    if (oi < r && c0 == 0) pmf_s[w][full + oi] = fma(re, re, im * im);
   }
   __syncwarp();
   // theboss normalises with Python's sequential sum, and numpy.random.choice then
@@ -267,20 +379,28 @@ __global__ void __launch_bounds__(kFinWarps * 32) gccb_finalize_kernel(FinalizeA
     if (lane >= off) incl += y;
   }
   const double total_fast = __shfl_sync(0xffffffffu, incl, 31);
+  double excl = __shfl_up_sync(0xffffffffu, incl, 1);
+  if (lane == 0) excl = 0.0;
   int idx = 0;
   if (!(total_fast > 0.0) || !isfinite(total_fast)) {
     if (lane == 0) atomicOr(a.err, 1);
   } else {
     const double inv = 1.0 / total_fast;
-    double c = (incl - local) * inv;
+    // Every cdf entry and the uniform are non-negative doubles, whose order is that of
+    // their bit patterns as integers: the comparisons run on the integer pipe.  An entry
+    // is "near" when it lies in [u (1 - 1e-12), u (1 + 1e-12)].
+    const long long ub = __double_as_longlong(uu);
+    const long long lo = __double_as_longlong(fma(-1e-12, uu, uu));
+    const long long hi = __double_as_longlong(fma(1e-12, uu, uu));
+    double c = excl * inv;
     int cnt = 0;
     bool near = false;
     for (int q = 0; q < K; ++q) {
       if (o0 + q >= m) break;
-      c += pmf_s[w][o0 + q] * inv;  // ~ cdf / cdf[-1] (the last entry is ~1)
-      const double d = c - uu;
-      near |= (o0 + q < m - 1) && (fabs(d) <= 1e-12 * fmax(c, uu));
-      cnt += (d <= 0.0) ? 1 : 0;
+      c = fma(pmf_s[w][o0 + q], inv, c);  // ~ cdf / cdf[-1] (the last entry is ~1)
+      const long long cb = __double_as_longlong(c);
+      near |= (o0 + q < m - 1) && cb >= lo && cb <= hi;
+      cnt += (cb <= ub) ? 1 : 0;
     }
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) cnt += __shfl_xor_sync(0xffffffffu, cnt, off);
@@ -314,7 +434,7 @@ __global__ void __launch_bounds__(kFinWarps * 32) gccb_finalize_kernel(FinalizeA
 
   // ---- the all-minors sweep of level k + 1 ----
   if (lane == 0) {
-    const int mode = a.add[(size_t)j * a.n + a.k];
+    const int mode = a.pmode[pop_particle(a.rem + (size_t)j * 8, a.idx[(size_t)j * a.n + a.k])];
     S[mode] = (uint8_t)(S[mode] + 1);
   }
   __syncwarp();
@@ -392,7 +512,7 @@ __global__ void __launch_bounds__(kFinWarps * 32) gccb_finalize_kernel(FinalizeA
     P.part_off = ls.part_off;
     P.scale = 1.0;
     P.fixed_digit = 0;
-    P.reserved = 0;
+    P.group = a.next_tab ? 1 : a.next_group;
   }
 }
 
@@ -416,8 +536,13 @@ static void destroy_events(GccbRun& R) {
   R.ev.clear();
 }
 
-static int gccb_prepare(Context* cx, const double* matrix, int m, int n, int N, const std::vector<int32_t>& L,
-                        const std::vector<uint8_t>& add, const std::vector<double>& uni, bool timing, GccbRun& R) {
+static int gccb_prepare(Context* cx, const double* matrix, int m, Draws& D, bool timing, GccbRun& R) {
+  const int N = (int)D.L.size();
+  const int n = std::max(D.n, 1);
+  const std::vector<int32_t>& L = D.L;
+  // Single-occupied inputs: every sample at level k sweeps 2^k codes over k digits,
+  // whichever particles it popped.  Binned inputs need the popped modes to plan.
+  if (D.binned && D.modes.empty()) modes_from_draws(D);
   R.N = N;
   R.m = m;
   R.n = n;
@@ -456,10 +581,15 @@ static int gccb_prepare(Context* cx, const double* matrix, int m, int n, int N, 
       uint64_t c = 1;
       int nd = 0;
       for (int k = 1; k <= L[s]; ++k) {
-        const int md = add[(size_t)s * n + (k - 1)];
-        c = c / ((uint64_t)occ[md] + 1) * ((uint64_t)occ[md] + 2);
-        if (occ[md] == 0) ++nd;
-        occ[md]++;
+        if (D.binned) {
+          const int md = D.modes[(size_t)s * n + (k - 1)];
+          c = c / ((uint64_t)occ[md] + 1) * ((uint64_t)occ[md] + 2);
+          if (occ[md] == 0) ++nd;
+          occ[md]++;
+        } else {
+          c *= 2;
+          ++nd;
+        }
         if (k >= 2) {
           lvl_codes[k][jj] = c;
           lvl_nd[k][jj] = nd;
@@ -468,11 +598,13 @@ static int gccb_prepare(Context* cx, const double* matrix, int m, int n, int N, 
           R.sweep_flops += (double)c * (9.0 * k - 12.0);
         }
       }
-      for (int k = 0; k < L[s]; ++k) occ[add[(size_t)s * n + k]] = 0;
+      if (D.binned)
+        for (int k = 0; k < L[s]; ++k) occ[D.modes[(size_t)s * n + k]] = 0;
     }
   }
   std::vector<char> uniform(Lmax + 2, 0);
   std::vector<LevelSample> uni_lvl(Lmax + 2);
+  std::vector<int> grp(Lmax + 2, 1);
   for (int k = 2; k <= Lmax; ++k) {
     const int Ak = A[k];
     const std::vector<uint64_t>& codes = lvl_codes[k];
@@ -483,7 +615,13 @@ static int gccb_prepare(Context* cx, const double* matrix, int m, int n, int N, 
     if (same) {  // one small descriptor instead of a per-sample table
       const double total = (double)codes[0] * Ak;
       const double want = std::max<double>(Ak, std::min<double>((double)resident, total / kMinCodesPerThread));
-      const int64_t tps = std::max<int64_t>(1, std::min<int64_t>((int64_t)codes[0], (int64_t)(want / Ak)));
+      int64_t tps = std::max<int64_t>(1, std::min<int64_t>((int64_t)codes[0], (int64_t)(want / Ak)));
+      // Each aligned group of G threads of a sample sums its minors inside the sweep:
+      // the largest G (up to a warp) that costs at most 2% of the sample's threads.
+      int G = 32;
+      while (G > 1 && !(tps >= G && (double)(tps / G * G) >= 0.98 * (double)tps)) G >>= 1;
+      tps = tps / G * G;
+      grp[k] = G;
       uniform[k] = 1;
       uni_lvl[k].n_codes = (int64_t)codes[0];
       uni_lvl[k].thread_begin = 0;
@@ -521,13 +659,14 @@ static int gccb_prepare(Context* cx, const double* matrix, int m, int n, int N, 
     max_parts = std::max(max_parts, lvl_parts[k]);
     max_pool = std::max(max_pool, lvl_pool[k]);
   }
-  // Arena (one H2D copy): err | level tables | add | uniforms | U | U fixed-point
+  // Arena (one H2D copy): err | level tables | randint results | particle modes | uniforms | U | U fixed-point
   auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
   size_t off = 0;
   const size_t o_err = off; off = al(off + sizeof(int));
   std::vector<size_t> o_tab(Lmax + 2, 0);
   for (int k = 2; k <= Lmax; ++k) { o_tab[k] = off; off = al(off + sizeof(LevelSample) * tab[k].size()); }
-  const size_t o_add = off; off = al(off + (size_t)N * n);
+  const size_t o_idx = off; off = al(off + (size_t)N * n);
+  const size_t o_pm = off; off = al(off + (size_t)n);
   const size_t o_uni = off; off = al(off + sizeof(double) * (size_t)N * n);
   const size_t o_U = off; off = al(off + sizeof(double2) * (size_t)m * m);
   const size_t o_Ufx = off; off = al(off + sizeof(longlong2) * (size_t)m * m);
@@ -541,16 +680,19 @@ static int gccb_prepare(Context* cx, const double* matrix, int m, int n, int N, 
   if ((st = ensure(cx->gccb[3], (size_t)A[1] * 32 * 2))) return st;                          // digit modes x2
   if ((st = ensure(cx->gccb[4], sizeof(longlong2) * (size_t)max_pool * 2 + 512))) return st;  // rows x2
   if ((st = ensure(cx->gccb[5], sizeof(double2) * (size_t)max_parts))) return st;            // partials
+  if ((st = ensure(cx->gccb[6], sizeof(uint32_t) * 8 * (size_t)N))) return st;                // particles left
   if ((st = ensure_pinned(cx, std::max(arena, al((size_t)N * m) + 256)))) return st;
   char* h = (char*)cx->pinned;
-  memset(h, 0, o_add);
+  memset(h, 0, o_idx);
   for (int k = 2; k <= Lmax; ++k) memcpy(h + o_tab[k], tab[k].data(), sizeof(LevelSample) * tab[k].size());
-  uint8_t* hadd = (uint8_t*)(h + o_add);
+  uint8_t* hidx = (uint8_t*)(h + o_idx);
   double* huni = (double*)(h + o_uni);
   for (int jj = 0; jj < N; ++jj) {
-    memcpy(hadd + (size_t)jj * n, &add[(size_t)order[jj] * n], n);
-    memcpy(huni + (size_t)jj * n, &uni[(size_t)order[jj] * n], sizeof(double) * n);
+    memcpy(hidx + (size_t)jj * n, &D.idx[(size_t)order[jj] * n], n);
+    memcpy(huni + (size_t)jj * n, &D.u[(size_t)order[jj] * n], sizeof(double) * n);
   }
+  memset(h + o_pm, 0, n);
+  memcpy(h + o_pm, D.particles.data(), D.particles.size());
   memcpy(h + o_U, matrix, sizeof(double2) * (size_t)m * m);
   longlong2* hfx = (longlong2*)(h + o_Ufx);
   for (size_t i = 0; i < (size_t)m * m; ++i) {
@@ -610,7 +752,9 @@ static int gccb_prepare(Context* cx, const double* matrix, int m, int n, int N, 
     fa.Ufx = (const longlong2*)(d + o_Ufx);
     fa.S = dS;
     fa.T = R.dT;
-    fa.add = (const uint8_t*)(d + o_add);
+    fa.idx = (const uint8_t*)(d + o_idx);
+    fa.pmode = (const uint8_t*)(d + o_pm);
+    fa.rem = (uint32_t*)cx->gccb[6].ptr;
     fa.uni = (const double*)(d + o_uni);
     fa.probs_cur = probs[cur];
     fa.dmode_cur = dmode[cur];
@@ -620,6 +764,7 @@ static int gccb_prepare(Context* cx, const double* matrix, int m, int n, int N, 
     fa.pool_next = pool[nxt];
     fa.next_tab = (k < Lmax && !uniform[k + 1]) ? (const LevelSample*)(d + o_tab[k + 1]) : nullptr;
     fa.next_uni = (k < Lmax) ? uni_lvl[k + 1] : LevelSample{};
+    fa.next_group = (k < Lmax) ? grp[k + 1] : 1;
     fa.err = R.derr;
     gccb_finalize_kernel<<<(A[k] + kFinWarps - 1) / kFinWarps, kFinWarps * 32, 0, s>>>(fa);
     le = cudaGetLastError();
@@ -682,11 +827,10 @@ static int gccb_collect(Context* cx, GccbRun& R, int32_t* samples_out) {
   return kOk;
 }
 
-static int run_gccb(Context* cx, const double* matrix, int m, int n, int N, const std::vector<int32_t>& L,
-                    const std::vector<uint8_t>& add, const std::vector<double>& uni, int32_t* samples_out) {
-  if (N == 0) return kOk;
+static int run_gccb(Context* cx, const double* matrix, int m, Draws& D, int32_t* samples_out) {
+  if (D.L.empty()) return kOk;
   GccbRun R;
-  int st = gccb_prepare(cx, matrix, m, n, N, L, add, uni, false, R);
+  int st = gccb_prepare(cx, matrix, m, D, false, R);
   if (st) return st;
   if ((st = gccb_launch(cx))) return st;
   return gccb_collect(cx, R, samples_out);
@@ -718,17 +862,17 @@ int boss_gccb_predraw(const int32_t* input_state, int32_t m, const double* parti
   MT19937 mt;
   int st = load_mt(mt, mt_key, mt_pos);
   if (st) return st;
-  std::vector<int32_t> L;
-  std::vector<uint8_t> add;
-  std::vector<double> u;
-  int n = 0;
-  st = predraw(input_state, m, particle_weights, particle_weights ? n_weights : 0, mt, n_samples, L, add, u, n);
+  Draws D;
+  st = predraw(input_state, m, particle_weights, particle_weights ? n_weights : 0, mt, n_samples, D);
   if (st) return st;
+  const std::vector<int32_t>& L = D.L;
+  const int n = D.n;
+  if (popped_modes) modes_from_draws(D);
   for (int s = 0; s < n_samples; ++s) {
     particles_kept[s] = L[s];
     for (int k = 0; k < n; ++k) {
-      if (popped_modes) popped_modes[(size_t)s * n + k] = (k < L[s]) ? add[(size_t)s * n + k] : -1;
-      if (uniforms) uniforms[(size_t)s * n + k] = (k < L[s]) ? u[(size_t)s * n + k] : 0.0;
+      if (popped_modes) popped_modes[(size_t)s * n + k] = (k < L[s]) ? D.modes[(size_t)s * n + k] : -1;
+      if (uniforms) uniforms[(size_t)s * n + k] = (k < L[s]) ? D.u[(size_t)s * n + k] : 0.0;
     }
   }
   memcpy(mt_key, mt.key, sizeof(mt.key));
@@ -750,12 +894,11 @@ int boss_gccb_sample(const double* matrix, int32_t m, const int32_t* input_state
   MT19937 mt;
   int st = load_mt(mt, mt_key, mt_pos);
   if (st) return st;
-  std::vector<int32_t> L;
-  std::vector<uint8_t> add;
-  std::vector<double> u;
-  int n = 0;
-  st = predraw(input_state, m, particle_weights, particle_weights ? n_weights : 0, mt, n_samples, L, add, u, n);
+  Draws D;
+  st = predraw(input_state, m, particle_weights, particle_weights ? n_weights : 0, mt, n_samples, D);
   if (st) return st;
+  const std::vector<int32_t>& L = D.L;
+  const int n = D.n;
   if (n > kMaxMinorDigits) {
     set_error("the batched sampler supports at most 32 input particles");
     return kErrLimit;
@@ -765,7 +908,7 @@ int boss_gccb_sample(const double* matrix, int32_t m, const int32_t* input_state
   if (any) {
     Context* cx = context(&st);
     if (!cx) return st;
-    st = run_gccb(cx, matrix, m, std::max(n, 1), n_samples, L, add, u, samples);
+    st = run_gccb(cx, matrix, m, D, samples);
     if (st) return st;
   }
   memcpy(mt_key, mt.key, sizeof(mt.key));
@@ -789,12 +932,11 @@ int boss_gccb_bench(const double* matrix, int32_t m, const int32_t* input_state,
   MT19937 mt;
   int st = load_mt(mt, mt_key, mt_pos);
   if (st) return st;
-  std::vector<int32_t> L;
-  std::vector<uint8_t> add;
-  std::vector<double> u;
-  int n = 0;
-  st = predraw(input_state, m, particle_weights, particle_weights ? n_weights : 0, mt, n_samples, L, add, u, n);
+  Draws D;
+  st = predraw(input_state, m, particle_weights, particle_weights ? n_weights : 0, mt, n_samples, D);
   if (st) return st;
+  const std::vector<int32_t>& L = D.L;
+  const int n = D.n;
   if (n > kMaxMinorDigits || n < 1) {
     set_error("the batched sampler benchmark needs 1..32 input particles");
     return kErrLimit;
@@ -812,7 +954,7 @@ int boss_gccb_bench(const double* matrix, int32_t m, const int32_t* input_state,
   cudaError_t e = cudaSuccess;
   // (1) the plain graph, timed per step
   GccbRun R;
-  st = gccb_prepare(cx, matrix, m, n, n_samples, L, add, u, false, R);
+  st = gccb_prepare(cx, matrix, m, D, false, R);
   for (int it = 0; !st && it < n_warmup + n_steps; ++it) {
     if (flush_bytes > 0 && (e = cudaMemsetAsync(cx->misc.ptr, it & 0xff, (size_t)flush_bytes, cx->stream)))
       break;
@@ -830,7 +972,7 @@ int boss_gccb_bench(const double* matrix, int32_t m, const int32_t* input_state,
   // (2) the same work with an event pair around every sweep launch: the sweep
   // kernels' share of a step (event nodes cost time, so steps are not timed here)
   GccbRun RT;
-  if (!st && e == cudaSuccess) st = gccb_prepare(cx, matrix, m, n, n_samples, L, add, u, true, RT);
+  if (!st && e == cudaSuccess) st = gccb_prepare(cx, matrix, m, D, true, RT);
   for (int it = 0; !st && e == cudaSuccess && it < n_steps; ++it) {
     if (flush_bytes > 0 && (e = cudaMemsetAsync(cx->misc.ptr, it & 0xff, (size_t)flush_bytes, cx->stream)))
       break;

@@ -63,7 +63,9 @@ struct SweepProblem {
   int64_t part_off;  // partials: n_threads complex (perms) or n_threads x nd (all-minors)
   double scale;      // final real scale
   int32_t fixed_digit;  // gradients: a binary digit held at r = 0 (Glynn halving) adds one weight-1 column
-  int32_t reserved;
+  int32_t group;     // all-minors: each aligned group of `group` threads (1, 2, 4, .., 32) sums its
+                     // minors, so the partials are (n_threads / group) x nd; n_threads and
+                     // thread_begin are multiples of it, and every sweep of the launch has the same
   uint8_t mult[kMaxDigits];
 };
 

@@ -152,8 +152,29 @@ __global__ void __launch_bounds__(128) minors_sweep_kernel(const SweepProblem* _
     }
     settle_minors(P, M, Rr, Ri, w, g, t_seg);
   }
-  double2* out = partials + P.part_off + q * nd;
-  for (int j = 0; j < nd; ++j) out[j] = M[j * 128];
+  const int G = P.group;
+  if (G > 1) {  // each aligned group of G lanes (one sweep's threads) sums its minors:
+                // lane l of the group adds up digits l, l + G, .. over the group, in a fixed order
+    const int lane = threadIdx.x & 31;
+    const int64_t warp0 = gt - lane;  // lanes past the launch's last thread have exited
+    const unsigned live = (warp0 + 32 <= total_threads) ? 0xffffffffu : ((1u << (total_threads - warp0)) - 1u);
+    __syncwarp(live);
+    const int gl = lane & (G - 1);
+    const double2* grp = minors_smem + (threadIdx.x - gl);
+    double2* out = partials + P.part_off + (q / G) * nd;
+    for (int j = gl; j < nd; j += G) {
+      double sx = 0.0, sy = 0.0;
+      for (int i = 0; i < G; ++i) {
+        const double2 v = grp[j * 128 + ((i + gl) & (G - 1))];  // staggered: fewer bank conflicts
+        sx += v.x;
+        sy += v.y;
+      }
+      out[j] = make_double2(sx, sy);
+    }
+  } else {
+    double2* out = partials + P.part_off + q * nd;
+    for (int j = 0; j < nd; ++j) out[j] = M[j * 128];
+  }
 }
 
 
