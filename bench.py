@@ -56,7 +56,7 @@ def parse():
     ap.add_argument("--samples", type=int, default=10000)
     ap.add_argument("--seed", type=int, default=2026)
     ap.add_argument("--quick", action="store_true", help="skip the single-permanent and plain-driver sections")
-    ap.add_argument("--case", choices=["perm", "grad"],
+    ap.add_argument("--case", choices=["perm", "grad", "dist"],
                     help="run one small kernel case instead of the bench (for profiler captures): "
                          "Glynn permanents or permanents with all n^2 derivatives, n photons in 2n modes")
     ap.add_argument("--n", type=int, default=24, help="photons of --case")
@@ -75,8 +75,16 @@ def run_case(args):
     T = c2_patterns(args.n, args.patterns, args.seed + args.n)
     S = np.zeros_like(T)
     S[:, :args.n] = 1
-    call = ((lambda: _native.perm_batch(U, S, T, _native.GLYNN)) if args.case == "perm"
-            else (lambda: _native.perm_grad_batch(U, S, T)))
+    if args.case == "dist":  # uniform-loss outcomes of n single photons in 2n modes
+        from theboss_gb300.utilities import possible_states_array
+
+        outs = possible_states_array(args.n, m, losses=True)
+        inp = [1] * args.n + [0] * args.n
+        call = lambda: _native.lossy_probabilities(U, inp, outs)  # noqa: E731
+    elif args.case == "perm":
+        call = lambda: _native.perm_batch(U, S, T, _native.GLYNN)  # noqa: E731
+    else:
+        call = lambda: _native.perm_grad_batch(U, S, T)  # noqa: E731
     call()
     t = time.perf_counter()
     call()
@@ -285,6 +293,53 @@ def adjoint_section(seed):
     return {"clements_log_likelihood_n12_m24": c4, "gradients_n24_m48": c5}
 
 
+def distribution_section(peak_tflops, seed):
+    """Exact uniform-loss distribution (theboss's BSDistributionCalculatorWithUniformLosses):
+    n=8 single photons in m=16 modes, eta=0.5, every one of the C(24, 8) = 735,471
+    lossy outcomes; GPU permanents of every (lossy input, outcome) pair.  The CPU
+    line is the oracle (C permanents, theboss's arithmetic in Python) on a bounded
+    sample of the outcomes."""
+    from math import comb
+
+    from oracle import oracle as O
+    from theboss_gb300 import _native
+    from theboss_gb300.distribution_calculators import (BosonSamplingExperimentConfiguration,
+                                                        BSDistributionCalculatorWithUniformLosses)
+    from theboss_gb300.utilities import haar_unitary, possible_states_array
+
+    n, m, eta = 8, 16, 0.5
+    U = haar_unitary(m, seed + 16)
+    inp = [1] * n + [0] * (m - n)
+    cfg = BosonSamplingExperimentConfiguration(interferometer_matrix=U, initial_state=inp,
+                                               initial_number_of_particles=n, number_of_modes=m,
+                                               number_of_particles_lost=0, number_of_particles_left=n,
+                                               uniform_transmissivity=eta)
+    calc = BSDistributionCalculatorWithUniformLosses(cfg, None)
+    calc.calculate_distribution()  # warm-up
+    t = time.perf_counter()
+    dist = np.array(calc.calculate_distribution())
+    e2e_s = time.perf_counter() - t
+    outs = possible_states_array(n, m, losses=True)
+    _, kernel_ms = _native.lossy_probabilities(U, inp, outs, timed=True)
+    ls = outs.sum(axis=1)
+    # Glynn flops per pair: 2^(l-1) codes x (8 l - 4); pairs: C(n, l) lossy inputs x outcomes of l
+    flops = float(sum(comb(n, l) * int((ls == l).sum()) * 2 ** (l - 1) * (8 * l - 4) for l in range(1, n + 1)))
+    tf = flops / (kernel_ms / 1e3) / 1e12
+    rng = np.random.default_rng(seed)
+    pick = rng.choice(len(outs), size=300, replace=False)
+    w = O.binomial_weights(n, eta)
+    t = time.perf_counter()
+    ref = [w[0] if ls[i] == 0 else O.fixed_loss_probability(U, inp, outs[i]) * w[ls[i]] for i in pick]
+    cpu_s = time.perf_counter() - t
+    err = float(np.max(np.abs(dist[pick] - ref) / np.maximum(np.abs(ref), 1e-300)))
+    return {"workload": "uniform losses eta=0.5, n=8, m=16, all 735,471 outcomes, Haar unitary",
+            "outcomes_per_s_e2e": len(outs) / e2e_s, "e2e_ms": e2e_s * 1e3, "kernel_ms": kernel_ms,
+            "sum": float(dist.sum()), "achieved_tflops": tf, "frac_of_fp64_peak": tf / peak_tflops,
+            "max_rel_err_vs_oracle_sample": err,
+            "cpu_oracle": {"outcomes_per_s": len(pick) / cpu_s, "cores": 1, "kind": "port",
+                           "sample": f"{len(pick)} random outcomes of the same workload, {cpu_s:.1f} s"}}
+
+
 def run_ours(args, rank, world):
     from theboss_gb300 import _native
     from theboss_gb300.simulation_strategies import GCCBPlainDriver
@@ -345,6 +400,7 @@ def run_ours(args, rank, world):
         line["batched_vs_plain"] = {"device": value / world / plain, "e2e": e2e["value"] / plain}
         line["single_permanents"] = single_permanents(peak, args.seed)
         line["adjoint"] = adjoint_section(args.seed)
+        line["exact_distribution"] = distribution_section(peak, args.seed)
     if rank == 0:
         line["cpu_baseline"] = cpu_baseline(U, inp, w, args.seed)
         print(json.dumps(line), flush=True)

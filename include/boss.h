@@ -217,6 +217,26 @@ BOSS_API int boss_perm_batch_noalloc(const double* matrix, int32_t m, const int3
  */
 BOSS_API int boss_fp64_peak(double* tflops, double* milliseconds);
 
+/*
+ * Exact probability of each outcome after particle losses, with l = sum(outcome)
+ * of the initial state's particles surviving.  Replaces
+ * BSDistributionCalculatorWithFixedLosses.__calculate_probability_of_outcome
+ * (bs_distribution_calculator_with_fixed_losses.py:84-151) with
+ * number_of_particles_left = l, evaluated for all outcomes at once; the
+ * uniform-loss calculator (bs_exact_distribution_with_uniform_losses.py:62-97)
+ * multiplies by its weight of l.
+ *   - outcomes: count x m occupations (any mix of particle counts <= sum(initial));
+ *     probabilities: count doubles.
+ *   - Lossy inputs in theboss's order (generate_lossy_n_particle_input_states);
+ *     an outcome with no particle has probability 1.
+ *   - kernel_ms (may be null): GPU time of the per-pair kernels, for benchmarks.
+ * BOSS_ERR_ARG when an outcome holds more particles than the initial state;
+ * BOSS_ERR_LIMIT beyond 5e7 particle combinations or 8 multiply occupied modes.
+ */
+BOSS_API int boss_lossy_probabilities(const double* matrix, int32_t m, const int32_t* initial_state,
+                                      const int32_t* outcomes, int32_t count, double* probabilities,
+                                      float* kernel_ms);
+
 #ifdef __cplusplus
 }
 #endif

@@ -245,8 +245,67 @@ def main(ref_root):
     with open(os.path.join(out_dir, "distributions.json"), "w") as f:
         json.dump([{"U": _m(P), "input": [1, 1, 1, 0, 0], "eta": 0.8, "distribution": [float(x) for x in dist]},
                    {"U": _m(U6), "input": [1, 1, 1, 0], "eta": 0.6, "distribution": [float(x) for x in dist2]}], f)
+    lossy_distributions(ref_root)
     print("fixtures written to", out_dir)
 
 
+def lossy_distributions(ref_root: str) -> None:
+    """Fixed- and uniform-loss exact distributions (standard and binned inputs, and
+    one 11-particle case) computed by theboss's own calculators."""
+    if ref_root not in sys.path:
+        sys.path.insert(0, ref_root)
+    from scipy.stats import unitary_group
+
+    from theboss.boson_sampling_utilities.permanent_calculators.ryser_permanent_calculator import (
+        RyserPermanentCalculator,
+    )
+    from theboss.boson_sampling_utilities.boson_sampling_utilities import generate_lossy_n_particle_input_states
+    from theboss.distribution_calculators.bs_exact_distribution_with_uniform_losses import (
+        BosonSamplingExperimentConfiguration,
+        BSDistributionCalculatorWithFixedLosses,
+        BSDistributionCalculatorWithUniformLosses,
+    )
+
+    out_dir = os.path.dirname(os.path.abspath(__file__))
+
+    def cfg(U, inp, lost, eta=1.0):
+        n = int(sum(inp))
+        return BosonSamplingExperimentConfiguration(
+            interferometer_matrix=U, initial_state=list(inp), initial_number_of_particles=n,
+            number_of_modes=len(inp), number_of_particles_lost=lost, number_of_particles_left=n - lost,
+            uniform_transmissivity=eta)
+
+    cases = []
+    U4 = unitary_group.rvs(4, random_state=71)
+    for inp, lost in (([1, 1, 1, 0], 1), ([3, 1, 2, 0], 2)):
+        c = BSDistributionCalculatorWithFixedLosses(cfg(U4, inp, lost), RyserPermanentCalculator(U4))
+        cases.append({"kind": "fixed", "U": _m(U4), "input": inp, "lost": lost,
+                      "outcomes": [[int(x) for x in o] for o in c.get_outcomes_in_proper_order()],
+                      "probabilities": [float(x) for x in c.calculate_distribution()],
+                      "lossy_inputs": [[int(x) for x in s]
+                                       for s in generate_lossy_n_particle_input_states(inp, sum(inp) - lost)]})
+    c = BSDistributionCalculatorWithUniformLosses(cfg(U4, [3, 1, 2, 0], 0, 0.5), RyserPermanentCalculator(U4))
+    cases.append({"kind": "uniform", "U": _m(U4), "input": [3, 1, 2, 0], "lost": 0, "eta": 0.5,
+                  "outcomes": [[int(x) for x in o] for o in c.get_outcomes_in_proper_order()],
+                  "probabilities": [float(x) for x in c.calculate_distribution()]})
+    U8 = unitary_group.rvs(8, random_state=72)
+    c = BSDistributionCalculatorWithUniformLosses(cfg(U8, [1, 1, 1, 1, 1, 0, 0, 0], 0, 0.7), RyserPermanentCalculator(U8))
+    outs = c.get_outcomes_in_proper_order()[::37]
+    cases.append({"kind": "uniform", "U": _m(U8), "input": [1, 1, 1, 1, 1, 0, 0, 0], "lost": 0, "eta": 0.7,
+                  "outcomes": [[int(x) for x in o] for o in outs],
+                  "probabilities": [float(x) for x in c.calculate_probabilities_of_outcomes(outs)]})
+    U12 = unitary_group.rvs(12, random_state=73)
+    inp12 = [1] * 12
+    c = BSDistributionCalculatorWithFixedLosses(cfg(U12, inp12, 1), RyserPermanentCalculator(U12))
+    outs = [[1] * 11 + [0], [2, 0] + [1] * 9 + [0], [0, 3, 1, 1, 1, 1, 1, 1, 1, 0, 1, 0]]
+    cases.append({"kind": "fixed", "U": _m(U12), "input": inp12, "lost": 1, "outcomes": outs,
+                  "probabilities": [float(x) for x in c.calculate_probabilities_of_outcomes(outs)]})
+    with open(os.path.join(out_dir, "lossy_distributions.json"), "w") as f:
+        json.dump(cases, f)
+
+
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) > 2 and sys.argv[2] == "--lossy-only":
+        lossy_distributions(sys.argv[1])
+    else:
+        main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")

@@ -63,6 +63,19 @@ def test_exact_distributions_match_reference(oracle):
         assert np.allclose(got, rec["distribution"], rtol=0, atol=1e-15)
 
 
+def test_lossy_distributions_match_reference(oracle):
+    """Fixed- and uniform-loss probabilities (standard, binned and 11-particle
+    cases) against theboss's own calculators."""
+    for rec in load_golden("lossy_distributions.json"):
+        U = as_matrix(rec["U"])
+        got = [oracle.fixed_loss_probability(U, rec["input"], T) for T in rec["outcomes"]]
+        if rec["kind"] == "uniform":
+            n = sum(rec["input"])
+            w = oracle.binomial_weights(n, rec["eta"])
+            got = [w[0] if sum(T) == 0 else p * w[sum(T)] for p, T in zip(got, rec["outcomes"])]
+        assert np.allclose(got, rec["probabilities"], rtol=1e-12, atol=1e-300)
+
+
 def test_known_answer_permutation_distribution(oracle):
     """tests/test_exact_distribution_calculator.py:75-141 of the reference."""
     P = np.zeros((5, 5), dtype=complex)

@@ -75,6 +75,9 @@ def load() -> ctypes.CDLL:
         L.boss_perm_bench.restype = ctypes.c_int
         L.boss_perm_bench.argtypes = [dp, ctypes.c_int32, ip, ip, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
                                       ctypes.c_int32, ctypes.c_int32, ctypes.c_int64, dp, dp, dp]
+        L.boss_lossy_probabilities.restype = ctypes.c_int
+        L.boss_lossy_probabilities.argtypes = [dp, ctypes.c_int32, ip, ip, ctypes.c_int32, dp,
+                                               ctypes.POINTER(ctypes.c_float)]
         _lib = L
         return L
 
@@ -167,6 +170,28 @@ def perm_batch_noalloc(U: np.ndarray, S: np.ndarray, T: np.ndarray, variant: int
     count, n = S.shape
     check(L.boss_perm_batch_noalloc(_dp(U.view(np.float64)), U.shape[0], _ip(S), _ip(T), n, count, variant,
                                     ctypes.c_void_p(int(results_device_ptr)), ctypes.c_void_p(int(stream_ptr))))
+
+
+def lossy_probabilities(U: np.ndarray, initial_state, outcomes, timed: bool = False):
+    """Probability of each outcome with sum(outcome) of the initial particles
+    surviving (theboss's fixed-loss formula, boss_lossy_probabilities).  Returns a
+    float64 array, and the GPU kernel milliseconds when `timed`."""
+    L = load()
+    U = as_matrix(U)
+    m = U.shape[0]
+    S = np.ascontiguousarray(np.rint(np.asarray(initial_state, dtype=np.float64)).astype(np.int32))
+    T = np.asarray(outcomes)
+    if T.dtype.kind in "iu":
+        T = np.ascontiguousarray(T, dtype=np.int32).reshape(-1, m)
+    else:  # integer-valued floats or sequences
+        T = np.ascontiguousarray(np.rint(np.asarray(outcomes, dtype=np.float64)).astype(np.int32).reshape(-1, m))
+    if len(S) != m:
+        raise AttributeError("initial state length differs from the matrix dimension")
+    out = np.zeros(T.shape[0], dtype=np.float64)
+    ms = ctypes.c_float(0.0)
+    check(L.boss_lossy_probabilities(_dp(U.view(np.float64)), m, _ip(S), _ip(T), T.shape[0], _dp(out),
+                                     ctypes.byref(ms)))
+    return (out, float(ms.value)) if timed else out
 
 
 def fp64_peak():

@@ -319,7 +319,7 @@ static int fill_sweep(HostSweep& hs, const Side& dig, const Side& col, int kind,
 
 // One permanent request.  Returns kOk and either fills `hs` (needs_sweep = true)
 // or sets `value` directly for the edge cases theboss special-cases.
-static int plan_permanent(const double* U, int m, const int32_t* S, const int32_t* T, int len, int variant,
+int plan_permanent(const double* U, int m, const int32_t* S, const int32_t* T, int len, int variant,
                           HostSweep& hs, bool& needs_sweep, double2& value) {
   needs_sweep = false;
   if (len > m || len < 0) {  // bs_permanent_calculator_base.py:61-72

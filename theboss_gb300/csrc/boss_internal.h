@@ -87,6 +87,7 @@ struct Context {
   cudaStream_t stream = nullptr;
   DeviceBuffer plans, pool, partials, out, counter, index, misc, gpart, pperm;
   DeviceBuffer gccb[16];
+  DeviceBuffer dist[4];
   void* pinned = nullptr;
   size_t pinned_bytes = 0;
 };
@@ -98,5 +99,11 @@ int ensure_pinned(Context* cx, size_t bytes);
 // and the reduction, copies the results back.  results: one complex per sweep
 // (perms) or nd_max complex per sweep (all-minors).
 int run_sweeps(Context* cx, const std::vector<HostSweep>& sweeps, bool minors, int nd_max, double2* results_host);
+
+// One permanent request (theboss's variant semantics).  Returns kOk and either
+// fills `hs` (needs_sweep = true) or sets `value` for the edge cases theboss
+// special-cases.
+int plan_permanent(const double* U, int m, const int32_t* S, const int32_t* T, int len, int variant, HostSweep& hs,
+                   bool& needs_sweep, double2& value);
 
 }  // namespace boss

@@ -1,6 +1,14 @@
 """Host-side helpers of the sampling path (numpy, no GPU work).
 
   mode_occupation_to_mode_assignment          boson_sampling_utilities.py:61-78
+  mode_assignment_to_mode_occupation          boson_sampling_utilities.py:42-58
+  generate_possible_states                    boson_sampling_utilities.py:81-155 (same
+                                              order: per particle count, descending
+                                              lexicographic)
+  possible_states_array                       the same states as one int32 array
+  generate_lossy_n_particle_input_states      boson_sampling_utilities.py:158-203 (same
+                                              order: first occurrence over particle-index
+                                              combinations)
   prepare_interferometer_matrix_in_expanded_space
                                               boson_sampling_utilities.py:264-342
   haar_unitary                                seeded Haar-random unitary (Mezzadri's
@@ -9,7 +17,9 @@
 """
 from __future__ import annotations
 
-from typing import Sequence, Tuple
+import itertools
+from functools import lru_cache
+from typing import List, Sequence, Tuple
 
 import numpy as np
 
@@ -19,6 +29,68 @@ def mode_occupation_to_mode_assignment(mode_occupation: Sequence[int]) -> Tuple[
     for i, v in enumerate(mode_occupation):
         out += [i] * int(v)
     return tuple(out)
+
+
+def mode_assignment_to_mode_occupation(mode_assignment: Sequence[int], observed_modes_number: int = 0) -> Tuple[int, ...]:
+    """Particle -> mode list to an occupation tuple of observed_modes_number entries
+    (1 + the largest mode when 0)."""
+    m = int(observed_modes_number) if observed_modes_number else max(mode_assignment) + 1
+    occ = [0] * m
+    for i in mode_assignment:
+        occ[int(i)] += 1
+    return tuple(occ)
+
+
+@lru_cache(maxsize=None)
+def _compositions(n: int, m: int) -> np.ndarray:
+    """All m-mode n-particle occupations, descending lexicographic order."""
+    if m == 1:
+        return np.array([[n]], dtype=np.int32)
+    parts = []
+    for first in range(n, -1, -1):
+        rest = _compositions(n - first, m - 1)
+        block = np.empty((rest.shape[0], m), dtype=np.int32)
+        block[:, 0] = first
+        block[:, 1:] = rest
+        parts.append(block)
+    out = np.concatenate(parts)
+    out.setflags(write=False)
+    return out
+
+
+@lru_cache(maxsize=8)
+def possible_states_array(particles_number: int, modes_number: int, losses: bool = False) -> np.ndarray:
+    """generate_possible_states as a read-only int32 array (rows in the same order)."""
+    if particles_number < 0 or modes_number < 1:
+        return np.zeros((0, max(modes_number, 0)), dtype=np.int32)
+    first = 0 if losses else particles_number
+    out = np.concatenate([_compositions(k, modes_number) for k in range(first, particles_number + 1)])
+    out.setflags(write=False)
+    return out
+
+
+def generate_possible_states(particles_number: int, modes_number: int, losses: bool = False) -> List[Tuple[int, ...]]:
+    """All m-mode states with n particles (or 0..n with losses), as tuples."""
+    return [tuple(int(x) for x in row) for row in possible_states_array(particles_number, modes_number, losses)]
+
+
+def generate_lossy_n_particle_input_states(initial_state: Sequence[int], number_of_particles_left: int) -> List[Tuple[int, ...]]:
+    """Distinct sub-occupations of `initial_state` with the given particle count, in
+    the order of their first appearance over combinations of particle indices."""
+    m = len(initial_state)
+    if sum(initial_state) == 0:
+        return [tuple(initial_state)]
+    x0 = mode_occupation_to_mode_assignment(initial_state)
+    seen, out = set(), []
+    for comb in itertools.combinations(range(len(x0)), number_of_particles_left):
+        occ = [0] * m
+        for c in comb:
+            occ[x0[c]] += 1
+        key = tuple(occ)
+        if key not in seen:
+            seen.add(key)
+            out.append(key)
+    return out
 
 
 def _loss_transfer_expansion(transmissivities: np.ndarray) -> np.ndarray:
