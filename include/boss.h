@@ -237,6 +237,18 @@ BOSS_API int boss_lossy_probabilities(const double* matrix, int32_t m, const int
                                       const int32_t* outcomes, int32_t count, double* probabilities,
                                       float* kernel_ms);
 
+/*
+ * How many of the n_samples samples (n_samples x m occupations) equal each of the
+ * n_outcomes listed outcomes; a sample equal to several listed outcomes counts for
+ * the first.  Replaces the Python scan of
+ * BSSampleBasedDistributionCalculator.calculate_approximate_distribution
+ * (bs_sample_based_distribution_calculator.py:94-106).  counts: n_outcomes int64.
+ * Sample occupations must lie in [0, 254] (BOSS_ERR_ARG otherwise); an outcome
+ * outside that range matches no sample.
+ */
+BOSS_API int boss_count_outcomes(const int32_t* samples, int64_t n_samples, const int32_t* outcomes,
+                                 int64_t n_outcomes, int32_t m, int64_t* counts);
+
 #ifdef __cplusplus
 }
 #endif

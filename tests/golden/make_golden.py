@@ -246,7 +246,66 @@ def main(ref_root):
         json.dump([{"U": _m(P), "input": [1, 1, 1, 0, 0], "eta": 0.8, "distribution": [float(x) for x in dist]},
                    {"U": _m(U6), "input": [1, 1, 1, 0], "eta": 0.6, "distribution": [float(x) for x in dist2]}], f)
     lossy_distributions(ref_root)
+    mode_assignment_samples(ref_root)
+    tvd_values(ref_root)
     print("fixtures written to", out_dir)
+
+
+def tvd_values(ref_root: str) -> None:
+    """theboss's total-variation distances of seeded distributions (lists and dicts)."""
+    if ref_root not in sys.path:
+        sys.path.insert(0, ref_root)
+    from theboss.quantum_computations_utilities import (
+        count_total_variation_distance,
+        count_total_variation_distance_dicts,
+    )
+
+    out_dir = os.path.dirname(os.path.abspath(__file__))
+    rng = np.random.default_rng(91)
+    recs = []
+    for size in (1, 7, 1000, 3001):
+        a, b = rng.random(size), rng.random(size)
+        a, b = a / a.sum(), b / b.sum()
+        recs.append({"kind": "list", "a": a.tolist(), "b": b.tolist(),
+                     "tvd": float(count_total_variation_distance(list(a), list(b)))})
+    for size in (5, 60, 400):
+        d1, d2 = {}, {}
+        for d in (d1, d2):
+            for _ in range(size):
+                d[tuple(int(v) for v in rng.integers(0, 4, 5))] = float(rng.random())
+        recs.append({"kind": "dict", "d1": [[list(k), v] for k, v in d1.items()],
+                     "d2": [[list(k), v] for k, v in d2.items()],
+                     "tvd": float(count_total_variation_distance_dicts(d1, d2))})
+    with open(os.path.join(out_dir, "tvd.json"), "w") as f:
+        json.dump(recs, f)
+
+
+def mode_assignment_samples(ref_root: str) -> None:
+    """Seeded sample streams of theboss's mode-assignment generalized C&C."""
+    if ref_root not in sys.path:
+        sys.path.insert(0, ref_root)
+    from scipy.stats import unitary_group
+
+    from theboss.boson_sampling_utilities.permanent_calculators.ryser_permanent_calculator import (
+        RyserPermanentCalculator,
+    )
+    from theboss.simulation_strategies.mode_assignment_generalized_cliffords_simulation_strategy import (
+        ModeAssignmentGeneralizedCliffordsSimulationStrategyInterface,
+    )
+
+    out_dir = os.path.dirname(os.path.abspath(__file__))
+    recs = []
+    for seed, inp, N in ((81, [1, 1, 1, 0, 0, 0], 30), (82, [2, 0, 1, 1, 0], 25)):
+        U = unitary_group.rvs(len(inp), random_state=seed)
+        np.random.seed(seed)
+        strat = ModeAssignmentGeneralizedCliffordsSimulationStrategyInterface(RyserPermanentCalculator(U))
+        samples = strat.simulate(inp, N)
+        recs.append({"seed": seed, "U": _m(U), "input": inp, "N": N,
+                     "samples": [[int(x) for x in s] for s in samples],
+                     "r_sample": [int(x) for x in strat.r_sample],
+                     "next_random": float(np.random.random())})
+    with open(os.path.join(out_dir, "mode_assignment_samples.json"), "w") as f:
+        json.dump(recs, f)
 
 
 def lossy_distributions(ref_root: str) -> None:
@@ -305,7 +364,9 @@ def lossy_distributions(ref_root: str) -> None:
 
 
 if __name__ == "__main__":
-    if len(sys.argv) > 2 and sys.argv[2] == "--lossy-only":
-        lossy_distributions(sys.argv[1])
+    # python make_golden.py <theboss checkout> [--only lossy|mode_assignment]
+    sections = {"lossy": lossy_distributions, "mode_assignment": mode_assignment_samples, "tvd": tvd_values}
+    if len(sys.argv) > 3 and sys.argv[2] == "--only":
+        sections[sys.argv[3]](sys.argv[1])
     else:
         main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")

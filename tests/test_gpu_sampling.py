@@ -51,6 +51,21 @@ def test_gccb_fixtures_match_reference_streams():
         assert np.random.random() == rec["next_random"], rec["kind"]
 
 
+def test_mode_assignment_gcc_matches_reference_streams():
+    """mode_assignment_generalized_cliffords_simulation_strategy.py: seeded streams,
+    the last sample's mode order and the generator state theboss leaves."""
+    from theboss_gb300 import simulation_strategies as ss
+
+    for rec in load_golden("mode_assignment_samples.json"):
+        np.random.seed(rec["seed"])
+        strat = ss.ModeAssignmentGeneralizedCliffordsSimulationStrategyInterface(_calc(as_matrix(rec["U"])))
+        out = strat.simulate(rec["input"], rec["N"])
+        assert all(isinstance(s, tuple) for s in out)
+        assert [list(s) for s in out] == rec["samples"]
+        assert list(strat.r_sample) == rec["r_sample"]
+        assert np.random.random() == rec["next_random"]
+
+
 @pytest.mark.parametrize("n,m,eta,N", [(12, 24, 0.5, 400), (20, 40, 0.5, 300), (8, 16, None, 200)])
 def test_batched_sampler_matches_oracle(oracle, n, m, eta, N):
     from theboss_gb300 import _native

@@ -78,6 +78,9 @@ def load() -> ctypes.CDLL:
         L.boss_lossy_probabilities.restype = ctypes.c_int
         L.boss_lossy_probabilities.argtypes = [dp, ctypes.c_int32, ip, ip, ctypes.c_int32, dp,
                                                ctypes.POINTER(ctypes.c_float)]
+        L.boss_count_outcomes.restype = ctypes.c_int
+        L.boss_count_outcomes.argtypes = [ip, ctypes.c_int64, ip, ctypes.c_int64, ctypes.c_int32,
+                                          ctypes.POINTER(ctypes.c_int64)]
         _lib = L
         return L
 
@@ -192,6 +195,27 @@ def lossy_probabilities(U: np.ndarray, initial_state, outcomes, timed: bool = Fa
     check(L.boss_lossy_probabilities(_dp(U.view(np.float64)), m, _ip(S), _ip(T), T.shape[0], _dp(out),
                                      ctypes.byref(ms)))
     return (out, float(ms.value)) if timed else out
+
+
+def _state_rows(states, m: int) -> np.ndarray:
+    a = np.asarray(states)
+    if a.size == 0:
+        return np.zeros((0, m), dtype=np.int32)
+    if a.dtype.kind not in "iu":
+        a = np.rint(np.asarray(a, dtype=np.float64))
+    return np.ascontiguousarray(a, dtype=np.int32).reshape(-1, m)
+
+
+def count_outcomes(samples, outcomes, m: int) -> np.ndarray:
+    """For each listed outcome, how many samples equal it (the first listed copy of
+    a repeated outcome gets the counts); boss_count_outcomes.  int64 array."""
+    L = load()
+    S = _state_rows(samples, m)
+    O = _state_rows(outcomes, m)
+    out = np.zeros(O.shape[0], dtype=np.int64)
+    check(L.boss_count_outcomes(_ip(S), S.shape[0], _ip(O), O.shape[0], m,
+                                out.ctypes.data_as(ctypes.POINTER(ctypes.c_int64))))
+    return out
 
 
 def fp64_peak():

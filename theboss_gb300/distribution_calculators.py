@@ -155,3 +155,81 @@ def _register_with_reference() -> None:
 
 
 _register_with_reference()
+
+
+class BosonSamplingSimulator:
+    """boson_sampling_simulator.py:18-25: runs a strategy."""
+
+    def __init__(self, simulation_strategy) -> None:
+        self._simulation_strategy = simulation_strategy
+
+    def get_classical_simulation_results(self, input_state, samples_number: int = 1):
+        return self._simulation_strategy.simulate(input_state, samples_number)
+
+
+class BSSampleBasedDistributionCalculator(BSDistributionCalculatorInterface):
+    """Empirical distribution of a strategy's samples over a list of outcomes
+    (bs_sample_based_distribution_calculator.py:18-113).  The samples are counted
+    on the GPU (boss_count_outcomes) instead of theboss's sample-by-outcome scan.
+    As in theboss, calculate_distribution() and calculate_probabilities_of_outcomes()
+    draw calculate_approximate_distribution's default 5000 samples."""
+
+    def __init__(self, experiment_configuration: BosonSamplingExperimentConfiguration, strategy,
+                 samples_number=5000, outcomes=None) -> None:
+        self._configuration = experiment_configuration
+        self._strategy = strategy
+        self._outcomes = outcomes
+        self._samples_number = samples_number
+
+    @property
+    def configuration(self) -> BosonSamplingExperimentConfiguration:
+        return self._configuration
+
+    @configuration.setter
+    def configuration(self, new_configuration: BosonSamplingExperimentConfiguration) -> None:
+        self._configuration = new_configuration
+
+    @property
+    def strategy(self):
+        return self._strategy
+
+    @strategy.setter
+    def strategy(self, new_strategy) -> None:
+        self._strategy = new_strategy
+
+    @property
+    def outcomes(self):
+        return self._outcomes
+
+    @outcomes.setter
+    def outcomes(self, new_outcomes) -> None:
+        self._outcomes = new_outcomes
+
+    @property
+    def samples_number(self) -> int:
+        return self._samples_number
+
+    @samples_number.setter
+    def samples_number(self, new_samples_number: int) -> None:
+        self._samples_number = new_samples_number
+
+    def calculate_distribution(self) -> List[float]:
+        return self.calculate_approximate_distribution()
+
+    def calculate_probabilities_of_outcomes(self, outcomes) -> List[float]:
+        self._outcomes = outcomes
+        return self.calculate_approximate_distribution()
+
+    def calculate_approximate_distribution(self, samples_number: int = 5000) -> List[float]:
+        m = self.configuration.number_of_modes
+        if self._outcomes is not None:
+            outcomes = self._outcomes
+        else:
+            outcomes = possible_states_array(self.configuration.number_of_particles_left, m)
+        samples = BosonSamplingSimulator(self._strategy).get_classical_simulation_results(
+            self.configuration.initial_state, samples_number)
+        counts = _native.count_outcomes(samples, outcomes, m)
+        return list(counts.astype(np.float64) / samples_number)
+
+    def get_outcomes_in_proper_order(self):
+        return self._outcomes

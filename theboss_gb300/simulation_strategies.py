@@ -199,6 +199,7 @@ class GeneralizedCliffordsSimulationStrategy(SimulationStrategyInterface):
         N = len(steps)
         offsets = np.concatenate([[0], np.cumsum(steps)]).astype(np.int64)
         r = [[0] * width for _ in range(N)]
+        self._last_modes = []  # modes sampled for the last sample, in order
         for k in range(max(steps, default=0)):
             active = [sidx for sidx in range(N) if steps[sidx] > k]
             missing = []
@@ -213,6 +214,8 @@ class GeneralizedCliffordsSimulationStrategy(SimulationStrategyInterface):
             for sidx in active:
                 key = tuple(r[sidx])
                 r[sidx] = self._sample(key, uniforms[offsets[sidx] + k])
+                if sidx == N - 1:
+                    self._last_modes.append(self._last_index)
         if N:
             self.r_sample = r[-1]
             self.current_key = tuple(self.r_sample)
@@ -230,6 +233,7 @@ class GeneralizedCliffordsSimulationStrategy(SimulationStrategyInterface):
                 break
             idx += 1
         self.current_sample_probability = pmf[idx]
+        self._last_index = idx
         return self.possible_outputs[key][idx]
 
     def _weights(self, k_vectors) -> np.ndarray:
@@ -311,3 +315,20 @@ class GeneralizedCliffordsUniformLossesSimulationStrategy(GeneralizedCliffordsSi
         uniforms = np.random.random(sum(kept)) if sum(kept) else np.zeros(0)
         width = len(self._bs_permanent_calculator.matrix)
         return [np.array(r, dtype=np.int64) for r in self._run(kept, uniforms, width)]
+
+
+class ModeAssignmentGeneralizedCliffordsSimulationStrategyInterface(GeneralizedCliffordsSimulationStrategy):
+    """Generalized C&C in the mode-assignment description
+    (mode_assignment_generalized_cliffords_simulation_strategy.py:16-112): the
+    prefix is the ordered tuple of sampled modes and layers are memoised per tuple.
+    A layer's probabilities depend only on the prefix's occupation, and theboss
+    draws the same one random() per step, so the samples equal the plain
+    strategy's for the same stream; this runs the same batched engine.  Samples
+    are occupation tuples; r_sample holds the last sample's modes in sampling order."""
+
+    def simulate(self, input_state, samples_number: int = 1) -> List[Tuple[int, ...]]:
+        samples = super().simulate(input_state, samples_number)
+        if samples:
+            self.r_sample = tuple(int(i) for i in self._last_modes)
+            self.current_key = self.r_sample
+        return [tuple(int(x) for x in s) for s in samples]
