@@ -249,6 +249,61 @@ BOSS_API int boss_lossy_probabilities(const double* matrix, int32_t m, const int
 BOSS_API int boss_count_outcomes(const int32_t* samples, int64_t n_samples, const int32_t* outcomes,
                                  int64_t n_outcomes, int32_t m, int64_t* counts);
 
+/*
+ * One lossless C&C-B sample per (matrix, input state) instance, all instances in
+ * one batched run.  Replaces the per-sample `helper_strategy.simulate(input)[0]`
+ * calls of the BOBS strategies (lossy_state_approximated_simulation_strategy.py:298-310,
+ * nonuniform_losses_approximation_strategy.py:274-296) and of
+ * GeneralizedCliffordsBSimulationStrategy.simulate (generalized_cliffords_b_simulation_strategy.py:41-110).
+ *   - matrices: n_matrices complex m x m (row-major U[out][in]); n_matrices is 1
+ *     (shared) or n_samples.  input_states: n_samples x m.
+ *   - randint_results / uniforms: n_samples x stride, the numbers theboss draws per
+ *     step (randint(0, particles left), then numpy.random.choice's random_sample);
+ *     entry k of row s is used for k < sum(input_states[s]).
+ *   - samples: n_samples x m output occupations.
+ * At most 32 particles per instance (BOSS_ERR_LIMIT); a randint result outside
+ * [0, particles left) is BOSS_ERR_ARG; an unnormalisable pmf is BOSS_ERR_PMF.
+ */
+BOSS_API int boss_gccb_sample_instances(const double* matrices, int32_t n_matrices, int32_t m,
+                                        const int32_t* input_states, int32_t n_samples,
+                                        const int32_t* randint_results, const double* uniforms, int32_t stride,
+                                        int32_t* samples);
+
+/*
+ * The random numbers of n_samples samples of the uniform-loss BOBS strategy
+ * (LossyStateApproximationSimulationStrategy._simulate_in_parallel,
+ * lossy_state_approximated_simulation_strategy.py:287-362), drawn in theboss's
+ * order from numpy's legacy MT19937 state (advanced in place): per sample the
+ * approximated part (choice over approx_parts with approx_weights), the exact
+ * part (choice over exact_parts), m - k phase uniforms, numpy's shuffle of
+ * range(m), then the C&C-B steps.  exact_parts: n_exact x k occupations;
+ * approx_parts: n_approx x (m - k).  Outputs: input_states (n_samples x m, the
+ * stacked parts), phase_uniforms (n_samples x (m - k)), permutations
+ * (n_samples x m), randint_results / uniforms (n_samples x stride).
+ */
+BOSS_API int boss_bobs_uniform_predraw(uint32_t* mt_key, int32_t* mt_pos, int32_t n_samples, int32_t m, int32_t k,
+                                       const int32_t* exact_parts, const double* exact_weights, int32_t n_exact,
+                                       const int32_t* approx_parts, const double* approx_weights, int32_t n_approx,
+                                       int32_t stride, int32_t* input_states, double* phase_uniforms,
+                                       int32_t* permutations, int32_t* randint_results, double* uniforms);
+
+/*
+ * The random numbers of n_samples samples of the non-uniform-loss BOBS strategy
+ * (NonuniformLossesApproximationStrategy._simulate_in_parallel,
+ * nonuniform_losses_approximation_strategy.py:263-347), in theboss's order: the
+ * mode that receives the approximated particles (randint(0, approximated_modes)),
+ * the surviving particles of every occupied mode when `lossy` (the module's
+ * choice(): one random() and a scan of loss_weights row `occupation`;
+ * loss_weights is (max_occupation + 1)^2), approximated_modes phase uniforms,
+ * then the C&C-B steps.  Outputs as in boss_bobs_uniform_predraw (no permutations).
+ */
+BOSS_API int boss_bobs_nonuniform_predraw(uint32_t* mt_key, int32_t* mt_pos, int32_t n_samples, int32_t m,
+                                          const int32_t* base_state, int32_t approximated_modes,
+                                          int32_t approximated_particles, const double* loss_weights,
+                                          int32_t max_occupation, int32_t lossy, int32_t stride,
+                                          int32_t* input_states, double* phase_uniforms, int32_t* randint_results,
+                                          double* uniforms);
+
 #ifdef __cplusplus
 }
 #endif

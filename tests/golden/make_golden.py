@@ -248,7 +248,61 @@ def main(ref_root):
     lossy_distributions(ref_root)
     mode_assignment_samples(ref_root)
     tvd_values(ref_root)
+    bobs_samples(ref_root)
     print("fixtures written to", out_dir)
+
+
+def bobs_samples(ref_root: str) -> None:
+    """Seeded streams of theboss's two BOBS strategies.  theboss's simulate() runs its
+    per-sample loop (_simulate_in_parallel) in spawned worker processes whose
+    generators cannot be seeded; the same loop is run here in this process after
+    the same preparation simulate() does."""
+    if ref_root not in sys.path:
+        sys.path.insert(0, ref_root)
+    from scipy.stats import unitary_group
+
+    from theboss.boson_sampling_utilities.permanent_calculators.ryser_permanent_calculator import (
+        RyserPermanentCalculator,
+    )
+    from theboss.simulation_strategies.lossy_state_approximated_simulation_strategy import (
+        LossyStateApproximationSimulationStrategy,
+    )
+    from theboss.simulation_strategies.nonuniform_losses_approximation_strategy import (
+        NonuniformLossesApproximationStrategy,
+    )
+
+    out_dir = os.path.dirname(os.path.abspath(__file__))
+    recs = []
+    for seed, inp, eta, k, N in ((101, [1, 1, 1, 1, 0, 0], 0.6, 2, 40), (102, [1, 1, 1, 1, 1, 0, 0], 0.8, 3, 30),
+                                 (103, [1, 1, 1, 0, 0], 0.5, 1, 30)):
+        U = unitary_group.rvs(len(inp), random_state=seed)
+        calc = RyserPermanentCalculator(U, input_state=inp)
+        strat = LossyStateApproximationSimulationStrategy(calc, eta, k, threads_number=1)
+        strat._prepare_not_approximated_lossy_mixed_state(inp[:k])
+        strat._prepare_approximated_input_state(inp[k:])
+        np.random.seed(seed)
+        samples = strat._simulate_in_parallel(N)
+        recs.append({"kind": "uniform_bobs", "seed": seed, "U": _m(U), "input": inp, "eta": eta, "k": k, "N": N,
+                     "samples": [[int(x) for x in s] for s in samples], "next_random": float(np.random.random())})
+    for seed, inp, ka, N in ((111, [1, 1, 1, 1, 0, 0], 2, 30), (112, [2, 1, 0, 1, 0], 3, 25)):
+        m = len(inp)
+        V = unitary_group.rvs(m, random_state=seed)
+        t = np.random.default_rng(seed).uniform(0.4, 0.9, m)
+        M = V @ np.diag(np.sqrt(t))
+        calc = RyserPermanentCalculator(M, input_state=inp)
+        strat = NonuniformLossesApproximationStrategy(calc, ka, threads_number=1)
+        strat._state_without_approximated_modes = list(inp)
+        for i in range(strat._approximated_modes_number):  # simulate()'s preparation
+            strat._approximated_modes_particles_number += inp[i]
+            strat._state_without_approximated_modes[i] = 0
+        strat._binomial_weights = strat._compute_binomial_weights(
+            max(max(inp), strat._approximated_modes_particles_number))
+        np.random.seed(seed)
+        samples = strat._simulate_in_parallel(N)
+        recs.append({"kind": "nonuniform_bobs", "seed": seed, "U": _m(M), "input": inp, "k": ka, "N": N,
+                     "samples": [[int(x) for x in s] for s in samples], "next_random": float(np.random.random())})
+    with open(os.path.join(out_dir, "bobs_samples.json"), "w") as f:
+        json.dump(recs, f)
 
 
 def tvd_values(ref_root: str) -> None:
@@ -365,7 +419,8 @@ def lossy_distributions(ref_root: str) -> None:
 
 if __name__ == "__main__":
     # python make_golden.py <theboss checkout> [--only lossy|mode_assignment]
-    sections = {"lossy": lossy_distributions, "mode_assignment": mode_assignment_samples, "tvd": tvd_values}
+    sections = {"lossy": lossy_distributions, "mode_assignment": mode_assignment_samples, "tvd": tvd_values,
+                "bobs": bobs_samples}
     if len(sys.argv) > 3 and sys.argv[2] == "--only":
         sections[sys.argv[3]](sys.argv[1])
     else:

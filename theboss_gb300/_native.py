@@ -81,6 +81,17 @@ def load() -> ctypes.CDLL:
         L.boss_count_outcomes.restype = ctypes.c_int
         L.boss_count_outcomes.argtypes = [ip, ctypes.c_int64, ip, ctypes.c_int64, ctypes.c_int32,
                                           ctypes.POINTER(ctypes.c_int64)]
+        L.boss_gccb_sample_instances.restype = ctypes.c_int
+        L.boss_gccb_sample_instances.argtypes = [dp, ctypes.c_int32, ctypes.c_int32, ip, ctypes.c_int32, ip, dp,
+                                                 ctypes.c_int32, ip]
+        L.boss_bobs_uniform_predraw.restype = ctypes.c_int
+        L.boss_bobs_uniform_predraw.argtypes = [up, ip, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, ip, dp,
+                                                ctypes.c_int32, ip, dp, ctypes.c_int32, ctypes.c_int32, ip, dp, ip,
+                                                ip, dp]
+        L.boss_bobs_nonuniform_predraw.restype = ctypes.c_int
+        L.boss_bobs_nonuniform_predraw.argtypes = [up, ip, ctypes.c_int32, ctypes.c_int32, ip, ctypes.c_int32,
+                                                   ctypes.c_int32, dp, ctypes.c_int32, ctypes.c_int32,
+                                                   ctypes.c_int32, ip, dp, ip, dp]
         _lib = L
         return L
 
@@ -216,6 +227,77 @@ def count_outcomes(samples, outcomes, m: int) -> np.ndarray:
     check(L.boss_count_outcomes(_ip(S), S.shape[0], _ip(O), O.shape[0], m,
                                 out.ctypes.data_as(ctypes.POINTER(ctypes.c_int64))))
     return out
+
+
+def gccb_sample_instances(matrices: np.ndarray, input_states: np.ndarray, randint_results: np.ndarray,
+                          uniforms: np.ndarray) -> np.ndarray:
+    """One lossless C&C-B sample per (matrix, input) instance with pre-drawn numbers
+    (boss_gccb_sample_instances).  matrices: (m, m) shared or (N, m, m).  Returns
+    int32 (N x m)."""
+    L = load()
+    Mx = np.ascontiguousarray(matrices, dtype=np.complex128)
+    m = Mx.shape[-1]
+    n_mats = 1 if Mx.ndim == 2 else Mx.shape[0]
+    S = np.ascontiguousarray(input_states, dtype=np.int32).reshape(-1, m)
+    N = S.shape[0]
+    R = np.ascontiguousarray(randint_results, dtype=np.int32).reshape(N, -1)
+    Uu = np.ascontiguousarray(uniforms, dtype=np.float64).reshape(N, -1)
+    stride = R.shape[1]
+    if Uu.shape[1] != stride:
+        raise ValueError("randint results and uniforms need the same row length")
+    out = np.zeros((N, m), dtype=np.int32)
+    check(L.boss_gccb_sample_instances(_dp(Mx.view(np.float64)), n_mats, m, _ip(S), N, _ip(R), _dp(Uu), stride,
+                                       _ip(out)))
+    return out
+
+
+def _up(a: np.ndarray):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32))
+
+
+def bobs_uniform_predraw(n_samples: int, m: int, k: int, exact_parts, exact_weights, approx_parts, approx_weights,
+                         stride: int):
+    """Random numbers of the uniform-loss BOBS strategy from numpy's global
+    RandomState (advanced as theboss advances it).  Returns (inputs, phase
+    uniforms, permutations, randint results, uniforms)."""
+    L = load()
+    st, key, pos = _get_mt()
+    E = np.ascontiguousarray(exact_parts, dtype=np.int32).reshape(-1, max(k, 0)) if k else np.zeros(
+        (len(exact_weights), 0), dtype=np.int32)
+    A = np.ascontiguousarray(approx_parts, dtype=np.int32).reshape(len(approx_weights), m - k)
+    ew = np.ascontiguousarray(exact_weights, dtype=np.float64)
+    aw = np.ascontiguousarray(approx_weights, dtype=np.float64)
+    inputs = np.zeros((n_samples, m), dtype=np.int32)
+    ph = np.zeros((n_samples, max(m - k, 1)), dtype=np.float64)
+    perms = np.zeros((n_samples, m), dtype=np.int32)
+    ri = np.zeros((n_samples, max(stride, 1)), dtype=np.int32)
+    uu = np.zeros((n_samples, max(stride, 1)), dtype=np.float64)
+    check(L.boss_bobs_uniform_predraw(_up(key), _ip(pos), n_samples, m, k, _ip(np.ascontiguousarray(E)), _dp(ew),
+                                      len(ew), _ip(A), _dp(aw), len(aw), max(stride, 1), _ip(inputs), _dp(ph),
+                                      _ip(perms), _ip(ri), _dp(uu)))
+    _set_mt(st, key, pos)
+    return inputs, ph[:, :m - k], perms, ri, uu
+
+
+def bobs_nonuniform_predraw(n_samples: int, base_state, approximated_modes: int, approximated_particles: int,
+                            loss_weights, lossy: bool, stride: int):
+    """Random numbers of the non-uniform-loss BOBS strategy from numpy's global
+    RandomState.  loss_weights: square table, row o = weights of 0..o survivors.
+    Returns (inputs, phase uniforms, randint results, uniforms)."""
+    L = load()
+    st, key, pos = _get_mt()
+    base = np.ascontiguousarray(base_state, dtype=np.int32)
+    m = len(base)
+    W = np.ascontiguousarray(loss_weights, dtype=np.float64)
+    inputs = np.zeros((n_samples, m), dtype=np.int32)
+    ph = np.zeros((n_samples, max(approximated_modes, 1)), dtype=np.float64)
+    ri = np.zeros((n_samples, max(stride, 1)), dtype=np.int32)
+    uu = np.zeros((n_samples, max(stride, 1)), dtype=np.float64)
+    check(L.boss_bobs_nonuniform_predraw(_up(key), _ip(pos), n_samples, m, _ip(base), approximated_modes,
+                                         approximated_particles, _dp(W), W.shape[0] - 1, int(bool(lossy)),
+                                         max(stride, 1), _ip(inputs), _dp(ph), _ip(ri), _dp(uu)))
+    _set_mt(st, key, pos)
+    return inputs, ph[:, :approximated_modes], ri, uu
 
 
 def fp64_peak():

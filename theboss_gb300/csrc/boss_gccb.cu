@@ -95,14 +95,25 @@ static inline uint32_t mask_for(uint32_t n) {
 // (generalized_cliffords_b_simulation_strategy.py:97-105); `idx` holds the
 // randint results, i.e. positions in the list of the particles not yet popped.
 struct Draws {
-  int n = 0;                       // input particles
+  int n = 0;                       // row stride: the most input particles of a sample
   bool binned = false;             // some input mode holds more than one particle
-  std::vector<uint8_t> particles;  // particle -> mode (ascending)
+  std::vector<uint8_t> particles;  // [sample][n] particle -> mode of the sample's input (ascending)
+  std::vector<uint8_t> nparticles; // [sample] particles of the sample's input
   std::vector<int32_t> L;          // [sample] particles kept
   std::vector<uint8_t> idx;        // [sample][n] randint results
   std::vector<double> u;           // [sample][n] uniforms of numpy.random.choice
   std::vector<uint8_t> modes;      // [sample][n] popped modes (host copy, filled on demand)
 };
+
+// Every sample draws from the same input state.
+static void same_input(Draws& D, const std::vector<uint8_t>& particles, int n_samples) {
+  const int n = (int)particles.size();
+  D.n = n;
+  D.particles.resize((size_t)n_samples * std::max(n, 1));
+  for (int s = 0; s < n_samples; ++s)
+    if (n) memcpy(&D.particles[(size_t)s * n], particles.data(), n);
+  D.nparticles.assign(n_samples, (uint8_t)n);
+}
 
 // The popped modes from the randint results: remove the idx-th remaining particle.
 static void modes_from_draws(Draws& D) {
@@ -110,13 +121,14 @@ static void modes_from_draws(Draws& D) {
   D.modes.assign((size_t)N * std::max(n, 1), 0);
   uint8_t work[257];
   for (int s = 0; s < N; ++s) {
-    for (int k = 0; k < n; ++k) work[k] = D.particles[k];
+    const int ns = D.nparticles[s];
+    for (int k = 0; k < ns; ++k) work[k] = D.particles[(size_t)s * n + k];
     const uint8_t* is = &D.idx[(size_t)s * n];
     uint8_t* ms = &D.modes[(size_t)s * n];
     for (int k = 0; k < D.L[s]; ++k) {
       const int i = is[k];
       ms[k] = work[i];
-      for (int q = 0; q < n - 1; ++q) work[q] = (q >= i) ? work[q + 1] : work[q];  // fixed trip count
+      for (int q = 0; q < ns - 1; ++q) work[q] = (q >= i) ? work[q + 1] : work[q];  // fixed trip count
     }
   }
 }
@@ -142,10 +154,12 @@ static int predraw(const int32_t* input_state, int m, const double* weights, int
     set_error("at most 255 input particles");
     return kErrLimit;
   }
-  D.n = n;
-  D.particles.clear();
-  for (int i = 0; i < m; ++i)
-    for (int k = 0; k < input_state[i]; ++k) D.particles.push_back((uint8_t)i);
+  {
+    std::vector<uint8_t> particles;
+    for (int i = 0; i < m; ++i)
+      for (int k = 0; k < input_state[i]; ++k) particles.push_back((uint8_t)i);
+    same_input(D, particles, n_samples);
+  }
   if (weights && n_weights != n + 1) {
     set_error("particle-number weights must have n + 1 entries");
     return kErrArg;
@@ -209,7 +223,9 @@ struct FinalizeArgs {
   uint8_t* S;             // [sample][m] current input occupations
   uint8_t* T;             // [sample][m] output occupations
   const uint8_t* idx;     // [sample][n] randint results (position among the particles left)
-  const uint8_t* pmode;   // [n] particle -> input mode
+  const uint8_t* pmode;   // [sample][n] particle -> input mode
+  const uint8_t* npart;   // [sample] input particles
+  int64_t mstride;        // elements between the samples' matrices (0: one matrix for all)
   uint32_t* rem;          // [sample][8] particles not yet popped, as bits
   const double* uni;      // [sample][n] uniforms
   const SweepProblem* probs_cur;
@@ -263,6 +279,8 @@ __global__ void __launch_bounds__(kFinWarps * 32) gccb_finalize_kernel(FinalizeA
   const int j = blockIdx.x * kFinWarps + w;
   if (j >= a.A) return;
   const int m = a.m;
+  const double2* Us = a.U + (size_t)j * a.mstride;        // this sample's matrix
+  const longlong2* Ufxs = a.Ufx + (size_t)j * a.mstride;  // and its fixed-point copy
   uint8_t* S = a.S + (size_t)j * m;
   uint8_t* T = a.T + (size_t)j * m;
   int nd;
@@ -272,11 +290,12 @@ __global__ void __launch_bounds__(kFinWarps * 32) gccb_finalize_kernel(FinalizeA
     int mode = 0;
     if (lane == 0) {
       uint32_t* rem = a.rem + (size_t)j * 8;
+      const int np = a.npart[j];
       for (int q = 0; q < 8; ++q) {
         const int lo = q * 32;
-        rem[q] = (a.n >= lo + 32) ? 0xffffffffu : (a.n > lo ? ((1u << (a.n - lo)) - 1u) : 0u);
+        rem[q] = (np >= lo + 32) ? 0xffffffffu : (np > lo ? ((1u << (np - lo)) - 1u) : 0u);
       }
-      mode = a.pmode[pop_particle(rem, a.idx[(size_t)j * a.n])];
+      mode = a.pmode[(size_t)j * a.n + pop_particle(rem, a.idx[(size_t)j * a.n])];
       S[mode] = 1;
       sub_s[w][0] = make_double2(1.0, 0.0);
       dm_s[w][0] = (uint8_t)mode;
@@ -329,7 +348,7 @@ __global__ void __launch_bounds__(kFinWarps * 32) gccb_finalize_kernel(FinalizeA
   const int full = m & ~31;
   for (int o = lane; o < full; o += 32) {
     double re = 0.0, im = 0.0;
-    const double2* Urow = a.U + (size_t)o * m;
+    const double2* Urow = Us + (size_t)o * m;
     for (int d = 0; d < nd; ++d) {
       const double2 c = sub_s[w][d];
       const double2 u = Urow[dm_s[w][d]];
@@ -345,7 +364,7 @@ __global__ void __launch_bounds__(kFinWarps * 32) gccb_finalize_kernel(FinalizeA
     const int oi = lane / s, c0 = lane & (s - 1);
     double re = 0.0, im = 0.0;
     if (oi < r) {
-      const double2* Urow = a.U + (size_t)(full + oi) * m;
+      const double2* Urow = Us + (size_t)(full + oi) * m;
       for (int d = c0; d < nd; d += s) {
         const double2 c = sub_s[w][d];
         const double2 u = Urow[dm_s[w][d]];
@@ -434,7 +453,7 @@ __global__ void __launch_bounds__(kFinWarps * 32) gccb_finalize_kernel(FinalizeA
 
   // ---- the all-minors sweep of level k + 1 ----
   if (lane == 0) {
-    const int mode = a.pmode[pop_particle(a.rem + (size_t)j * 8, a.idx[(size_t)j * a.n + a.k])];
+    const int mode = a.pmode[(size_t)j * a.n + pop_particle(a.rem + (size_t)j * 8, a.idx[(size_t)j * a.n + a.k])];
     S[mode] = (uint8_t)(S[mode] + 1);
   }
   __syncwarp();
@@ -489,7 +508,7 @@ __global__ void __launch_bounds__(kFinWarps * 32) gccb_finalize_kernel(FinalizeA
   longlong2* D = a.pool_next + ls.pool_off;
   for (int e = lane; e < nd * nf; e += 32) {
     const int d = e / nf, f = e - d * nf;
-    D[e] = a.Ufx[(size_t)fm_s[w][f] * m + dm_s[w][d]];  // Ryser rows: U[out][in]
+    D[e] = Ufxs[(size_t)fm_s[w][f] * m + dm_s[w][d]];  // Ryser rows: U[out][in]
   }
   SweepProblem& P = a.probs_next[j];
   P.mult[lane] = (lane < nd) ? mult_s[w][lane] : 0;
@@ -536,7 +555,14 @@ static void destroy_events(GccbRun& R) {
   R.ev.clear();
 }
 
-static int gccb_prepare(Context* cx, const double* matrix, int m, Draws& D, bool timing, GccbRun& R) {
+__global__ void to_fixed_kernel(const double* __restrict__ x, long long* __restrict__ y, int64_t count, int fx) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < count) y[i] = __double2ll_rn(ldexp(x[i], fx));  // exact scaling, round to nearest even
+}
+
+// matrices: n_mats complex m x m matrices, U[out][in]; one for every sample
+// (n_mats == 1) or one per sample (n_mats == number of samples).
+static int gccb_prepare(Context* cx, const double* matrix, int n_mats, int m, Draws& D, bool timing, GccbRun& R) {
   const int N = (int)D.L.size();
   const int n = std::max(D.n, 1);
   const std::vector<int32_t>& L = D.L;
@@ -557,7 +583,7 @@ static int gccb_prepare(Context* cx, const double* matrix, int m, Draws& D, bool
     for (int k = 1; k <= L[s]; ++k) A[k]++;
   // fixed point: |row sum| <= n * max |component of U|
   double umax = 0.0;
-  for (size_t i = 0; i < (size_t)2 * m * m; ++i) umax = std::max(umax, std::fabs(matrix[i]));
+  for (size_t i = 0; i < (size_t)2 * m * m * n_mats; ++i) umax = std::max(umax, std::fabs(matrix[i]));
   int ex = 0;
   std::frexp(std::max(umax, 1e-300) * std::max(n, 1), &ex);
   const int fx = std::max(-900, std::min(61 - ex, 200));
@@ -666,10 +692,10 @@ static int gccb_prepare(Context* cx, const double* matrix, int m, Draws& D, bool
   std::vector<size_t> o_tab(Lmax + 2, 0);
   for (int k = 2; k <= Lmax; ++k) { o_tab[k] = off; off = al(off + sizeof(LevelSample) * tab[k].size()); }
   const size_t o_idx = off; off = al(off + (size_t)N * n);
-  const size_t o_pm = off; off = al(off + (size_t)n);
+  const size_t o_pm = off; off = al(off + (size_t)N * n);
+  const size_t o_np = off; off = al(off + (size_t)N);
   const size_t o_uni = off; off = al(off + sizeof(double) * (size_t)N * n);
-  const size_t o_U = off; off = al(off + sizeof(double2) * (size_t)m * m);
-  const size_t o_Ufx = off; off = al(off + sizeof(longlong2) * (size_t)m * m);
+  const size_t o_U = off; off = al(off + sizeof(double2) * (size_t)m * m * n_mats);
   const size_t arena = off;
   R.h2d_bytes = arena;
   R.d2h_bytes = (size_t)N * m + sizeof(int);
@@ -681,24 +707,25 @@ static int gccb_prepare(Context* cx, const double* matrix, int m, Draws& D, bool
   if ((st = ensure(cx->gccb[4], sizeof(longlong2) * (size_t)max_pool * 2 + 512))) return st;  // rows x2
   if ((st = ensure(cx->gccb[5], sizeof(double2) * (size_t)max_parts))) return st;            // partials
   if ((st = ensure(cx->gccb[6], sizeof(uint32_t) * 8 * (size_t)N))) return st;                // particles left
+  if ((st = ensure(cx->gccb[7], sizeof(longlong2) * (size_t)m * m * n_mats))) return st;      // U fixed point
   if ((st = ensure_pinned(cx, std::max(arena, al((size_t)N * m) + 256)))) return st;
   char* h = (char*)cx->pinned;
   memset(h, 0, o_idx);
   for (int k = 2; k <= Lmax; ++k) memcpy(h + o_tab[k], tab[k].data(), sizeof(LevelSample) * tab[k].size());
   uint8_t* hidx = (uint8_t*)(h + o_idx);
+  uint8_t* hpm = (uint8_t*)(h + o_pm);
+  uint8_t* hnp = (uint8_t*)(h + o_np);
   double* huni = (double*)(h + o_uni);
-  for (int jj = 0; jj < N; ++jj) {
-    memcpy(hidx + (size_t)jj * n, &D.idx[(size_t)order[jj] * n], n);
-    memcpy(huni + (size_t)jj * n, &D.u[(size_t)order[jj] * n], sizeof(double) * n);
+  const size_t mm = (size_t)m * m;
+  for (int jj = 0; jj < N; ++jj) {  // samples in level order
+    const int s = order[jj];
+    memcpy(hidx + (size_t)jj * n, &D.idx[(size_t)s * n], n);
+    memcpy(huni + (size_t)jj * n, &D.u[(size_t)s * n], sizeof(double) * n);
+    memcpy(hpm + (size_t)jj * n, &D.particles[(size_t)s * n], n);
+    hnp[jj] = D.nparticles[s];
+    if (n_mats > 1) memcpy(h + o_U + sizeof(double2) * mm * jj, matrix + 2 * mm * s, sizeof(double2) * mm);
   }
-  memset(h + o_pm, 0, n);
-  memcpy(h + o_pm, D.particles.data(), D.particles.size());
-  memcpy(h + o_U, matrix, sizeof(double2) * (size_t)m * m);
-  longlong2* hfx = (longlong2*)(h + o_Ufx);
-  for (size_t i = 0; i < (size_t)m * m; ++i) {
-    hfx[i].x = std::llrint(std::ldexp(matrix[2 * i], fx));
-    hfx[i].y = std::llrint(std::ldexp(matrix[2 * i + 1], fx));
-  }
+  if (n_mats == 1) memcpy(h + o_U, matrix, sizeof(double2) * mm);
   char* d = (char*)cx->gccb[0].ptr;
   uint8_t* dS = (uint8_t*)cx->gccb[1].ptr;
   R.dT = dS + (size_t)N * m;
@@ -710,6 +737,12 @@ static int gccb_prepare(Context* cx, const double* matrix, int m, Draws& D, bool
   cudaStream_t s = cx->stream;
   cudaError_t e = cudaMemcpyAsync(d, h, arena, cudaMemcpyHostToDevice, s);
   if (e != cudaSuccess) return fail_cuda(e, "H2D sampler arena");
+  longlong2* dUfx = (longlong2*)cx->gccb[7].ptr;
+  {
+    const int64_t cnt = (int64_t)2 * mm * n_mats;
+    to_fixed_kernel<<<(unsigned)((cnt + 255) / 256), 256, 0, s>>>((const double*)(d + o_U), (long long*)dUfx, cnt, fx);
+    if ((e = cudaGetLastError()) != cudaSuccess) return fail_cuda(e, "fixed-point matrices");
+  }
   destroy_events(R);
   if (timing) {
     R.ev.resize(2 * (size_t)std::max(Lmax - 1, 0));
@@ -749,7 +782,9 @@ static int gccb_prepare(Context* cx, const double* matrix, int m, Draws& D, bool
     fa.n = n;
     fa.fx = fx;
     fa.U = (const double2*)(d + o_U);
-    fa.Ufx = (const longlong2*)(d + o_Ufx);
+    fa.Ufx = dUfx;
+    fa.mstride = (n_mats > 1) ? (int64_t)mm : 0;
+    fa.npart = (const uint8_t*)(d + o_np);
     fa.S = dS;
     fa.T = R.dT;
     fa.idx = (const uint8_t*)(d + o_idx);
@@ -827,10 +862,10 @@ static int gccb_collect(Context* cx, GccbRun& R, int32_t* samples_out) {
   return kOk;
 }
 
-static int run_gccb(Context* cx, const double* matrix, int m, Draws& D, int32_t* samples_out) {
+static int run_gccb(Context* cx, const double* matrix, int n_mats, int m, Draws& D, int32_t* samples_out) {
   if (D.L.empty()) return kOk;
   GccbRun R;
-  int st = gccb_prepare(cx, matrix, m, D, false, R);
+  int st = gccb_prepare(cx, matrix, n_mats, m, D, false, R);
   if (st) return st;
   if ((st = gccb_launch(cx))) return st;
   return gccb_collect(cx, R, samples_out);
@@ -908,7 +943,7 @@ int boss_gccb_sample(const double* matrix, int32_t m, const int32_t* input_state
   if (any) {
     Context* cx = context(&st);
     if (!cx) return st;
-    st = run_gccb(cx, matrix, m, D, samples);
+    st = run_gccb(cx, matrix, 1, m, D, samples);
     if (st) return st;
   }
   memcpy(mt_key, mt.key, sizeof(mt.key));
@@ -954,7 +989,7 @@ int boss_gccb_bench(const double* matrix, int32_t m, const int32_t* input_state,
   cudaError_t e = cudaSuccess;
   // (1) the plain graph, timed per step
   GccbRun R;
-  st = gccb_prepare(cx, matrix, m, D, false, R);
+  st = gccb_prepare(cx, matrix, 1, m, D, false, R);
   for (int it = 0; !st && it < n_warmup + n_steps; ++it) {
     if (flush_bytes > 0 && (e = cudaMemsetAsync(cx->misc.ptr, it & 0xff, (size_t)flush_bytes, cx->stream)))
       break;
@@ -972,7 +1007,7 @@ int boss_gccb_bench(const double* matrix, int32_t m, const int32_t* input_state,
   // (2) the same work with an event pair around every sweep launch: the sweep
   // kernels' share of a step (event nodes cost time, so steps are not timed here)
   GccbRun RT;
-  if (!st && e == cudaSuccess) st = gccb_prepare(cx, matrix, m, D, true, RT);
+  if (!st && e == cudaSuccess) st = gccb_prepare(cx, matrix, 1, m, D, true, RT);
   for (int it = 0; !st && e == cudaSuccess && it < n_steps; ++it) {
     if (flush_bytes > 0 && (e = cudaMemsetAsync(cx->misc.ptr, it & 0xff, (size_t)flush_bytes, cx->stream)))
       break;
@@ -1000,6 +1035,206 @@ int boss_gccb_bench(const double* matrix, int32_t m, const int32_t* input_state,
   info[3] = (double)R.kernels;
   info[4] = (double)R.sweeps;
   info[5] = (double)R.Lmax;
+  memcpy(mt_key, mt.key, sizeof(mt.key));
+  *mt_pos = mt.pos;
+  return kOk;
+}
+
+// ---------------------------------------------------------------------------
+// Independent instances: one (matrix, input state) per sample, pre-drawn numbers.
+// ---------------------------------------------------------------------------
+int boss_gccb_sample_instances(const double* matrices, int32_t n_matrices, int32_t m, const int32_t* input_states,
+                               int32_t n_samples, const int32_t* randint_results, const double* uniforms,
+                               int32_t stride, int32_t* samples) {
+  if (!matrices || !input_states || !samples || m <= 0 || n_samples < 0 || stride < 0 ||
+      (n_samples > 0 && stride > 0 && (!randint_results || !uniforms))) {
+    set_error("null pointer or bad size");
+    return kErrArg;
+  }
+  if (n_matrices != 1 && n_matrices != n_samples) {
+    set_error("give one matrix, or one per sample");
+    return kErrArg;
+  }
+  if (m > 256) {
+    set_error("the batched sampler supports at most 256 modes");
+    return kErrLimit;
+  }
+  Draws D;
+  int n = 0;
+  std::vector<int> ns(n_samples, 0);
+  for (int s = 0; s < n_samples; ++s) {
+    for (int i = 0; i < m; ++i) {
+      const int v = input_states[(size_t)s * m + i];
+      if (v < 0 || v > 255) {
+        set_error("input occupations must be in [0, 255]");
+        return kErrArg;
+      }
+      if (v > 1) D.binned = true;
+      ns[s] += v;
+    }
+    n = std::max(n, ns[s]);
+  }
+  if (n > kMaxMinorDigits) {
+    set_error("the batched sampler supports at most 32 particles per sample");
+    return kErrLimit;
+  }
+  if (n > stride) {
+    set_error("stride is below the particle count of a sample");
+    return kErrArg;
+  }
+  D.n = n;
+  const int rs = std::max(n, 1);
+  D.particles.assign((size_t)n_samples * rs, 0);
+  D.nparticles.assign(n_samples, 0);
+  D.L.assign(n_samples, 0);
+  D.idx.assign((size_t)n_samples * rs, 0);
+  D.u.assign((size_t)n_samples * rs, 0.0);
+  for (int s = 0; s < n_samples; ++s) {
+    int p = 0;
+    for (int i = 0; i < m; ++i)
+      for (int c = 0; c < input_states[(size_t)s * m + i]; ++c) D.particles[(size_t)s * rs + p++] = (uint8_t)i;
+    D.nparticles[s] = (uint8_t)ns[s];
+    D.L[s] = ns[s];
+    for (int k = 0; k < ns[s]; ++k) {
+      const int r = randint_results[(size_t)s * stride + k];
+      if (r < 0 || r >= ns[s] - k) {
+        set_error("a randint result is outside [0, particles left)");
+        return kErrArg;
+      }
+      D.idx[(size_t)s * rs + k] = (uint8_t)r;
+      D.u[(size_t)s * rs + k] = uniforms[(size_t)s * stride + k];
+    }
+  }
+  D.n = rs;
+  memset(samples, 0, sizeof(int32_t) * (size_t)n_samples * m);
+  if (n == 0) return kOk;
+  std::lock_guard<std::mutex> lk(g_api_mutex);
+  int st;
+  Context* cx = context(&st);
+  if (!cx) return st;
+  return run_gccb(cx, matrices, n_matrices, m, D, samples);
+}
+
+// numpy legacy choice(range(len(p)), p=p): cdf = cumsum(p) / its last entry, one
+// random_sample, searchsorted(..., 'right').
+static std::vector<double> choice_cdf(const double* p, int n) {
+  std::vector<double> cdf(n);
+  double acc = 0.0;
+  for (int i = 0; i < n; ++i) cdf[i] = acc = acc + p[i];
+  const double last = cdf[n - 1];
+  for (int i = 0; i < n; ++i) cdf[i] /= last;
+  return cdf;
+}
+static int choice_draw(MT19937& mt, const std::vector<double>& cdf) {
+  const double u = mt.next_double();
+  return (int)(std::upper_bound(cdf.begin(), cdf.end(), u) - cdf.begin());
+}
+// The C&C-B steps of one lossless sample: per particle randint(0, left), then
+// numpy.random.choice's random_sample (generalized_cliffords_b_simulation_strategy.py:97-110).
+static void gccb_draws(MT19937& mt, int particles, int32_t* ri, double* uu) {
+  for (int k = 0; k < particles; ++k) {
+    const uint32_t left = (uint32_t)(particles - k);
+    ri[k] = (int32_t)mt.bounded(left, mask_for(left));
+    uu[k] = mt.next_double();
+  }
+}
+
+int boss_bobs_uniform_predraw(uint32_t* mt_key, int32_t* mt_pos, int32_t n_samples, int32_t m, int32_t k,
+                              const int32_t* exact_parts, const double* exact_weights, int32_t n_exact,
+                              const int32_t* approx_parts, const double* approx_weights, int32_t n_approx,
+                              int32_t stride, int32_t* input_states, double* phase_uniforms, int32_t* permutations,
+                              int32_t* randint_results, double* uniforms) {
+  if (!mt_key || !mt_pos || n_samples < 0 || m <= 0 || k < 0 || k > m || n_exact <= 0 || n_approx <= 0 ||
+      !exact_weights || !approx_weights || !input_states || !permutations || stride < 0) {
+    set_error("null pointer or bad size");
+    return kErrArg;
+  }
+  MT19937 mt;
+  int st = load_mt(mt, mt_key, mt_pos);
+  if (st) return st;
+  const int ma = m - k;  // approximated modes
+  const std::vector<double> cdf_a = choice_cdf(approx_weights, n_approx), cdf_e = choice_cdf(exact_weights, n_exact);
+  for (int s = 0; s < n_samples; ++s) {
+    // lossy_state_approximated_simulation_strategy.py:312-332: approximated part first
+    const int ia = choice_draw(mt, cdf_a);
+    const int ie = choice_draw(mt, cdf_e);
+    int32_t* in = input_states + (size_t)s * m;
+    int particles = 0;
+    for (int i = 0; i < k; ++i) particles += (in[i] = exact_parts[(size_t)ie * k + i]);
+    for (int i = 0; i < ma; ++i) particles += (in[k + i] = approx_parts[(size_t)ia * ma + i]);
+    if (particles > stride) {
+      set_error("stride is below the particle count of a sample");
+      return kErrArg;
+    }
+    // :348-362: the random phases are drawn before the column permutation
+    for (int i = 0; i < ma; ++i) phase_uniforms[(size_t)s * ma + i] = mt.next_double();
+    int32_t* perm = permutations + (size_t)s * m;
+    for (int i = 0; i < m; ++i) perm[i] = i;
+    for (int i = m - 1; i >= 1; --i) {  // numpy's legacy shuffle
+      const uint32_t j = mt.bounded((uint32_t)i + 1u, mask_for((uint32_t)i + 1u));
+      std::swap(perm[i], perm[j]);
+    }
+    gccb_draws(mt, particles, randint_results + (size_t)s * stride, uniforms + (size_t)s * stride);
+  }
+  memcpy(mt_key, mt.key, sizeof(mt.key));
+  *mt_pos = mt.pos;
+  return kOk;
+}
+
+int boss_bobs_nonuniform_predraw(uint32_t* mt_key, int32_t* mt_pos, int32_t n_samples, int32_t m,
+                                 const int32_t* base_state, int32_t approximated_modes, int32_t approximated_particles,
+                                 const double* loss_weights, int32_t max_occupation, int32_t lossy, int32_t stride,
+                                 int32_t* input_states, double* phase_uniforms, int32_t* randint_results,
+                                 double* uniforms) {
+  if (!mt_key || !mt_pos || n_samples < 0 || m <= 0 || !base_state || approximated_modes < 0 ||
+      approximated_modes > m || max_occupation < 0 || !input_states || stride < 0 || (lossy && !loss_weights)) {
+    set_error("null pointer or bad size");
+    return kErrArg;
+  }
+  MT19937 mt;
+  int st = load_mt(mt, mt_key, mt_pos);
+  if (st) return st;
+  const int ka = approximated_modes;
+  const int W = max_occupation + 1;  // loss_weights: row o = binomial weights of o particles
+  std::vector<int32_t> state(m);
+  for (int s = 0; s < n_samples; ++s) {
+    // nonuniform_losses_approximation_strategy.py:280-294
+    for (int i = 0; i < m; ++i) state[i] = base_state[i];
+    if (ka > 0) state[mt.bounded((uint32_t)ka, mask_for((uint32_t)ka))] = approximated_particles;
+    int32_t* in = input_states + (size_t)s * m;
+    int particles = 0;
+    for (int i = 0; i < m; ++i) {  // :298-329, the module's own choice()
+      const int occ = state[i];
+      int v = occ;
+      if (lossy && occ > 0) {
+        if (occ > max_occupation) {
+          set_error("an occupation exceeds the loss-weight table");
+          return kErrArg;
+        }
+        const double r = mt.next_double();
+        double acc = 0.0;
+        v = -1;
+        for (int q = 0; q <= occ; ++q) {
+          acc += loss_weights[(size_t)occ * W + q];
+          if (acc > r) {
+            v = q;
+            break;
+          }
+        }
+        if (v < 0) {
+          set_error("loss weights sum below the random number");
+          return kErrArg;
+        }
+      }
+      particles += (in[i] = v);
+    }
+    if (particles > stride) {
+      set_error("stride is below the particle count of a sample");
+      return kErrArg;
+    }
+    for (int i = 0; i < ka; ++i) phase_uniforms[(size_t)s * ka + i] = mt.next_double();
+    gccb_draws(mt, particles, randint_results + (size_t)s * stride, uniforms + (size_t)s * stride);
+  }
   memcpy(mt_key, mt.key, sizeof(mt.key));
   *mt_pos = mt.pos;
   return kOk;

@@ -11,6 +11,8 @@
                                               combinations)
   prepare_interferometer_matrix_in_expanded_space
                                               boson_sampling_utilities.py:264-342
+  compute_qft_matrix                          quantum_computations_utilities.py:158-178
+  generate_qft_matrix_for_first_m_modes       boson_sampling_utilities.py:505-521
   haar_unitary                                seeded Haar-random unitary (Mezzadri's
                                               QR of a complex Gaussian matrix with the
                                               phases of R's diagonal divided out)
@@ -91,6 +93,23 @@ def generate_lossy_n_particle_input_states(initial_state: Sequence[int], number_
             seen.add(key)
             out.append(key)
     return out
+
+
+def compute_qft_matrix(n: int) -> np.ndarray:
+    """n x n discrete Fourier matrix omega^(i j) / sqrt(n), omega = exp(2 pi i / n),
+    with theboss's numpy expression (so the entries are the same doubles)."""
+    if n == 0:
+        return np.asarray([])
+    omega = np.exp(2j * np.pi / n)
+    horizontal = np.tile(range(n), n).reshape(n, n)
+    return np.power(omega, horizontal * horizontal.transpose()) / np.sqrt(n)
+
+
+def generate_qft_matrix_for_first_m_modes(m: int, all_modes_number: int) -> np.ndarray:
+    """QFT on the first m modes, identity on the others."""
+    qft = np.eye(all_modes_number, dtype=np.complex128)
+    qft[0:m, 0:m] = compute_qft_matrix(m)
+    return qft
 
 
 def _loss_transfer_expansion(transmissivities: np.ndarray) -> np.ndarray:
