@@ -340,6 +340,66 @@ def distribution_section(peak_tflops, seed):
                            "sample": f"{len(pick)} random outcomes of the same workload, {cpu_s:.1f} s"}}
 
 
+def strategies_section(seed):
+    """The other samplers of the path, each timed through its drop-in class:
+    C1 plain generalized C&C (n=8, m=16, 1000 samples), C5 lossy-network C&C-B
+    (n=30 in m=60, 120 expanded modes, 16 samples), uniform-loss BOBS (n=20, m=40,
+    eta=0.5, hierarchy level 10, 2000 samples) and the GPU outcome counter
+    (10^6 samples over the 12,376 outcomes of n=6, m=12)."""
+    from theboss_gb300 import _native
+    from theboss_gb300.approximation_strategies import LossyStateApproximationSimulationStrategy
+    from theboss_gb300.permanent_calculators import RyserPermanentCalculator
+    from theboss_gb300.simulation_strategies import (GeneralizedCliffordsSimulationStrategy,
+                                                     LossyNetworksGeneralizedCliffordsSimulationStrategy)
+    from theboss_gb300.utilities import haar_unitary, possible_states_array
+
+    out = {}
+    U = haar_unitary(16, seed + 8)
+    strat = GeneralizedCliffordsSimulationStrategy(RyserPermanentCalculator(U))
+    np.random.seed(seed)
+    strat.simulate([1] * 8 + [0] * 8, 50)  # warm-up
+    np.random.seed(seed)
+    t = time.perf_counter()
+    strat.simulate([1] * 8 + [0] * 8, 1000)
+    dt = time.perf_counter() - t
+    out["c1_plain_gcc_n8_m16"] = {"samples_per_s": 1000 / dt, "s": dt, "samples": 1000}
+
+    m = 60
+    V = haar_unitary(m, seed + 60)
+    tr = np.random.default_rng(seed).uniform(0.3, 0.9, m)
+    calc = RyserPermanentCalculator(V @ np.diag(np.sqrt(tr)))
+    strat = LossyNetworksGeneralizedCliffordsSimulationStrategy(calc)
+    np.random.seed(seed)
+    t = time.perf_counter()
+    smp = strat.simulate([1] * 30 + [0] * 30, 16)
+    dt = time.perf_counter() - t
+    out["c5_lossy_network_n30_m60"] = {"samples_per_s": 16 / dt, "s": dt, "samples": 16,
+                                       "mean_particles_detected": float(np.mean([sum(s) for s in smp]))}
+
+    U40 = haar_unitary(40, seed + 40)
+    inp = [1] * 20 + [0] * 20
+    strat = LossyStateApproximationSimulationStrategy(RyserPermanentCalculator(U40, input_state=inp), 0.5, 10,
+                                                      threads_number=1)
+    np.random.seed(seed)
+    strat.simulate(inp, 100)
+    np.random.seed(seed)
+    t = time.perf_counter()
+    strat.simulate(inp, 2000)
+    dt = time.perf_counter() - t
+    out["uniform_bobs_n20_m40_k10"] = {"samples_per_s": 2000 / dt, "s": dt, "samples": 2000}
+
+    outs = possible_states_array(6, 12)
+    idx = np.random.default_rng(seed).integers(0, len(outs), 10 ** 6)
+    smp = np.ascontiguousarray(outs[idx])
+    _native.count_outcomes(smp[:1000], outs, 12)
+    t = time.perf_counter()
+    cnt = _native.count_outcomes(smp, outs, 12)
+    dt = time.perf_counter() - t
+    assert int(cnt.sum()) == 10 ** 6
+    out["outcome_counting_1e6_samples_12376_outcomes"] = {"samples_per_s": 1e6 / dt, "s": dt}
+    return out
+
+
 def run_ours(args, rank, world):
     from theboss_gb300 import _native
     from theboss_gb300.simulation_strategies import GCCBPlainDriver
@@ -401,6 +461,7 @@ def run_ours(args, rank, world):
         line["single_permanents"] = single_permanents(peak, args.seed)
         line["adjoint"] = adjoint_section(args.seed)
         line["exact_distribution"] = distribution_section(peak, args.seed)
+        line["strategies"] = strategies_section(args.seed)
     if rank == 0:
         line["cpu_baseline"] = cpu_baseline(U, inp, w, args.seed)
         print(json.dumps(line), flush=True)
