@@ -264,6 +264,19 @@ BOSS_API int boss_count_outcomes(const int32_t* samples, int64_t n_samples, cons
  * At most 32 particles per instance (BOSS_ERR_LIMIT); a randint result outside
  * [0, particles left) is BOSS_ERR_ARG; an unnormalisable pmf is BOSS_ERR_PMF.
  */
+/*
+ * boss_gccb_sample for one slice of a sample stream: replays the whole stream of
+ * n_samples samples (advancing the MT19937 state over all of them) and samples
+ * only samples [first, first + count) into `samples` (count x m).  Ranks that
+ * each take a slice of the same stream, from the same state, together produce
+ * exactly the samples of one boss_gccb_sample call (data-parallel sampling with
+ * the single-process stream).
+ */
+BOSS_API int boss_gccb_sample_slice(const double* matrix, int32_t m, const int32_t* input_state,
+                                    const double* particle_weights, int32_t n_weights, uint32_t* mt_key,
+                                    int32_t* mt_pos, int32_t n_samples, int32_t first, int32_t count,
+                                    int32_t* samples);
+
 BOSS_API int boss_gccb_sample_instances(const double* matrices, int32_t n_matrices, int32_t m,
                                         const int32_t* input_states, int32_t n_samples,
                                         const int32_t* randint_results, const double* uniforms, int32_t stride,

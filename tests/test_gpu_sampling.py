@@ -51,6 +51,28 @@ def test_gccb_fixtures_match_reference_streams():
         assert np.random.random() == rec["next_random"], rec["kind"]
 
 
+def test_stream_slices_reassemble_one_call():
+    """Ranks that each sample a slice of the same stream (boss_gccb_sample_slice)
+    together give exactly one process's samples and numpy state."""
+    from theboss_gb300 import _native
+    from theboss_gb300.distributed import shard
+    from theboss_gb300.utilities import haar_unitary
+
+    U = haar_unitary(24, 8)
+    inp = [1] * 12 + [0] * 12
+    w = [1 / 13] * 13
+    np.random.seed(23)
+    full = _native.gccb_sample(U, inp, w, 301)
+    after = np.random.random()
+    parts = []
+    for r in range(3):
+        np.random.seed(23)
+        first, count = shard(301, r, 3)
+        parts.append(_native.gccb_sample_slice(U, inp, w, 301, first, count))
+        assert np.random.random() == after
+    assert np.array_equal(np.concatenate(parts), full)
+
+
 def test_mode_assignment_gcc_matches_reference_streams():
     """mode_assignment_generalized_cliffords_simulation_strategy.py: seeded streams,
     the last sample's mode order and the generator state theboss leaves."""

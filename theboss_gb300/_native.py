@@ -92,6 +92,9 @@ def load() -> ctypes.CDLL:
         L.boss_bobs_nonuniform_predraw.argtypes = [up, ip, ctypes.c_int32, ctypes.c_int32, ip, ctypes.c_int32,
                                                    ctypes.c_int32, dp, ctypes.c_int32, ctypes.c_int32,
                                                    ctypes.c_int32, ip, dp, ip, dp]
+        L.boss_gccb_sample_slice.restype = ctypes.c_int
+        L.boss_gccb_sample_slice.argtypes = [dp, ctypes.c_int32, ip, dp, ctypes.c_int32, up, ip, ctypes.c_int32,
+                                             ctypes.c_int32, ctypes.c_int32, ip]
         _lib = L
         return L
 
@@ -226,6 +229,24 @@ def count_outcomes(samples, outcomes, m: int) -> np.ndarray:
     out = np.zeros(O.shape[0], dtype=np.int64)
     check(L.boss_count_outcomes(_ip(S), S.shape[0], _ip(O), O.shape[0], m,
                                 out.ctypes.data_as(ctypes.POINTER(ctypes.c_int64))))
+    return out
+
+
+def gccb_sample_slice(U: np.ndarray, input_state, weights, n_samples: int, first: int, count: int) -> np.ndarray:
+    """Samples [first, first + count) of the stream of n_samples C&C-B samples;
+    numpy's global RandomState advances over the whole stream.  int32 (count x m)."""
+    L = load()
+    inp = np.ascontiguousarray(input_state, dtype=np.int32)
+    m = U.shape[0]
+    if len(inp) != m:
+        raise AttributeError("input state length differs from the matrix dimension")
+    w, nw, wp = _weights_arg(weights)
+    st, key, pos = _get_mt()
+    out = np.zeros((max(count, 0), m), dtype=np.int32)
+    check(L.boss_gccb_sample_slice(_dp(U.view(np.float64)), m, _ip(inp), wp, nw,
+                                   key.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32)), _ip(pos), n_samples, first,
+                                   count, _ip(out)))
+    _set_mt(st, key, pos)
     return out
 
 

@@ -917,7 +917,15 @@ int boss_gccb_predraw(const int32_t* input_state, int32_t m, const double* parti
 
 int boss_gccb_sample(const double* matrix, int32_t m, const int32_t* input_state, const double* particle_weights,
                      int32_t n_weights, uint32_t* mt_key, int32_t* mt_pos, int32_t n_samples, int32_t* samples) {
-  if (!matrix || !input_state || !samples || m <= 0 || n_samples < 0) {
+  return boss_gccb_sample_slice(matrix, m, input_state, particle_weights, n_weights, mt_key, mt_pos, n_samples, 0,
+                                n_samples, samples);
+}
+
+int boss_gccb_sample_slice(const double* matrix, int32_t m, const int32_t* input_state,
+                           const double* particle_weights, int32_t n_weights, uint32_t* mt_key, int32_t* mt_pos,
+                           int32_t n_samples, int32_t first, int32_t count, int32_t* samples) {
+  if (!matrix || !input_state || (count > 0 && !samples) || m <= 0 || n_samples < 0 || first < 0 || count < 0 ||
+      (int64_t)first + count > n_samples) {
     set_error("null pointer or bad size");
     return kErrArg;
   }
@@ -932,13 +940,25 @@ int boss_gccb_sample(const double* matrix, int32_t m, const int32_t* input_state
   Draws D;
   st = predraw(input_state, m, particle_weights, particle_weights ? n_weights : 0, mt, n_samples, D);
   if (st) return st;
-  const std::vector<int32_t>& L = D.L;
-  const int n = D.n;
-  if (n > kMaxMinorDigits) {
+  if (D.n > kMaxMinorDigits) {
     set_error("the batched sampler supports at most 32 input particles");
     return kErrLimit;
   }
-  memset(samples, 0, sizeof(int32_t) * (size_t)n_samples * m);
+  if (first != 0 || count != n_samples) {  // keep this slice of the stream's samples
+    const size_t rs = (size_t)std::max(D.n, 1);
+    D.particles.erase(D.particles.begin(), D.particles.begin() + first * rs);
+    D.particles.resize(count * rs);
+    D.nparticles.erase(D.nparticles.begin(), D.nparticles.begin() + first);
+    D.nparticles.resize(count);
+    D.L.erase(D.L.begin(), D.L.begin() + first);
+    D.L.resize(count);
+    D.idx.erase(D.idx.begin(), D.idx.begin() + first * rs);
+    D.idx.resize(count * rs);
+    D.u.erase(D.u.begin(), D.u.begin() + first * rs);
+    D.u.resize(count * rs);
+  }
+  const std::vector<int32_t>& L = D.L;
+  if (count > 0) memset(samples, 0, sizeof(int32_t) * (size_t)count * m);
   const bool any = std::any_of(L.begin(), L.end(), [](int32_t l) { return l > 0; });
   if (any) {
     Context* cx = context(&st);
