@@ -214,6 +214,10 @@ def c2_patterns(n, count, seed):
 
 
 def single_permanents(peak_tflops, seed):
+    """C2: 64 Glynn permanents per size, device-timed; the relative error of the
+    first pattern against the double-double oracle for n <= 24 (its CPU cost grows
+    as 2^n: 7 s at n = 24 on 16 Arm cores, 170 s at n = 28)."""
+    from oracle import oracle as O
     from theboss_gb300 import _native
     from theboss_gb300.utilities import haar_unitary
 
@@ -228,6 +232,10 @@ def single_permanents(peak_tflops, seed):
         tf = b["flops"] / (ms / 1e3) / 1e12
         res[str(n)] = {"perms_per_s": 64 / (ms / 1e3), "ms_per_64": ms, "codes": b["codes"],
                        "achieved_tflops": tf, "frac_of_fp64_peak": tf / peak_tflops}
+        if n <= 24:
+            hi, lo = O.perm_dd(U, S[0], T[0])
+            ref = hi + lo
+            res[str(n)]["rel_err_vs_dd_pattern0"] = float(abs(b["results"][0] - ref) / abs(ref))
     return res
 
 

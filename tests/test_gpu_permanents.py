@@ -69,6 +69,23 @@ def test_single_photon_permanents_against_double_double(calcs, oracle, n):
             assert abs(got - ref) <= tol * abs(ref), (name, n, got, ref, abs(got - ref) / abs(ref))
 
 
+@pytest.mark.parametrize("n,names", [(24, ("glynn", "chin_huh", "ryser"))])
+def test_large_permanents_against_double_double(calcs, oracle, n, names):
+    """One pattern: the double-double oracle's cost grows as 2^n (7 s at n = 24 on
+    16 Arm cores, 170 s at n = 28)."""
+    rng = np.random.default_rng(200 + n)
+    m = 2 * n
+    U = haar(m, n)
+    S = [1] * n + [0] * n
+    T = pattern_with_doubles(m, n, rng)
+    hi, lo = oracle.perm_dd(U, S, T)
+    ref = hi + lo
+    for name in names:
+        got = calcs[name](U, S, T).compute_permanent()
+        tol = 1e-10 if name != "ryser" else 1e-8
+        assert abs(got - ref) <= tol * abs(ref), (name, n, got, ref, abs(got - ref) / abs(ref))
+
+
 def test_edge_cases(calcs):
     U = haar(4, 1)
     z = [0, 0, 0, 0]
