@@ -1,7 +1,7 @@
 /*
  * boss_oracle.c -- TEST INFRASTRUCTURE, NOT PRODUCT CODE.
  *
- * A plain-C restatement of theboss's permanent hot path, used only as the checker
+ * A plain-C restatement of theboss's permanent hot path, used only to check results
  * by tests/, by __graft_entry__.smoke() and by bench.py's CPU baseline leg.  The
  * product (theboss_gb300/) never links, imports or calls anything in this file.
  *

@@ -4,7 +4,7 @@ ctypes front end of the CPU restatement in ``oracle/boss_oracle.c`` plus the
 numpy-level pieces of theboss's samplers that decide *which* random numbers are
 drawn (they must call numpy's global RandomState in exactly the reference's
 order).  Only ``tests/``, ``__graft_entry__.smoke()`` and ``bench.py``'s CPU
-baseline / reference leg use this module, always as the checker or the CPU
+baseline / reference leg use this module, always to check results or as the CPU
 baseline, never as the thing being measured on the GPU.
 
 Reference files followed (paths inside theboss):

@@ -20,7 +20,7 @@ struct SweepLaunch {
   const longlong2* pool = nullptr;
   int64_t total_threads = 0;
   double2* partials = nullptr;
-  double2* partials2 = nullptr;  // gradients: per-thread permanent partials
+  double2* partials2 = nullptr;  // gradients: per-warp permanent partials
   int grid = 1;
 };
 

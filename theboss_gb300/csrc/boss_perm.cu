@@ -129,9 +129,9 @@ __global__ void minors_reduce_kernel(const SweepProblem* __restrict__ probs, con
   }
 }
 
-// One block per gradient sweep: every (digit, factor) entry of the per-thread
-// gradient slices and the per-thread permanents, summed over the sweep's threads
-// in a fixed order.  grad_out row = (nd + fixed) x nf entries.
+// One block per gradient sweep: every (digit, factor) entry of the per-warp
+// gradient partials and the per-warp permanents, summed over the sweep's groups
+// of 32 threads in a fixed order.  grad_out row = (nd + fixed) x nf entries.
 __global__ void grad_reduce_kernel(const SweepProblem* __restrict__ probs, const double2* __restrict__ gpart,
                                    const double2* __restrict__ ppart, double2* __restrict__ grad_out,
                                    double2* __restrict__ perm_out, int row_stride) {

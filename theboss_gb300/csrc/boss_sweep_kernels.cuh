@@ -183,13 +183,16 @@ __global__ void __launch_bounds__(128) minors_sweep_kernel(const SweepProblem* _
 // scale * sum over the copies f of the mode of
 //     G_{b,f} = sum_r sign(r) prod C(mult, r) w_b(r) L_f(r),  L_f = prod_{f' != f} s_f'
 // (the derivative of the Chin-Huh sum; mult_b * copies(f) * minor once summed).
-// Per code the leave-one-out products come from a prefix array in registers and
-// a running suffix, and sign * L_f is added to a running total R_f (shared
-// memory).  w_b only changes when digit b flips, so G is settled at flips:
+// Per code the leave-one-out products come from a prefix array (shared memory)
+// and a running suffix, with the factors converted from the fixed-point sums in
+// each pass, and sign * L_f is added to a running total R_f (shared memory).
+// w_b only changes when digit b flips, so G is settled at flips:
 // G_{b,.} += (w_b(before) - w_b(after)) * R_. , and at the end of each segment
 // G_{b,.} += w_b * R_. for every digit.  A halved (fixed) digit has w = 1.
 // The permanent itself is accumulated alongside (one fused product per code).
-// Per-thread G lives in global scratch: (nd + fixed) x NF complex, row = digit.
+// Per-thread G lives in global scratch: (nd + fixed) x NF complex, row = digit,
+// lane-interleaved within each group of 32 threads; each warp sums its lanes'
+// rows at the end and leaves one group partial.
 template <int NF>
 __global__ void __launch_bounds__(64) grad_sweep_kernel(const SweepProblem* __restrict__ probs, int n_probs,
                                                         const longlong2* __restrict__ pool, int64_t total_threads,
