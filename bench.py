@@ -455,7 +455,12 @@ def run_ours(args, rank, world):
             "roofline": {"bound": "fp64", "kernel": "minors_sweep_kernel (all levels of a step)",
                          "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
                          "traffic": traffic, "peak_source": "boss_fp64_peak, measured in this run",
-                         "sweep_ms_per_step": sweep_s * 1e3, "flops_per_step": b["sweep_flops"]},
+                         "sweep_ms_per_step": sweep_s * 1e3, "flops_per_step": b["sweep_flops"],
+                         "flops_note": "9k - 12 flops per Guan code at level k over the codes the Glynn-form "
+                                       "all-minors sweeps walk (half of theboss's Ryser-form codes for single "
+                                       "photons); ryser_form_* count theboss's codes",
+                         "ryser_form_flops_per_step": b["ref_flops"],
+                         "ryser_form_equivalent_tflops": b["ref_flops"] / sweep_s / 1e12},
             "wall_s_device_section": t_wall}
     if rank == 0 and not args.quick:
         # theboss's per-step loop with the GPU all-minors calculator, bounded sample

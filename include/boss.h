@@ -173,10 +173,12 @@ BOSS_API int boss_gccb_sample(const double* matrix, int32_t m, const int32_t* in
  * times with inputs resident in GPU memory.  Before every run a flush_bytes
  * memset evicts L2.  Per timed run it writes the graph time (step_ms) and the
  * summed time of its all-minors sweep launches (sweep_ms), both from CUDA events
- * on the library stream.  info[0..5] = algorithmic flops of the sweeps per run,
- * H2D bytes and D2H bytes of one boss_gccb_sample call, kernels per run, sweep
- * launches per run, and the deepest level.  samples (optional) receives the last
- * run's samples.  No reference counterpart.
+ * on the library stream.  info[0..6] = flops of the sweeps per run (9k - 12 per
+ * Guan code at level k, over the codes the Glynn-form sweeps walk), H2D bytes and
+ * D2H bytes of one boss_gccb_sample call, kernels per run, sweep launches per
+ * run, the deepest level, and the same flop count over theboss's Ryser-form codes
+ * (twice as many for single photons).  info must hold 8 doubles.  samples
+ * (optional) receives the last run's samples.  No reference counterpart.
  */
 BOSS_API int boss_gccb_bench(const double* matrix, int32_t m, const int32_t* input_state,
                              const double* particle_weights, int32_t n_weights, uint32_t* mt_key, int32_t* mt_pos,

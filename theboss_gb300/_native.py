@@ -421,7 +421,7 @@ def gccb_bench(U: np.ndarray, input_state, weights, n_samples: int, warmup: int,
     _set_mt(st, key, pos)
     return dict(step_ms=step_ms, sweep_ms=sweep_ms, sweep_flops=float(info[0]), h2d_bytes=int(info[1]),
                 d2h_bytes=int(info[2]), kernels=int(info[3]), sweeps=int(info[4]), levels=int(info[5]),
-                samples=samples)
+                ref_flops=float(info[6]), samples=samples)
 
 
 def perm_bench(U: np.ndarray, S: np.ndarray, T: np.ndarray, variant: int, warmup: int, steps: int,

@@ -304,7 +304,7 @@ __global__ void __launch_bounds__(kFinWarps * 32) gccb_finalize_kernel(FinalizeA
     nd = 1;
   } else {
     const SweepProblem& P = a.probs_cur[j];
-    nd = P.nd;
+    nd = P.nd + P.fixed_digit;  // the held (halved) digit's minor is the last row
     const int64_t parts = P.n_threads / P.group;
     if (parts <= 64) {  // lane d sums digit d's partials
       if (lane < nd) {
@@ -336,13 +336,8 @@ __global__ void __launch_bounds__(kFinWarps * 32) gccb_finalize_kernel(FinalizeA
   }
   __syncwarp();
   // Laplace expansion perm(T + e_o) = sum_i S_i sub_i U[o][i]
-  // (generalized_cliffords_b_simulation_strategy.py:82-89), then |.|^2.
-  if (lane < nd) {
-    const double mu = (double)mult_s[w][lane];
-    const double2 sv = sub_s[w][lane];
-    sub_s[w][lane] = make_double2(mu * sv.x, mu * sv.y);
-  }
-  __syncwarp();
+  // (generalized_cliffords_b_simulation_strategy.py:82-89), then |.|^2.  The
+  // Glynn-form sweep already delivers S_i sub_i.
   // FP64 instructions cost the same whatever the number of active lanes, so the
   // outputs that do not fill a warp split their digits over several lanes.
   const int full = m & ~31;
@@ -495,6 +490,24 @@ __global__ void __launch_bounds__(kFinWarps * 32) gccb_finalize_kernel(FinalizeA
   }
   __syncwarp();
   nd = nb + nmul;
+  // Glynn form: hold the last binary digit at r = 0 (halving); it moves to the
+  // end of the digit list, where its minor row is.
+  const int held = (nb > 0) ? 1 : 0;
+  if (held) {
+    const int src = (lane + 1 < nd) ? lane + 1 : nb - 1;  // rotate entries nb-1 .. nd-1 left by one
+    uint8_t dmv = 0, muv = 0;
+    if (lane >= nb - 1 && lane < nd) {
+      dmv = dm_s[w][src];
+      muv = mult_s[w][src];
+    }
+    __syncwarp();
+    if (lane >= nb - 1 && lane < nd) {
+      dm_s[w][lane] = dmv;
+      mult_s[w][lane] = muv;
+    }
+    __syncwarp();
+  }
+  const int nds = nd - held;  // digits of the sweep
   LevelSample ls;
   if (a.next_tab) {
     ls = a.next_tab[j];
@@ -505,32 +518,47 @@ __global__ void __launch_bounds__(kFinWarps * 32) gccb_finalize_kernel(FinalizeA
     ls.part_off = (int64_t)j * a.next_uni.part_off;
     ls.pool_off = (int64_t)j * a.next_uni.pool_off;
   }
+  // rows: -2 U[out][in] for the sweep's digits; base sums: sum_i S_i U[out][i]
+  // over every input mode (all signs +1 at r = 0), exact in fixed point
   longlong2* D = a.pool_next + ls.pool_off;
-  for (int e = lane; e < nd * nf; e += 32) {
+  for (int e = lane; e < nds * nf; e += 32) {
     const int d = e / nf, f = e - d * nf;
-    D[e] = Ufxs[(size_t)fm_s[w][f] * m + dm_s[w][d]];  // Ryser rows: U[out][in]
+    const longlong2 u = Ufxs[(size_t)fm_s[w][f] * m + dm_s[w][d]];
+    D[e] = make_longlong2(-2 * u.x, -2 * u.y);
+  }
+  longlong2* B = D + (size_t)nds * nf;
+  for (int f = lane; f < nf; f += 32) {
+    long long bx = 0, by = 0;
+    for (int d = 0; d < nd; ++d) {
+      const longlong2 u = Ufxs[(size_t)fm_s[w][f] * m + dm_s[w][d]];
+      bx += (long long)mult_s[w][d] * u.x;
+      by += (long long)mult_s[w][d] * u.y;
+    }
+    B[f] = make_longlong2(bx, by);
   }
   SweepProblem& P = a.probs_next[j];
   P.mult[lane] = (lane < nd) ? mult_s[w][lane] : 0;
   P.mult[lane + 32] = 0;
   a.dmode_next[(size_t)j * 32 + lane] = (lane < nd) ? dm_s[w][lane] : 0;
   if (lane == 0) {
-    P.nd = nd;
-    P.nb = nb;
+    // S_i minor_i = 2^-(k-1) (halved) or 2^-k (not) times the Glynn sum, k = nf + 1
+    // input particles; the kernel accumulates half of it.
+    P.nd = nds;
+    P.nb = nb - held;
     P.nf = nf;
-    P.kind = kRyser;
-    P.parity0 = nf & 1;  // multiplier (-1)^sum(T), bs_submatrices_permanent_calculator_base.py:185
+    P.kind = kGlynn;
+    P.parity0 = 0;
     P.fx = a.fx;
-    P.has_base = 0;
+    P.has_base = 1;
     P.out_idx = j;
     P.n_codes = ls.n_codes;
     P.thread_begin = ls.thread_begin;
     P.n_threads = ls.n_threads;
     P.mat_off = ls.pool_off;
-    P.base_off = 0;
+    P.base_off = ls.pool_off + (int64_t)nds * nf;
     P.part_off = ls.part_off;
-    P.scale = 1.0;
-    P.fixed_digit = 0;
+    P.scale = ldexp(1.0, held ? -(nf - 1) : -nf);
+    P.fixed_digit = held;
     P.group = a.next_tab ? 1 : a.next_group;
   }
 }
@@ -545,7 +573,8 @@ struct GccbRun {
   uint8_t* dT = nullptr;
   int* derr = nullptr;
   int kernels = 0, sweeps = 0;
-  double sweep_flops = 0.0;  // algorithmic flops of all sweep launches
+  double sweep_flops = 0.0;  // flops of all sweep launches (the Glynn form's codes)
+  double ref_flops = 0.0;    // the same count over theboss's Ryser-form codes
   std::vector<cudaEvent_t> ev;  // 2 per sweep level when timing
 };
 static cudaGraphExec_t g_gccb_exec = nullptr;
@@ -600,28 +629,34 @@ static int gccb_prepare(Context* cx, const double* matrix, int n_mats, int m, Dr
     lvl_nd[k].resize(A[k]);
   }
   R.sweep_flops = 0.0;
+  R.ref_flops = 0.0;
   {
     std::vector<uint8_t> occ(m, 0);
     for (int jj = 0; jj < A[1]; ++jj) {
       const int s = order[jj];
-      uint64_t c = 1;
-      int nd = 0;
+      uint64_t c = 1;  // prod (S_i + 1): theboss's Guan codes
+      int nd = 0, singles = 0;
       for (int k = 1; k <= L[s]; ++k) {
         if (D.binned) {
           const int md = D.modes[(size_t)s * n + (k - 1)];
           c = c / ((uint64_t)occ[md] + 1) * ((uint64_t)occ[md] + 2);
           if (occ[md] == 0) ++nd;
+          singles += (occ[md] == 0) ? 1 : (occ[md] == 1 ? -1 : 0);
           occ[md]++;
         } else {
           c *= 2;
           ++nd;
+          ++singles;
         }
         if (k >= 2) {
-          lvl_codes[k][jj] = c;
+          const uint64_t cg = singles > 0 ? c / 2 : c;  // Glynn form: one single digit held
+          lvl_codes[k][jj] = cg;
           lvl_nd[k][jj] = nd;
-          // algorithmic flops of theboss's all-minors sweep per code: (k-1) complex
-          // adds, (k-2) complex products, one sign, k/2 real-weighted adds = 9k - 12
-          R.sweep_flops += (double)c * (9.0 * k - 12.0);
+          // flops per code of the all-minors sweep: (k-1) complex adds, (k-2) complex
+          // products, one sign, k/2 real-weighted adds = 9k - 12; theboss's Ryser
+          // form sweeps c codes, the Glynn form cg
+          R.sweep_flops += (double)cg * (9.0 * k - 12.0);
+          R.ref_flops += (double)c * (9.0 * k - 12.0);
         }
       }
       if (D.binned)
@@ -653,10 +688,10 @@ static int gccb_prepare(Context* cx, const double* matrix, int n_mats, int m, Dr
       uni_lvl[k].thread_begin = 0;
       uni_lvl[k].n_threads = tps;
       uni_lvl[k].part_off = tps * ndv[0];
-      uni_lvl[k].pool_off = (int64_t)ndv[0] * (k - 1);
+      uni_lvl[k].pool_off = (int64_t)(ndv[0] + 1) * (k - 1);  // rows and base sums
       lvl_threads[k] = tps * Ak;
       lvl_parts[k] = tps * ndv[0] * Ak;
-      lvl_pool[k] = (int64_t)ndv[0] * (k - 1) * Ak;
+      lvl_pool[k] = (int64_t)(ndv[0] + 1) * (k - 1) * Ak;
       continue;
     }
     std::vector<int64_t> nthr;
@@ -673,7 +708,7 @@ static int gccb_prepare(Context* cx, const double* matrix, int n_mats, int m, Dr
       ls.pool_off = pool;
       threads += nthr[jj];
       parts += nthr[jj] * ndv[jj];
-      pool += (int64_t)ndv[jj] * (k - 1);
+      pool += (int64_t)(ndv[jj] + 1) * (k - 1);
       t[jj] = ls;
     }
     lvl_threads[k] = threads;
@@ -1050,6 +1085,7 @@ int boss_gccb_bench(const double* matrix, int32_t m, const int32_t* input_state,
   if (!st && e != cudaSuccess) st = fail_cuda(e, "bench");
   if (st) return st;
   info[0] = R.sweep_flops;
+  info[6] = R.ref_flops;
   info[1] = (double)R.h2d_bytes;
   info[2] = (double)R.d2h_bytes;
   info[3] = (double)R.kernels;

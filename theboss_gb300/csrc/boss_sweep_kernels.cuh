@@ -82,8 +82,43 @@ __device__ __forceinline__ void settle_minors(const SweepProblem& P, double2* M,
   }
 }
 
-// All-minors sweep (C&C-B).  For a binary digit i the minor receives every code
-// with r_i = 0.  A running signed total R of the products is kept and a minor is
+// Glynn form of the all-minors (kind kGlynn): with an extra row of variables x
+// appended, perm([U[T, S]; x]) = sum_i x_i S_i minor_i, and Glynn's formula for it
+// gives S_i minor_i = scale * sum_r sign(r) prod C(mult, r) w_i(r) prod_f s_f(r),
+// w_i = mult_i - 2 r_i: the same running total R as the Ryser form, but every code
+// counts for every digit with weight w_i, and one binary digit can be held at
+// r = 0 (Glynn's halving) -- half the codes.  The held digit has w = 1 and is row
+// nd.  At a flip of binary digit i, w_i goes +1 -> -1 (or back), so the minor
+// receives (w_before - w_after) R = +-2R.  The kernel accumulates half of every
+// minor (flips add +-R, as in the Ryser form; settles add w R / 2) and the
+// problem's scale carries the factor 2.
+__device__ __forceinline__ void settle_minors_glynn(const SweepProblem& P, double2* M, double Rr, double Ri, double w,
+                                                   uint64_t g, uint64_t t_seg) {
+  const double wr = 0.5 * w * Rr, wi = 0.5 * w * Ri;
+  for (int j = 0; j < P.nb; ++j) {
+    const uint32_t neg = (uint32_t)((g >> j) & 1ull) << 31;
+    double2 v = M[j * 128];
+    v.x += xor_sign(wr, neg);
+    v.y += xor_sign(wi, neg);
+    M[j * 128] = v;
+  }
+  for (int j = P.nb; j < P.nd; ++j) {
+    const double f = (double)P.mult[j] - 2.0 * (double)digit_value(P, t_seg, j);
+    double2 v = M[j * 128];
+    v.x = fma(wr, f, v.x);
+    v.y = fma(wi, f, v.y);
+    M[j * 128] = v;
+  }
+  if (P.fixed_digit) {
+    double2 v = M[P.nd * 128];
+    v.x += wr;
+    v.y += wi;
+    M[P.nd * 128] = v;
+  }
+}
+
+// All-minors sweep (C&C-B).  Ryser form (kind kRyser): for a binary digit i the
+// minor receives every code with r_i = 0.  A running signed total R of the products is kept and a minor is
 // touched only when its digit flips: 0 -> 1 ends a run of r_i = 0 codes
 // (minor += R), 1 -> 0 starts one (minor -= R).  Segments of 2^16 codes (and
 // every change of a multi-valued digit) are closed by settle_minors and R
@@ -98,7 +133,8 @@ __global__ void __launch_bounds__(128) minors_sweep_kernel(const SweepProblem* _
   if (gt >= total_threads) return;
   const SweepProblem& P = probs[find_problem(probs, n_probs, gt)];
   const int64_t q = gt - P.thread_begin;
-  const int nd = P.nd;
+  const bool glynn = (P.kind == kGlynn);
+  const int nd = P.nd + (glynn ? P.fixed_digit : 0);  // minors written per thread
   double2* M = minors_smem + threadIdx.x;
   for (int j = 0; j < nd; ++j) M[j * 128] = make_double2(0.0, 0.0);
   int64_t a, len;
@@ -135,7 +171,8 @@ __global__ void __launch_bounds__(128) minors_sweep_kernel(const SweepProblem* _
         flip_binary<NF>(D, i, bit, sr, si);
         parity ^= 1u;
       } else {
-        settle_minors(P, M, Rr, Ri, w, g, t_seg);
+        if (glynn) settle_minors_glynn(P, M, Rr, Ri, w, g, t_seg);
+        else settle_minors(P, M, Rr, Ri, w, g, t_seg);
         Rr = 0.0;
         Ri = 0.0;
         t_seg = t;
@@ -150,7 +187,8 @@ __global__ void __launch_bounds__(128) minors_sweep_kernel(const SweepProblem* _
       }
       accumulate_product<NF>(sr, si, bias, parity << 31, Rr, Ri);
     }
-    settle_minors(P, M, Rr, Ri, w, g, t_seg);
+    if (glynn) settle_minors_glynn(P, M, Rr, Ri, w, g, t_seg);
+    else settle_minors(P, M, Rr, Ri, w, g, t_seg);
   }
   const int G = P.group;
   if (G > 1) {  // each aligned group of G lanes (one sweep's threads) sums its minors:
