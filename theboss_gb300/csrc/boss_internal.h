@@ -38,7 +38,7 @@ cudaError_t launch_minors_reduce(const SweepProblem* probs, int n_probs, const d
 
 // Splits `n_codes` codes over at most `resident` threads, proportionally, at
 // least one thread per sweep and at least kMinCodesPerThread codes per thread.
-constexpr int64_t kMinCodesPerThread = 32;
+constexpr int64_t kMinCodesPerThread = 8;
 void partition_threads(const std::vector<uint64_t>& n_codes, int64_t resident, std::vector<int64_t>& n_threads);
 
 // ---------------------------------------------------------------------------
