@@ -377,9 +377,10 @@ __global__ void __launch_bounds__(kFinWarps * 32) gccb_finalize_kernel(FinalizeA
   // theboss normalises with Python's sequential sum, and numpy.random.choice then
   // takes cdf = cumsum(p), cdf /= cdf[-1], searchsorted(cdf, u, 'right')
   // (generalized_cliffords_b_simulation_strategy.py:91-92, 107-110).  Fast path:
-  // the same quantities from a warp scan and a reciprocal, whose rounding differs
-  // from the sequential evaluation by far less than 1e-12 relative; whenever some
-  // cdf entry lies within 1e-12 of the uniform the sequential evaluation decides.
+  // the same decisions from a warp scan of the unnormalised pmf compared with
+  // u * total, whose rounding differs from the sequential evaluation by far less
+  // than 1e-12 relative; whenever some cdf entry lies within 1e-12 of the uniform
+  // the sequential evaluation decides.
   const double uu = a.uni[(size_t)j * a.n + (a.k - 1)];
   const int K = (m + 31) >> 5;  // contiguous outputs per lane
   const int o0 = lane * K;
@@ -396,22 +397,24 @@ __global__ void __launch_bounds__(kFinWarps * 32) gccb_finalize_kernel(FinalizeA
   double excl = __shfl_up_sync(0xffffffffu, incl, 1);
   if (lane == 0) excl = 0.0;
   int idx = 0;
-  if (!(total_fast > 0.0) || !isfinite(total_fast)) {
+  const long long tb = __double_as_longlong(total_fast);
+  if (!(tb > 0 && tb < 0x7ff0000000000000ll)) {  // not a positive finite double
     if (lane == 0) atomicOr(a.err, 1);
   } else {
-    const double inv = 1.0 / total_fast;
-    // Every cdf entry and the uniform are non-negative doubles, whose order is that of
-    // their bit patterns as integers: the comparisons run on the integer pipe.  An entry
-    // is "near" when it lies in [u (1 - 1e-12), u (1 + 1e-12)].
-    const long long ub = __double_as_longlong(uu);
-    const long long lo = __double_as_longlong(fma(-1e-12, uu, uu));
-    const long long hi = __double_as_longlong(fma(1e-12, uu, uu));
-    double c = excl * inv;
+    // The comparisons are made on the unnormalised cdf against u * total (no
+    // division).  Every cdf entry and u * total are non-negative doubles, whose
+    // order is that of their bit patterns as integers: the comparisons run on the
+    // integer pipe.  An entry is "near" when it lies in [ut (1 - 1e-12), ut (1 + 1e-12)].
+    const double ut = uu * total_fast;
+    const long long ub = __double_as_longlong(ut);
+    const long long lo = __double_as_longlong(fma(-1e-12, ut, ut));
+    const long long hi = __double_as_longlong(fma(1e-12, ut, ut));
+    double c = excl;
     int cnt = 0;
     bool near = false;
     for (int q = 0; q < K; ++q) {
       if (o0 + q >= m) break;
-      c = fma(pmf_s[w][o0 + q], inv, c);  // ~ cdf / cdf[-1] (the last entry is ~1)
+      c += pmf_s[w][o0 + q];  // ~ cdf * total
       const long long cb = __double_as_longlong(c);
       near |= (o0 + q < m - 1) && cb >= lo && cb <= hi;
       cnt += (cb <= ub) ? 1 : 0;
