@@ -598,21 +598,33 @@ static int gccb_prepare(Context* cx, const double* matrix, int n_mats, int m, Dr
   const int N = (int)D.L.size();
   const int n = std::max(D.n, 1);
   const std::vector<int32_t>& L = D.L;
-  // Single-occupied inputs: every sample at level k sweeps 2^k codes over k digits,
-  // whichever particles it popped.  Binned inputs need the popped modes to plan.
+  // Single-occupied inputs: every sample at level k sweeps 2^(k-1) Glynn-form codes
+  // over k digits, whichever particles it popped.  Binned inputs need the popped
+  // modes to plan.
   if (D.binned && D.modes.empty()) modes_from_draws(D);
   R.N = N;
   R.m = m;
   R.n = n;
-  R.order.resize(N);
-  std::iota(R.order.begin(), R.order.end(), 0);
-  std::stable_sort(R.order.begin(), R.order.end(), [&](int x, int y) { return L[x] > L[y]; });
+  // samples by particle count, descending, stable (a counting sort: L <= 255)
+  int Lmax = 0;
+  std::vector<int> cnt(257, 0);
+  for (int s = 0; s < N; ++s) {
+    cnt[L[s]]++;
+    Lmax = std::max(Lmax, (int)L[s]);
+  }
+  std::vector<int> A(Lmax + 2, 0);  // samples with at least k particles
+  for (int k = Lmax; k >= 1; --k) A[k] = A[k + 1] + cnt[k];
+  {
+    std::vector<int> pos(Lmax + 2, 0);
+    for (int l = Lmax, p = 0; l >= 0; --l) {
+      pos[l] = p;
+      p += cnt[l];
+    }
+    R.order.resize(N);
+    for (int s = 0; s < N; ++s) R.order[pos[L[s]]++] = s;
+  }
   const std::vector<int>& order = R.order;
-  const int Lmax = L[order[0]];
   R.Lmax = Lmax;
-  std::vector<int> A(Lmax + 2, 0);
-  for (int s = 0; s < N; ++s)
-    for (int k = 1; k <= L[s]; ++k) A[k]++;
   // fixed point: |row sum| <= n * max |component of U|
   double umax = 0.0;
   for (size_t i = 0; i < (size_t)2 * m * m * n_mats; ++i) umax = std::max(umax, std::fabs(matrix[i]));
@@ -627,30 +639,29 @@ static int gccb_prepare(Context* cx, const double* matrix, int n_mats, int m, Dr
   // count by (occ_a + 2) / (occ_a + 1).
   std::vector<std::vector<uint64_t>> lvl_codes(Lmax + 2);
   std::vector<std::vector<int>> lvl_nd(Lmax + 2);
-  for (int k = 2; k <= Lmax; ++k) {
-    lvl_codes[k].resize(A[k]);
-    lvl_nd[k].resize(A[k]);
-  }
   R.sweep_flops = 0.0;
   R.ref_flops = 0.0;
-  {
+  if (!D.binned) {
+    for (int k = 2; k <= Lmax; ++k) {
+      R.sweep_flops += (double)A[k] * std::ldexp(9.0 * k - 12.0, k - 1);
+      R.ref_flops += (double)A[k] * std::ldexp(9.0 * k - 12.0, k);
+    }
+  } else {
+    for (int k = 2; k <= Lmax; ++k) {
+      lvl_codes[k].resize(A[k]);
+      lvl_nd[k].resize(A[k]);
+    }
     std::vector<uint8_t> occ(m, 0);
     for (int jj = 0; jj < A[1]; ++jj) {
       const int s = order[jj];
       uint64_t c = 1;  // prod (S_i + 1): theboss's Guan codes
       int nd = 0, singles = 0;
       for (int k = 1; k <= L[s]; ++k) {
-        if (D.binned) {
-          const int md = D.modes[(size_t)s * n + (k - 1)];
-          c = c / ((uint64_t)occ[md] + 1) * ((uint64_t)occ[md] + 2);
-          if (occ[md] == 0) ++nd;
-          singles += (occ[md] == 0) ? 1 : (occ[md] == 1 ? -1 : 0);
-          occ[md]++;
-        } else {
-          c *= 2;
-          ++nd;
-          ++singles;
-        }
+        const int md = D.modes[(size_t)s * n + (k - 1)];
+        c = c / ((uint64_t)occ[md] + 1) * ((uint64_t)occ[md] + 2);
+        if (occ[md] == 0) ++nd;
+        singles += (occ[md] == 0) ? 1 : (occ[md] == 1 ? -1 : 0);
+        occ[md]++;
         if (k >= 2) {
           const uint64_t cg = singles > 0 ? c / 2 : c;  // Glynn form: one single digit held
           lvl_codes[k][jj] = cg;
@@ -662,8 +673,7 @@ static int gccb_prepare(Context* cx, const double* matrix, int n_mats, int m, Dr
           R.ref_flops += (double)c * (9.0 * k - 12.0);
         }
       }
-      if (D.binned)
-        for (int k = 0; k < L[s]; ++k) occ[D.modes[(size_t)s * n + k]] = 0;
+      for (int k = 0; k < L[s]; ++k) occ[D.modes[(size_t)s * n + k]] = 0;
     }
   }
   std::vector<char> uniform(Lmax + 2, 0);
@@ -675,11 +685,17 @@ static int gccb_prepare(Context* cx, const double* matrix, int n_mats, int m, Dr
     const std::vector<int>& ndv = lvl_nd[k];
     const int64_t resident = sweep_resident_threads(k - 1, SweepOp::kMinors, cx->sm_count);
     bool same = true;
-    for (int jj = 1; jj < Ak && same; ++jj) same = (codes[jj] == codes[0] && ndv[jj] == ndv[0]);
+    uint64_t code0 = 1ull << (k - 1);
+    int nd0 = k;
+    if (D.binned) {
+      code0 = codes[0];
+      nd0 = ndv[0];
+      for (int jj = 1; jj < Ak && same; ++jj) same = (codes[jj] == code0 && ndv[jj] == nd0);
+    }
     if (same) {  // one small descriptor instead of a per-sample table
-      const double total = (double)codes[0] * Ak;
+      const double total = (double)code0 * Ak;
       const double want = std::max<double>(Ak, std::min<double>((double)resident, total / kMinCodesPerThread));
-      int64_t tps = std::max<int64_t>(1, std::min<int64_t>((int64_t)codes[0], (int64_t)(want / Ak)));
+      int64_t tps = std::max<int64_t>(1, std::min<int64_t>((int64_t)code0, (int64_t)(want / Ak)));
       // Each aligned group of G threads of a sample sums its minors inside the sweep:
       // the largest G (up to a warp) that costs at most 2% of the sample's threads.
       int G = 32;
@@ -687,14 +703,14 @@ static int gccb_prepare(Context* cx, const double* matrix, int n_mats, int m, Dr
       tps = tps / G * G;
       grp[k] = G;
       uniform[k] = 1;
-      uni_lvl[k].n_codes = (int64_t)codes[0];
+      uni_lvl[k].n_codes = (int64_t)code0;
       uni_lvl[k].thread_begin = 0;
       uni_lvl[k].n_threads = tps;
-      uni_lvl[k].part_off = tps * ndv[0];
-      uni_lvl[k].pool_off = (int64_t)(ndv[0] + 1) * (k - 1);  // rows and base sums
+      uni_lvl[k].part_off = tps * nd0;
+      uni_lvl[k].pool_off = (int64_t)(nd0 + 1) * (k - 1);  // rows and base sums
       lvl_threads[k] = tps * Ak;
-      lvl_parts[k] = tps * ndv[0] * Ak;
-      lvl_pool[k] = (int64_t)(ndv[0] + 1) * (k - 1) * Ak;
+      lvl_parts[k] = tps * nd0 * Ak;
+      lvl_pool[k] = (int64_t)(nd0 + 1) * (k - 1) * Ak;
       continue;
     }
     std::vector<int64_t> nthr;
