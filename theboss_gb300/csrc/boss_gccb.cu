@@ -37,8 +37,19 @@ extern std::mutex g_api_mutex;
 // ---------------------------------------------------------------------------
 struct MT19937 {
   uint32_t key[624];
+  uint32_t out[624];  // the tempered outputs of key (the next 624 - pos draws)
   int pos;
 
+  void temper_all() {  // one vectorisable pass per block instead of per draw
+    for (int j = 0; j < 624; ++j) {
+      uint32_t y = key[j];
+      y ^= y >> 11;
+      y ^= (y << 7) & 0x9d2c5680u;
+      y ^= (y << 15) & 0xefc60000u;
+      y ^= y >> 18;
+      out[j] = y;
+    }
+  }
   void twist() {
     const uint32_t upper = 0x80000000u, lower = 0x7fffffffu, a = 0x9908b0dfu;
     int i = 0;
@@ -52,16 +63,12 @@ struct MT19937 {
     }
     const uint32_t y = (key[623] & upper) | (key[0] & lower);
     key[623] = key[396] ^ (y >> 1) ^ ((0u - (y & 1u)) & a);
+    temper_all();
     pos = 0;
   }
   inline uint32_t next32() {
     if (pos >= 624) twist();
-    uint32_t y = key[pos++];
-    y ^= y >> 11;
-    y ^= (y << 7) & 0x9d2c5680u;
-    y ^= (y << 15) & 0xefc60000u;
-    y ^= y >> 18;
-    return y;
+    return out[pos++];
   }
   // 53-bit uniform in [0, 1): numpy.random.random / random_sample.
   inline double next_double() {
@@ -936,6 +943,7 @@ static int load_mt(MT19937& mt, const uint32_t* key, const int32_t* pos) {
   }
   memcpy(mt.key, key, sizeof(mt.key));
   mt.pos = *pos;
+  if (mt.pos < 624) mt.temper_all();
   return kOk;
 }
 
