@@ -73,6 +73,29 @@ def test_stream_slices_reassemble_one_call():
     assert np.array_equal(np.concatenate(parts), full)
 
 
+def test_pipelined_halves_equal_single_batches():
+    """A call of >= 4096 samples runs as two pipelined halves; its samples equal
+    the same stream sampled slice by slice in single batches."""
+    from theboss_gb300 import _native
+    from theboss_gb300.utilities import haar_unitary
+
+    U = haar_unitary(20, 9)
+    inp = [1] * 10 + [0] * 10
+    w = [1 / 11] * 11
+    N = 5001
+    np.random.seed(31)
+    full = _native.gccb_sample(U, inp, w, N)
+    after = np.random.random()
+    parts = []
+    for first, count in ((0, 2000), (2000, 2000), (4000, 1001)):
+        np.random.seed(31)
+        parts.append(_native.gccb_sample_slice(U, inp, w, N, first, count))
+    assert np.random.random() == after
+    assert np.array_equal(np.concatenate(parts), full)
+    np.random.seed(31)
+    assert np.array_equal(_native.gccb_sample_slice(U, inp, w, N, 700, 4300), full[700:5000])
+
+
 def test_mode_assignment_gcc_matches_reference_streams():
     """mode_assignment_generalized_cliffords_simulation_strategy.py: seeded streams,
     the last sample's mode order and the generator state theboss leaves."""

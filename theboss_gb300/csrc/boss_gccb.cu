@@ -578,6 +578,7 @@ __global__ void __launch_bounds__(kFinWarps * 32) gccb_finalize_kernel(FinalizeA
 // ---------------------------------------------------------------------------
 struct GccbRun {
   int N = 0, m = 0, n = 0, Lmax = 0;
+  int slot = 0;  // which set of device buffers, pinned buffer and graph
   std::vector<int> order;
   size_t h2d_bytes = 0, d2h_bytes = 0;
   uint8_t* dT = nullptr;
@@ -587,7 +588,26 @@ struct GccbRun {
   double ref_flops = 0.0;    // the same count over theboss's Ryser-form codes
   std::vector<cudaEvent_t> ev;  // 2 per sweep level when timing
 };
-static cudaGraphExec_t g_gccb_exec = nullptr;
+// Two independent slots (device buffers cx->gccb[8 slot .. 8 slot + 7], a pinned
+// staging buffer and a graph each): the host can plan one batch while the GPU
+// runs the other.
+constexpr int kGccbSlots = 2;
+constexpr int kGccbPipelineMin = 4096;  // samples from which a call runs as two pipelined halves
+static cudaGraphExec_t g_gccb_exec[kGccbSlots] = {nullptr, nullptr};
+static void* g_gccb_pinned[kGccbSlots] = {nullptr, nullptr};
+static size_t g_gccb_pinned_bytes[kGccbSlots] = {0, 0};
+
+static int ensure_slot_pinned(int slot, size_t bytes) {
+  if (g_gccb_pinned_bytes[slot] >= bytes) return kOk;
+  if (g_gccb_pinned[slot]) cudaFreeHost(g_gccb_pinned[slot]);
+  g_gccb_pinned[slot] = nullptr;
+  g_gccb_pinned_bytes[slot] = 0;
+  const size_t cap = std::max(bytes, (size_t)1 << 20);
+  cudaError_t e = cudaHostAlloc(&g_gccb_pinned[slot], cap, cudaHostAllocDefault);
+  if (e != cudaSuccess) return fail_cuda(e, "pinned sampler buffer");
+  g_gccb_pinned_bytes[slot] = cap;
+  return kOk;
+}
 
 static void destroy_events(GccbRun& R) {
   for (auto e : R.ev) cudaEventDestroy(e);
@@ -601,8 +621,11 @@ __global__ void to_fixed_kernel(const double* __restrict__ x, long long* __restr
 
 // matrices: n_mats complex m x m matrices, U[out][in]; one for every sample
 // (n_mats == 1) or one per sample (n_mats == number of samples).
-static int gccb_prepare(Context* cx, const double* matrix, int n_mats, int m, Draws& D, bool timing, GccbRun& R) {
+static int gccb_prepare(Context* cx, const double* matrix, int n_mats, int m, Draws& D, bool timing, GccbRun& R,
+                        int slot = 0) {
   const int N = (int)D.L.size();
+  R.slot = slot;
+  DeviceBuffer* B = cx->gccb + 8 * slot;
   const int n = std::max(D.n, 1);
   const std::vector<int32_t>& L = D.L;
   // Single-occupied inputs: every sample at level k sweeps 2^(k-1) Glynn-form codes
@@ -761,16 +784,16 @@ static int gccb_prepare(Context* cx, const double* matrix, int n_mats, int m, Dr
   R.h2d_bytes = arena;
   R.d2h_bytes = (size_t)N * m + sizeof(int);
   int st;
-  if ((st = ensure(cx->gccb[0], arena))) return st;
-  if ((st = ensure(cx->gccb[1], (size_t)N * m * 2))) return st;                              // S | T
-  if ((st = ensure(cx->gccb[2], sizeof(SweepProblem) * (size_t)A[1] * 2 + 512))) return st;  // problems x2
-  if ((st = ensure(cx->gccb[3], (size_t)A[1] * 32 * 2))) return st;                          // digit modes x2
-  if ((st = ensure(cx->gccb[4], sizeof(longlong2) * (size_t)max_pool * 2 + 512))) return st;  // rows x2
-  if ((st = ensure(cx->gccb[5], sizeof(double2) * (size_t)max_parts))) return st;            // partials
-  if ((st = ensure(cx->gccb[6], sizeof(uint32_t) * 8 * (size_t)N))) return st;                // particles left
-  if ((st = ensure(cx->gccb[7], sizeof(longlong2) * (size_t)m * m * n_mats))) return st;      // U fixed point
-  if ((st = ensure_pinned(cx, std::max(arena, al((size_t)N * m) + 256)))) return st;
-  char* h = (char*)cx->pinned;
+  if ((st = ensure(B[0], arena))) return st;
+  if ((st = ensure(B[1], (size_t)N * m * 2))) return st;                              // S | T
+  if ((st = ensure(B[2], sizeof(SweepProblem) * (size_t)A[1] * 2 + 512))) return st;  // problems x2
+  if ((st = ensure(B[3], (size_t)A[1] * 32 * 2))) return st;                          // digit modes x2
+  if ((st = ensure(B[4], sizeof(longlong2) * (size_t)max_pool * 2 + 512))) return st;  // rows x2
+  if ((st = ensure(B[5], sizeof(double2) * (size_t)max_parts))) return st;            // partials
+  if ((st = ensure(B[6], sizeof(uint32_t) * 8 * (size_t)N))) return st;                // particles left
+  if ((st = ensure(B[7], sizeof(longlong2) * (size_t)m * m * n_mats))) return st;      // U fixed point
+  if ((st = ensure_slot_pinned(slot, std::max(arena, al((size_t)N * m) + 256)))) return st;
+  char* h = (char*)g_gccb_pinned[slot];
   memset(h, 0, o_idx);
   for (int k = 2; k <= Lmax; ++k) memcpy(h + o_tab[k], tab[k].data(), sizeof(LevelSample) * tab[k].size());
   uint8_t* hidx = (uint8_t*)(h + o_idx);
@@ -787,18 +810,18 @@ static int gccb_prepare(Context* cx, const double* matrix, int n_mats, int m, Dr
     if (n_mats > 1) memcpy(h + o_U + sizeof(double2) * mm * jj, matrix + 2 * mm * s, sizeof(double2) * mm);
   }
   if (n_mats == 1) memcpy(h + o_U, matrix, sizeof(double2) * mm);
-  char* d = (char*)cx->gccb[0].ptr;
-  uint8_t* dS = (uint8_t*)cx->gccb[1].ptr;
+  char* d = (char*)B[0].ptr;
+  uint8_t* dS = (uint8_t*)B[1].ptr;
   R.dT = dS + (size_t)N * m;
   R.derr = (int*)(d + o_err);
-  SweepProblem* probs[2] = {(SweepProblem*)cx->gccb[2].ptr, (SweepProblem*)cx->gccb[2].ptr + A[1]};
-  uint8_t* dmode[2] = {(uint8_t*)cx->gccb[3].ptr, (uint8_t*)cx->gccb[3].ptr + (size_t)A[1] * 32};
-  longlong2* pool[2] = {(longlong2*)cx->gccb[4].ptr, (longlong2*)cx->gccb[4].ptr + max_pool};
-  double2* partials = (double2*)cx->gccb[5].ptr;
+  SweepProblem* probs[2] = {(SweepProblem*)B[2].ptr, (SweepProblem*)B[2].ptr + A[1]};
+  uint8_t* dmode[2] = {(uint8_t*)B[3].ptr, (uint8_t*)B[3].ptr + (size_t)A[1] * 32};
+  longlong2* pool[2] = {(longlong2*)B[4].ptr, (longlong2*)B[4].ptr + max_pool};
+  double2* partials = (double2*)B[5].ptr;
   cudaStream_t s = cx->stream;
   cudaError_t e = cudaMemcpyAsync(d, h, arena, cudaMemcpyHostToDevice, s);
   if (e != cudaSuccess) return fail_cuda(e, "H2D sampler arena");
-  longlong2* dUfx = (longlong2*)cx->gccb[7].ptr;
+  longlong2* dUfx = (longlong2*)B[7].ptr;
   {
     const int64_t cnt = (int64_t)2 * mm * n_mats;
     to_fixed_kernel<<<(unsigned)((cnt + 255) / 256), 256, 0, s>>>((const double*)(d + o_U), (long long*)dUfx, cnt, fx);
@@ -850,7 +873,7 @@ static int gccb_prepare(Context* cx, const double* matrix, int n_mats, int m, Dr
     fa.T = R.dT;
     fa.idx = (const uint8_t*)(d + o_idx);
     fa.pmode = (const uint8_t*)(d + o_pm);
-    fa.rem = (uint32_t*)cx->gccb[6].ptr;
+    fa.rem = (uint32_t*)B[6].ptr;
     fa.uni = (const double*)(d + o_uni);
     fa.probs_cur = probs[cur];
     fa.dmode_cur = dmode[cur];
@@ -873,21 +896,22 @@ static int gccb_prepare(Context* cx, const double* matrix, int n_mats, int m, Dr
   }
   if (e != cudaSuccess) return fail_cuda(e, "end capture");
   bool updated = false;
-  if (g_gccb_exec) {
+  cudaGraphExec_t& exec = g_gccb_exec[slot];
+  if (exec) {
     cudaGraphExecUpdateResultInfo info;
-    if (cudaGraphExecUpdate(g_gccb_exec, graph, &info) == cudaSuccess) {
+    if (cudaGraphExecUpdate(exec, graph, &info) == cudaSuccess) {
       updated = true;
     } else {
       cudaGetLastError();
-      cudaGraphExecDestroy(g_gccb_exec);
-      g_gccb_exec = nullptr;
+      cudaGraphExecDestroy(exec);
+      exec = nullptr;
     }
   }
   if (!updated) {
-    e = cudaGraphInstantiate(&g_gccb_exec, graph, 0);
+    e = cudaGraphInstantiate(&exec, graph, 0);
     if (e != cudaSuccess) {
       cudaGraphDestroy(graph);
-      g_gccb_exec = nullptr;
+      exec = nullptr;
       return fail_cuda(e, "graph instantiate");
     }
   }
@@ -895,32 +919,45 @@ static int gccb_prepare(Context* cx, const double* matrix, int n_mats, int m, Dr
   return kOk;
 }
 
-static int gccb_launch(Context* cx) {
-  cudaError_t e = cudaGraphLaunch(g_gccb_exec, cx->stream);
+static int gccb_launch(Context* cx, int slot = 0) {
+  cudaError_t e = cudaGraphLaunch(g_gccb_exec[slot], cx->stream);
   return e == cudaSuccess ? kOk : fail_cuda(e, "graph launch");
 }
 
-static int gccb_collect(Context* cx, GccbRun& R, int32_t* samples_out) {
+// Queues the copies of a run's samples and status into its slot's pinned buffer.
+static int gccb_queue_results(Context* cx, GccbRun& R) {
   cudaStream_t s = cx->stream;
-  cudaError_t e = cudaMemcpyAsync(cx->pinned, R.dT, (size_t)R.N * R.m, cudaMemcpyDeviceToHost, s);
+  char* h = (char*)g_gccb_pinned[R.slot];
+  cudaError_t e = cudaMemcpyAsync(h, R.dT, (size_t)R.N * R.m, cudaMemcpyDeviceToHost, s);
   if (e != cudaSuccess) return fail_cuda(e, "D2H samples");
-  int* herr = (int*)((char*)cx->pinned + (((size_t)R.N * R.m + 255) & ~(size_t)255));
+  int* herr = (int*)(h + (((size_t)R.N * R.m + 255) & ~(size_t)255));
   e = cudaMemcpyAsync(herr, R.derr, sizeof(int), cudaMemcpyDeviceToHost, s);
-  if (e != cudaSuccess) return fail_cuda(e, "D2H status");
-  e = cudaStreamSynchronize(s);
-  if (e != cudaSuccess) return fail_cuda(e, "sampler");
-  if (*herr) {
+  return e == cudaSuccess ? kOk : fail_cuda(e, "D2H status");
+}
+
+// After the stream is synchronised: the status, then the samples in input order.
+static int gccb_read_results(const GccbRun& R, int32_t* samples_out) {
+  const char* h = (const char*)g_gccb_pinned[R.slot];
+  if (*(const int*)(h + (((size_t)R.N * R.m + 255) & ~(size_t)255))) {
     set_error("probabilities contain NaN (a pmf summed to zero or a non-finite value)");
     return kErrPmf;
   }
   if (samples_out) {
-    const uint8_t* hT = (const uint8_t*)cx->pinned;
+    const uint8_t* hT = (const uint8_t*)h;
     for (int jj = 0; jj < R.N; ++jj) {
       int32_t* row = samples_out + (size_t)R.order[jj] * R.m;
       for (int i = 0; i < R.m; ++i) row[i] = hT[(size_t)jj * R.m + i];
     }
   }
   return kOk;
+}
+
+static int gccb_collect(Context* cx, GccbRun& R, int32_t* samples_out) {
+  int st = gccb_queue_results(cx, R);
+  if (st) return st;
+  cudaError_t e = cudaStreamSynchronize(cx->stream);
+  if (e != cudaSuccess) return fail_cuda(e, "sampler");
+  return gccb_read_results(R, samples_out);
 }
 
 static int run_gccb(Context* cx, const double* matrix, int n_mats, int m, Draws& D, int32_t* samples_out) {
@@ -930,6 +967,22 @@ static int run_gccb(Context* cx, const double* matrix, int n_mats, int m, Draws&
   if (st) return st;
   if ((st = gccb_launch(cx))) return st;
   return gccb_collect(cx, R, samples_out);
+}
+
+// Keeps samples [first, first + count) of a replayed batch.
+static void keep_rows(Draws& D, int first, int count) {
+  const size_t rs = (size_t)std::max(D.n, 1);
+  D.particles.erase(D.particles.begin(), D.particles.begin() + first * rs);
+  D.particles.resize(count * rs);
+  D.nparticles.erase(D.nparticles.begin(), D.nparticles.begin() + first);
+  D.nparticles.resize(count);
+  D.L.erase(D.L.begin(), D.L.begin() + first);
+  D.L.resize(count);
+  D.idx.erase(D.idx.begin(), D.idx.begin() + first * rs);
+  D.idx.resize(count * rs);
+  D.u.erase(D.u.begin(), D.u.begin() + first * rs);
+  D.u.resize(count * rs);
+  D.modes.clear();
 }
 
 }  // namespace boss
@@ -999,34 +1052,42 @@ int boss_gccb_sample_slice(const double* matrix, int32_t m, const int32_t* input
   MT19937 mt;
   int st = load_mt(mt, mt_key, mt_pos);
   if (st) return st;
-  Draws D;
-  st = predraw(input_state, m, particle_weights, particle_weights ? n_weights : 0, mt, n_samples, D);
-  if (st) return st;
-  if (D.n > kMaxMinorDigits) {
-    set_error("the batched sampler supports at most 32 input particles");
-    return kErrLimit;
-  }
-  if (first != 0 || count != n_samples) {  // keep this slice of the stream's samples
-    const size_t rs = (size_t)std::max(D.n, 1);
-    D.particles.erase(D.particles.begin(), D.particles.begin() + first * rs);
-    D.particles.resize(count * rs);
-    D.nparticles.erase(D.nparticles.begin(), D.nparticles.begin() + first);
-    D.nparticles.resize(count);
-    D.L.erase(D.L.begin(), D.L.begin() + first);
-    D.L.resize(count);
-    D.idx.erase(D.idx.begin(), D.idx.begin() + first * rs);
-    D.idx.resize(count * rs);
-    D.u.erase(D.u.begin(), D.u.begin() + first * rs);
-    D.u.resize(count * rs);
-  }
-  const std::vector<int32_t>& L = D.L;
+  const int nw = particle_weights ? n_weights : 0;
   if (count > 0) memset(samples, 0, sizeof(int32_t) * (size_t)count * m);
-  const bool any = std::any_of(L.begin(), L.end(), [](int32_t l) { return l > 0; });
-  if (any) {
-    Context* cx = context(&st);
-    if (!cx) return st;
-    st = run_gccb(cx, matrix, 1, m, D, samples);
+  // Large batches run as two parts: the host replays and plans the second part
+  // while the GPU samples the first (separate buffers, pinned memory and graphs).
+  // The first part is a third, so that the GPU starts early and the host's work
+  // on the rest still ends before the GPU finishes the first part.
+  const int halves = (count >= kGccbPipelineMin) ? 2 : 1;
+  const int c0 = (halves == 2) ? count / 3 : count;
+  const int cut[3] = {first, first + c0, first + count};
+  GccbRun R[2];
+  bool launched[2] = {false, false};
+  Context* cx = nullptr;
+  int done = 0;  // stream samples replayed so far
+  for (int h = 0; h < halves; ++h) {
+    Draws D;
+    const int upto = (h + 1 == halves) ? n_samples : cut[h + 1];  // the last half replays the stream's tail
+    st = predraw(input_state, m, particle_weights, nw, mt, upto - done, D);
     if (st) return st;
+    if (D.n > kMaxMinorDigits) {
+      set_error("the batched sampler supports at most 32 input particles");
+      return kErrLimit;
+    }
+    keep_rows(D, cut[h] - done, cut[h + 1] - cut[h]);
+    done = upto;
+    if (!std::any_of(D.L.begin(), D.L.end(), [](int32_t l) { return l > 0; })) continue;
+    if (!cx && !(cx = context(&st))) return st;
+    if ((st = gccb_prepare(cx, matrix, 1, m, D, false, R[h], h))) return st;
+    if ((st = gccb_launch(cx, h))) return st;
+    if ((st = gccb_queue_results(cx, R[h]))) return st;
+    launched[h] = true;
+  }
+  if (cx) {
+    cudaError_t e = cudaStreamSynchronize(cx->stream);
+    if (e != cudaSuccess) return fail_cuda(e, "sampler");
+    for (int h = 0; h < halves; ++h)
+      if (launched[h] && (st = gccb_read_results(R[h], samples + (size_t)(cut[h] - first) * m))) return st;
   }
   memcpy(mt_key, mt.key, sizeof(mt.key));
   *mt_pos = mt.pos;
