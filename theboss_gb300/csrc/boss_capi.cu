@@ -131,9 +131,10 @@ static int sweeps_prepare(Context* cx, const std::vector<HostSweep>& sweeps, boo
     pool_n += (int64_t)h.base.size();
     P.part_off = parts;
     P.scale = h.scale;
+    P.fixed_digit = (h.fixed_mode >= 0) ? 1 : 0;
     for (int i = 0; i < h.nd; ++i) P.mult[i] = h.mult[i];
     threads += nthr[p];
-    parts += nthr[p] * (minors ? h.nd : 1);
+    parts += nthr[p] * (minors ? h.nd + (h.kind == kGlynn ? P.fixed_digit : 0) : 1);
   }
   // arena: problems | pool
   size_t off = 0;
@@ -449,10 +450,13 @@ static int plan_minors(const double* U, int m, const int32_t* S, const int32_t* 
     }
     return kOk;
   }
+  // Glynn form: the coefficients of an appended row of variables (every S_i minor_i
+  // from one sweep, one single-occupied digit held at r = 0); the kernel
+  // accumulates half of each, hence the factor 2.
   auto entry = [&](int i_mode, int j_mode) { return U_at(U, m, j_mode, i_mode); };
-  const int st = fill_sweep(hs, in, out, kRyser, false, entry);
+  const int st = fill_sweep(hs, in, out, kGlynn, true, entry);
   if (st) return st;
-  hs.parity0 = out.n & 1;  // multiplier (-1)^sum(T), bs_submatrices_permanent_calculator_base.py:185
+  hs.scale *= 2.0;
   needs_sweep = true;
   return kOk;
 }
@@ -571,7 +575,11 @@ int boss_submatrices_batch(const double* matrix, int32_t m, const int32_t* input
     for (size_t a = 0; a < by_nf[nf].size(); ++a) {
       const HostSweep& hs = by_nf[nf][a];
       double2* row = res + (size_t)which[nf][a] * len;
-      for (int d = 0; d < hs.nd; ++d) row[hs.digit_mode[d]] = out[a * nd_max + d];
+      for (int d = 0; d < hs.nd; ++d) {  // the sweep gives S_i minor_i
+        const double2 v = out[a * nd_max + d];
+        row[hs.digit_mode[d]] = make_double2(v.x / hs.mult[d], v.y / hs.mult[d]);
+      }
+      if (hs.fixed_mode >= 0) row[hs.fixed_mode] = out[a * nd_max + hs.nd];  // the held digit (S_i = 1)
     }
   }
   return kOk;
