@@ -134,7 +134,7 @@ static int sweeps_prepare(Context* cx, const std::vector<HostSweep>& sweeps, boo
     P.fixed_digit = (h.fixed_mode >= 0) ? 1 : 0;
     for (int i = 0; i < h.nd; ++i) P.mult[i] = h.mult[i];
     threads += nthr[p];
-    parts += nthr[p] * (minors ? h.nd + (h.kind == kGlynn ? P.fixed_digit : 0) : 1);
+    parts += nthr[p] * (minors ? h.nd + P.fixed_digit : 1);
   }
   // arena: problems | pool
   size_t off = 0;

@@ -106,7 +106,7 @@ __global__ void minors_reduce_kernel(const SweepProblem* __restrict__ probs, con
                                      double2* __restrict__ out, int nd_max) {
   __shared__ double sr[256], si[256];
   const SweepProblem& P = probs[blockIdx.x];
-  const int nd = P.nd + (P.kind == kGlynn ? P.fixed_digit : 0);  // Glynn form: the held digit's row last
+  const int nd = P.nd + P.fixed_digit;  // the held digit's row last
   for (int j = 0; j < nd; ++j) {
     double ar = 0.0, ai = 0.0;
     for (int64_t q = threadIdx.x; q < P.n_threads; q += blockDim.x) {

@@ -60,9 +60,9 @@ struct SweepProblem {
   int64_t n_threads;     // threads working on it
   int64_t mat_off;   // D: nd x nf fixed-point complex (longlong2), row-major
   int64_t base_off;  // nf fixed-point complex
-  int64_t part_off;  // partials: n_threads complex (perms) or n_threads x nd (all-minors)
+  int64_t part_off;  // partials: n_threads complex (perms) or n_threads x (nd + fixed_digit) (all-minors)
   double scale;      // final real scale
-  int32_t fixed_digit;  // gradients: a binary digit held at r = 0 (Glynn halving) adds one weight-1 column
+  int32_t fixed_digit;  // gradients, all-minors: a binary digit held at r = 0 (Glynn halving) adds a weight-1 row
   int32_t group;     // all-minors: each aligned group of `group` threads (1, 2, 4, .., 32) sums its
                      // minors, so the partials are (n_threads / group) x nd; n_threads and
                      // thread_begin are multiples of it, and every sweep of the launch has the same

@@ -53,46 +53,10 @@ __global__ void __launch_bounds__(128) perm_sweep_kernel(const SweepProblem* __r
   partials[P.part_off + q] = make_double2(tr, ti);
 }
 
-// Closes the current segment of an all-minors sweep: every digit whose value is
-// constant over the segment receives R times its weight
-// (S_j - r_j) / S_j * prod C(S_l, r_l)
-// (bs_cc_ryser_submatrices_permanent_calculator.py:96-119); binary digits get R
-// when r_j = 0, which also closes the run the flip bookkeeping left open.
+// Closes the current segment of an all-minors sweep: every digit receives R
+// times its weight w_j = mult_j - 2 r_j (binary digits: +-1) times prod C(mult, r),
+// the held digit (row nd) R times 1 -- halved, see minors_sweep_kernel.
 __device__ __forceinline__ void settle_minors(const SweepProblem& P, double2* M, double Rr, double Ri, double w,
-                                             uint64_t g, uint64_t t_seg) {
-  const double wr = w * Rr, wi = w * Ri;
-  for (int j = 0; j < P.nb; ++j) {
-    if (((g >> j) & 1ull) == 0ull) {
-      double2 v = M[j * 128];
-      v.x += wr;
-      v.y += wi;
-      M[j * 128] = v;
-    }
-  }
-  for (int j = P.nb; j < P.nd; ++j) {
-    const uint32_t r = digit_value(P, t_seg, j);
-    const uint32_t mu = P.mult[j];
-    if (r < mu) {
-      const double f = (double)(mu - r) / (double)mu;
-      double2 v = M[j * 128];
-      v.x = fma(wr, f, v.x);
-      v.y = fma(wi, f, v.y);
-      M[j * 128] = v;
-    }
-  }
-}
-
-// Glynn form of the all-minors (kind kGlynn): with an extra row of variables x
-// appended, perm([U[T, S]; x]) = sum_i x_i S_i minor_i, and Glynn's formula for it
-// gives S_i minor_i = scale * sum_r sign(r) prod C(mult, r) w_i(r) prod_f s_f(r),
-// w_i = mult_i - 2 r_i: the same running total R as the Ryser form, but every code
-// counts for every digit with weight w_i, and one binary digit can be held at
-// r = 0 (Glynn's halving) -- half the codes.  The held digit has w = 1 and is row
-// nd.  At a flip of binary digit i, w_i goes +1 -> -1 (or back), so the minor
-// receives (w_before - w_after) R = +-2R.  The kernel accumulates half of every
-// minor (flips add +-R, as in the Ryser form; settles add w R / 2) and the
-// problem's scale carries the factor 2.
-__device__ __forceinline__ void settle_minors_glynn(const SweepProblem& P, double2* M, double Rr, double Ri, double w,
                                                    uint64_t g, uint64_t t_seg) {
   const double wr = 0.5 * w * Rr, wi = 0.5 * w * Ri;
   for (int j = 0; j < P.nb; ++j) {
@@ -117,12 +81,20 @@ __device__ __forceinline__ void settle_minors_glynn(const SweepProblem& P, doubl
   }
 }
 
-// All-minors sweep (C&C-B).  Ryser form (kind kRyser): for a binary digit i the
-// minor receives every code with r_i = 0.  A running signed total R of the products is kept and a minor is
-// touched only when its digit flips: 0 -> 1 ends a run of r_i = 0 codes
-// (minor += R), 1 -> 0 starts one (minor -= R).  Segments of 2^16 codes (and
-// every change of a multi-valued digit) are closed by settle_minors and R
-// restarts from zero.  Per-thread minors live in shared memory (digit-major,
+// All-minors sweep (C&C-B), in Glynn form.  theboss sums each minor over the
+// Ryser codes with r_i = 0 (bs_cc_ryser_submatrices_permanent_calculator.py:96-119).
+// Here a row of variables x is appended: perm([U[T, S]; x]) = sum_i x_i S_i minor_i,
+// and Glynn's formula for it gives
+//     S_i minor_i = scale * sum_r sign(r) prod C(mult, r) w_i(r) prod_f s_f(r),
+// w_i = mult_i - 2 r_i (s_f from the base sums with rows -2U): every code counts
+// for every digit, and one single-occupied digit is held at r = 0 (Glynn's
+// halving; its row has w = 1 and comes last) -- half of theboss's codes.  A
+// running signed total R of the products is kept and a minor is touched only
+// when its digit flips: w_i goes +1 -> -1 (or back), so the minor receives
+// (w_before - w_after) R = +-2R.  The kernel accumulates half of every minor
+// (flips add +-R, settles w R / 2); the problem's scale carries the factor 2.
+// Segments of 2^16 codes (and every change of a multi-valued digit) are closed
+// by settle_minors and R restarts from zero.  Per-thread minors live in shared memory (digit-major,
 // 128-thread stride); every thread writes nd complex partials.
 template <int NF>
 __global__ void __launch_bounds__(128) minors_sweep_kernel(const SweepProblem* __restrict__ probs, int n_probs,
@@ -133,8 +105,7 @@ __global__ void __launch_bounds__(128) minors_sweep_kernel(const SweepProblem* _
   if (gt >= total_threads) return;
   const SweepProblem& P = probs[find_problem(probs, n_probs, gt)];
   const int64_t q = gt - P.thread_begin;
-  const bool glynn = (P.kind == kGlynn);
-  const int nd = P.nd + (glynn ? P.fixed_digit : 0);  // minors written per thread
+  const int nd = P.nd + P.fixed_digit;  // minors written per thread
   double2* M = minors_smem + threadIdx.x;
   for (int j = 0; j < nd; ++j) M[j * 128] = make_double2(0.0, 0.0);
   int64_t a, len;
@@ -171,8 +142,7 @@ __global__ void __launch_bounds__(128) minors_sweep_kernel(const SweepProblem* _
         flip_binary<NF>(D, i, bit, sr, si);
         parity ^= 1u;
       } else {
-        if (glynn) settle_minors_glynn(P, M, Rr, Ri, w, g, t_seg);
-        else settle_minors(P, M, Rr, Ri, w, g, t_seg);
+        settle_minors(P, M, Rr, Ri, w, g, t_seg);
         Rr = 0.0;
         Ri = 0.0;
         t_seg = t;
@@ -187,8 +157,7 @@ __global__ void __launch_bounds__(128) minors_sweep_kernel(const SweepProblem* _
       }
       accumulate_product<NF>(sr, si, bias, parity << 31, Rr, Ri);
     }
-    if (glynn) settle_minors_glynn(P, M, Rr, Ri, w, g, t_seg);
-    else settle_minors(P, M, Rr, Ri, w, g, t_seg);
+    settle_minors(P, M, Rr, Ri, w, g, t_seg);
   }
   const int G = P.group;
   if (G > 1) {  // each aligned group of G lanes (one sweep's threads) sums its minors:
