@@ -500,13 +500,33 @@ int boss_perm_batch(const double* matrix, int32_t m, const int32_t* input_states
   std::lock_guard<std::mutex> lk(g_api_mutex);
   std::vector<HostSweep> by_nf[kMaxFactors + 1];
   std::vector<int> which[kMaxFactors + 1];
-  bool any = false;
+  std::vector<int> small[kSmallPermMax + 1];  // one GPU thread per permanent, no planning
+  bool any = false, any_small = false;
+  if (variant < BOSS_RYSER || variant > BOSS_CLASSIC) {
+    set_error("unknown permanent variant");
+    return kErrArg;
+  }
   for (int k = 0; k < count; ++k) {
+    const int32_t* Sk = input_states + (size_t)k * len;
+    const int32_t* Tk = output_states + (size_t)k * len;
+    if (len <= m) {  // equal particle counts up to kSmallPermMax: every variant is the permanent
+      int ni = 0, no = 0;
+      bool ok = true;
+      for (int i = 0; i < len; ++i) {
+        ok &= (Sk[i] >= 0 && Tk[i] >= 0 && Sk[i] <= 255 && Tk[i] <= 255);
+        ni += Sk[i];
+        no += Tk[i];
+      }
+      if (ok && ni == no && ni >= 1 && ni <= kSmallPermMax) {
+        small[ni].push_back(k);
+        any_small = true;
+        continue;
+      }
+    }
     HostSweep hs;
     bool need = false;
     double2 v = make_double2(0.0, 0.0);
-    const int st = plan_permanent(matrix, m, input_states + (size_t)k * len, output_states + (size_t)k * len, len,
-                                  variant, hs, need, v);
+    const int st = plan_permanent(matrix, m, Sk, Tk, len, variant, hs, need, v);
     if (st) return st;
     if (need) {
       which[hs.nf].push_back(k);
@@ -517,10 +537,13 @@ int boss_perm_batch(const double* matrix, int32_t m, const int32_t* input_states
       results[2 * k + 1] = v.y;
     }
   }
-  if (!any) return kOk;
+  if (!any && !any_small) return kOk;
   int st;
   Context* cx = context(&st);
   if (!cx) return st;
+  if (any_small && (st = small_perm_batch(cx, matrix, m, len, input_states, output_states, small,
+                                          (double2*)results)))
+    return st;
   for (int nf = 1; nf <= kMaxFactors; ++nf) {
     if (by_nf[nf].empty()) continue;
     std::vector<double2> out(by_nf[nf].size());

@@ -40,11 +40,11 @@ extern std::mutex g_api_mutex;
 constexpr int kDistMaxL = 10;  // per-thread permanents up to 10 x 10 (512 sign vectors)
 constexpr int kDistMaxDiv = 8;  // divisors (factorials of occupations >= 2) kept per state
 
-// |perm(U[rows, cols])|^2 for one L x L pair: Glynn's formula with the sign of
+// perm(U[rows, cols]) for one L x L matrix: Glynn's formula with the sign of
 // column 0 fixed, columns 1..L-1 walked in binary-reflected Gray order.
 template <int L>
-__device__ __forceinline__ double glynn_abs2(const double2* __restrict__ U, int m, const int (&row)[L],
-                                            const int (&col)[L]) {
+__device__ __forceinline__ double2 glynn_small(const double2* __restrict__ U, int m, const int (&row)[L],
+                                              const int (&col)[L]) {
   double sr[L], si[L];
 #pragma unroll
   for (int a = 0; a < L; ++a) {
@@ -89,9 +89,31 @@ __device__ __forceinline__ double glynn_abs2(const double2* __restrict__ U, int 
     }
   }
   const double s = ldexp(1.0, -(L - 1));
-  accr *= s;
-  acci *= s;
-  return fma(accr, accr, acci * acci);
+  return make_double2(accr * s, acci * s);
+}
+
+template <int L>
+__device__ __forceinline__ double glynn_abs2(const double2* __restrict__ U, int m, const int (&row)[L],
+                                            const int (&col)[L]) {
+  const double2 p = glynn_small<L>(U, m, row, col);
+  return fma(p.x, p.x, p.y * p.y);
+}
+
+// Small permanents, one thread each: perm(U[T_k, S_k]) from the occupation rows
+// (len entries, uint8) of equally many (L) input and output particles.
+template <int L>
+__global__ void __launch_bounds__(128) small_perm_kernel(const double2* __restrict__ U, int m, int len,
+                                                         const uint8_t* __restrict__ S, const uint8_t* __restrict__ T,
+                                                         int64_t count, double2* __restrict__ out) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= count) return;
+  int row[L], col[L];
+  int a = 0, b = 0;
+  for (int i = 0; i < len; ++i) {
+    for (int c = T[k * len + i]; c > 0 && a < L; --c) row[a++] = i;
+    for (int c = S[k * len + i]; c > 0 && b < L; --c) col[b++] = i;
+  }
+  out[k] = glynn_small<L>(U, m, row, col);
 }
 
 // One thread per (lossy input k, outcome o); the layout [k][o] lets the outcome
@@ -389,6 +411,77 @@ static int group_large(Context* cx, const double* matrix, int m, int n, int l, c
     for (int d = 0; d < nd; ++d) p /= div[d];
     prob_out[where[o]] = p;
   }
+  return kOk;
+}
+
+template <int L>
+static cudaError_t launch_small(const double2* U, int m, int len, const uint8_t* S, const uint8_t* T, int64_t count,
+                                double2* out, cudaStream_t s) {
+  small_perm_kernel<L><<<(unsigned)((count + 127) / 128), 128, 0, s>>>(U, m, len, S, T, count, out);
+  return cudaGetLastError();
+}
+
+static cudaError_t launch_small_l(int l, const double2* U, int m, int len, const uint8_t* S, const uint8_t* T,
+                                  int64_t count, double2* out, cudaStream_t s) {
+  switch (l) {
+    case 1: return launch_small<1>(U, m, len, S, T, count, out, s);
+    case 2: return launch_small<2>(U, m, len, S, T, count, out, s);
+    case 3: return launch_small<3>(U, m, len, S, T, count, out, s);
+    case 4: return launch_small<4>(U, m, len, S, T, count, out, s);
+    case 5: return launch_small<5>(U, m, len, S, T, count, out, s);
+    case 6: return launch_small<6>(U, m, len, S, T, count, out, s);
+    case 7: return launch_small<7>(U, m, len, S, T, count, out, s);
+    case 8: return launch_small<8>(U, m, len, S, T, count, out, s);
+    case 9: return launch_small<9>(U, m, len, S, T, count, out, s);
+    case 10: return launch_small<10>(U, m, len, S, T, count, out, s);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+int small_perm_batch(Context* cx, const double* matrix, int m, int len, const int32_t* S, const int32_t* T,
+                     const std::vector<int>* by_l, double2* results) {
+  int64_t total = 0;
+  for (int l = 1; l <= kSmallPermMax; ++l) total += (int64_t)by_l[l].size();
+  if (total == 0) return kOk;
+  auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
+  const size_t o_U = 0, o_S = al(sizeof(double2) * (size_t)m * m), o_T = o_S + al((size_t)total * len);
+  const size_t o_out = o_T + al((size_t)total * len), arena = o_out + sizeof(double2) * (size_t)total;
+  int st;
+  if ((st = ensure(cx->dist[3], arena))) return st;
+  if ((st = ensure_pinned(cx, arena))) return st;
+  char* h = (char*)cx->pinned;
+  memcpy(h + o_U, matrix, sizeof(double2) * (size_t)m * m);
+  uint8_t* hS = (uint8_t*)(h + o_S);
+  uint8_t* hT = (uint8_t*)(h + o_T);
+  int64_t at = 0;
+  for (int l = 1; l <= kSmallPermMax; ++l)
+    for (int k : by_l[l]) {
+      for (int i = 0; i < len; ++i) {
+        hS[at * len + i] = (uint8_t)S[(size_t)k * len + i];
+        hT[at * len + i] = (uint8_t)T[(size_t)k * len + i];
+      }
+      ++at;
+    }
+  char* d = (char*)cx->dist[3].ptr;
+  cudaStream_t s = cx->stream;
+  cudaError_t e = cudaMemcpyAsync(d, h, o_out, cudaMemcpyHostToDevice, s);
+  if (e != cudaSuccess) return fail_cuda(e, "H2D small permanents");
+  at = 0;
+  for (int l = 1; l <= kSmallPermMax; ++l) {
+    const int64_t c = (int64_t)by_l[l].size();
+    if (!c) continue;
+    e = launch_small_l(l, (const double2*)(d + o_U), m, len, (const uint8_t*)(d + o_S) + at * len,
+                       (const uint8_t*)(d + o_T) + at * len, c, (double2*)(d + o_out) + at, s);
+    if (e != cudaSuccess) return fail_cuda(e, "small permanents");
+    at += c;
+  }
+  e = cudaMemcpyAsync(h + o_out, d + o_out, sizeof(double2) * (size_t)total, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return fail_cuda(e, "small permanents");
+  const double2* hr = (const double2*)(h + o_out);
+  at = 0;
+  for (int l = 1; l <= kSmallPermMax; ++l)
+    for (int k : by_l[l]) results[k] = hr[at++];
   return kOk;
 }
 

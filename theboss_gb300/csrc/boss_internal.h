@@ -100,6 +100,13 @@ int ensure_pinned(Context* cx, size_t bytes);
 // (perms) or nd_max complex per sweep (all-minors).
 int run_sweeps(Context* cx, const std::vector<HostSweep>& sweeps, bool minors, int nd_max, double2* results_host);
 
+// Permanents of at most kSmallPermMax particles, one GPU thread each (Glynn's
+// formula in registers, no sweep planning): by_l[l] lists the requests k with
+// l = sum(S_k) = sum(T_k) particles; S, T are the callers' occupation rows.
+constexpr int kSmallPermMax = 10;
+int small_perm_batch(Context* cx, const double* matrix, int m, int len, const int32_t* S, const int32_t* T,
+                     const std::vector<int>* by_l, double2* results);
+
 // One permanent request (theboss's variant semantics).  Returns kOk and either
 // fills `hs` (needs_sweep = true) or sets `value` for the edge cases theboss
 // special-cases.
