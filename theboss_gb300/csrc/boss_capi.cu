@@ -106,8 +106,13 @@ static int sweeps_prepare(Context* cx, const std::vector<HostSweep>& sweeps, boo
     codes[p] = sweeps[p].total_codes;
     B.codes += (double)codes[p];
   }
+  int rows = 1;  // all-minors: shared-memory rows of minors per thread
+  for (int p = 0; p < n; ++p) rows = std::max(rows, sweeps[p].nd + (sweeps[p].fixed_mode >= 0 ? 1 : 0));
   std::vector<int64_t> nthr;
-  partition_threads(codes, sweep_resident_threads(B.nf, op, cx->sm_count), nthr);
+  partition_threads(codes,
+                    minors ? sweep_resident_minors(B.nf, rows, cx->sm_count)
+                           : sweep_resident_threads(B.nf, op, cx->sm_count),
+                    nthr);
   std::vector<SweepProblem> probs(n);
   int64_t pool_n = 0, threads = 0, parts = 0;
   for (int p = 0; p < n; ++p) {
@@ -163,6 +168,7 @@ static int sweeps_prepare(Context* cx, const std::vector<HostSweep>& sweeps, boo
   B.L.total_threads = threads;
   B.L.partials = (double2*)cx->partials.ptr;
   B.L.grid = (int)((threads + 127) / 128);
+  B.L.rows = rows;
   return kOk;
 }
 

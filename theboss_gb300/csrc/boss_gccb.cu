@@ -713,7 +713,8 @@ static int gccb_prepare(Context* cx, const double* matrix, int n_mats, int m, Dr
     const int Ak = A[k];
     const std::vector<uint64_t>& codes = lvl_codes[k];
     const std::vector<int>& ndv = lvl_nd[k];
-    const int64_t resident = sweep_resident_threads(k - 1, SweepOp::kMinors, cx->sm_count);
+    // k input particles: at most k distinct modes, so at most k rows of minors per thread
+    const int64_t resident = sweep_resident_minors(k - 1, std::min(k, kMaxMinorDigits), cx->sm_count);
     bool same = true;
     uint64_t code0 = 1ull << (k - 1);
     int nd0 = k;
@@ -851,6 +852,7 @@ static int gccb_prepare(Context* cx, const double* matrix, int n_mats, int m, Dr
       SL.total_threads = lvl_threads[k];
       SL.partials = partials;
       SL.grid = (int)((lvl_threads[k] + 127) / 128);
+      SL.rows = std::min(k, kMaxMinorDigits);
       if (timing) le = cudaEventRecordWithFlags(R.ev[2 * (k - 2)], s, cudaEventRecordExternal);
       if (le == cudaSuccess) le = launch_sweep(k - 1, SweepOp::kMinors, SL, s);
       if (timing && le == cudaSuccess) le = cudaEventRecordWithFlags(R.ev[2 * (k - 2) + 1], s, cudaEventRecordExternal);

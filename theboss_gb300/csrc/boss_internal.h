@@ -22,12 +22,15 @@ struct SweepLaunch {
   double2* partials = nullptr;
   double2* partials2 = nullptr;  // gradients: per-warp permanent partials
   int grid = 1;
+  int rows = 32;  // all-minors: shared-memory rows of minors per thread (nd + held digit, at most 32)
 };
 
 // Sets kernel attributes and records occupancy (once per process, outside any capture).
 cudaError_t prepare_sweep_kernels();
 // Resident threads of one full wave of the sweep kernel for `nf` factors.
 int64_t sweep_resident_threads(int nf, SweepOp op, int sm_count);
+// Resident threads of the all-minors kernel with `rows` rows of minors per thread.
+int64_t sweep_resident_minors(int nf, int rows, int sm_count);
 cudaError_t launch_sweep(int nf, SweepOp op, const SweepLaunch& L, cudaStream_t st);
 cudaError_t launch_perm_reduce(const SweepProblem* probs, int n_probs, const double2* partials, double2* out,
                                cudaStream_t st);

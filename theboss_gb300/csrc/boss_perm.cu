@@ -22,14 +22,20 @@ cudaError_t sweep_nf_c_grad_occupancy(int nf, int* occ);
 cudaError_t sweep_nf_d_grad_occupancy(int nf, int* occ);
 
 static int g_perm_occ[kMaxFactors + 1];
-static int g_minors_occ[kMaxFactors + 1];
+static int g_minors_occ[kMaxFactors + 1][kMaxMinorDigits + 1];  // [nf][rows of minors]
 
 cudaError_t prepare_sweep_kernels() {
   cudaError_t e;
-  if ((e = sweep_nf_a_prepare(g_perm_occ + 1, g_minors_occ + 1)) != cudaSuccess) return e;
-  if ((e = sweep_nf_b_prepare(g_perm_occ + 9, g_minors_occ + 9)) != cudaSuccess) return e;
-  if ((e = sweep_nf_c_prepare(g_perm_occ + 17, g_minors_occ + 17)) != cudaSuccess) return e;
-  return sweep_nf_d_prepare(g_perm_occ + 25, g_minors_occ + 25);
+  if ((e = sweep_nf_a_prepare(g_perm_occ + 1, &g_minors_occ[1][0])) != cudaSuccess) return e;
+  if ((e = sweep_nf_b_prepare(g_perm_occ + 9, &g_minors_occ[9][0])) != cudaSuccess) return e;
+  if ((e = sweep_nf_c_prepare(g_perm_occ + 17, &g_minors_occ[17][0])) != cudaSuccess) return e;
+  return sweep_nf_d_prepare(g_perm_occ + 25, &g_minors_occ[25][0]);
+}
+
+int64_t sweep_resident_minors(int nf, int rows, int sm_count) {
+  if (nf < 1 || nf > kMaxFactors) return 128;
+  rows = std::min(std::max(rows, 1), kMaxMinorDigits);
+  return (int64_t)std::max(1, g_minors_occ[nf][rows]) * sm_count * 128;
 }
 
 int64_t sweep_resident_threads(int nf, SweepOp op, int sm_count) {
@@ -46,7 +52,7 @@ int64_t sweep_resident_threads(int nf, SweepOp op, int sm_count) {
     }
     return (int64_t)std::max(occ, 1) * sm_count * 64;
   }
-  const int occ = std::max(1, op == SweepOp::kPerm ? g_perm_occ[nf] : g_minors_occ[nf]);
+  const int occ = std::max(1, op == SweepOp::kPerm ? g_perm_occ[nf] : g_minors_occ[nf][kMaxMinorDigits]);
   return (int64_t)occ * sm_count * 128;
 }
 

@@ -391,9 +391,10 @@ cudaError_t sweep_launch_t(SweepOp op, const SweepLaunch& L, cudaStream_t st) {
   }
   if (op == SweepOp::kPerm) {
     perm_sweep_kernel<NF><<<L.grid, 128, 0, st>>>(L.probs, L.n_probs, L.pool, L.total_threads, L.partials);
-  } else {
-    minors_sweep_kernel<NF><<<L.grid, 128, kMinorsSmem, st>>>(L.probs, L.n_probs, L.pool, L.total_threads,
-                                                              L.partials);
+  } else {  // shared memory: the launch's rows of minors per thread, 128 threads per block
+    const int rows = (L.rows >= 1 && L.rows <= kMaxMinorDigits) ? L.rows : kMaxMinorDigits;
+    minors_sweep_kernel<NF><<<L.grid, 128, (size_t)rows * 128 * sizeof(double2), st>>>(
+        L.probs, L.n_probs, L.pool, L.total_threads, L.partials);
   }
   return cudaGetLastError();
 }
@@ -404,6 +405,8 @@ cudaError_t grad_occupancy_t(int* blocks_per_sm) {
                                                        (size_t)(2 * NF) * 64 * sizeof(double2));
 }
 
+// minors_blocks_per_sm[r] (r = 1..kMaxMinorDigits): blocks per SM with r rows of
+// minors per thread in shared memory.
 template <int NF>
 cudaError_t sweep_prepare_t(int* perm_blocks_per_sm, int* minors_blocks_per_sm) {
   cudaError_t e = cudaFuncSetAttribute(minors_sweep_kernel<NF>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -413,8 +416,12 @@ cudaError_t sweep_prepare_t(int* perm_blocks_per_sm, int* minors_blocks_per_sm) 
   if (e != cudaSuccess) return e;
   e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(perm_blocks_per_sm, perm_sweep_kernel<NF>, 128, 0);
   if (e != cudaSuccess) return e;
-  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(minors_blocks_per_sm, minors_sweep_kernel<NF>, 128,
-                                                       kMinorsSmem);
+  for (int r = 1; r <= kMaxMinorDigits; ++r) {
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(minors_blocks_per_sm + r, minors_sweep_kernel<NF>, 128,
+                                                      (size_t)r * 128 * sizeof(double2));
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
 }
 
 }  // namespace boss
@@ -448,16 +455,17 @@ cudaError_t sweep_prepare_t(int* perm_blocks_per_sm, int* minors_blocks_per_sm) 
       default: return cudaErrorInvalidValue;                                                             \
     }                                                                                                    \
   }                                                                                                      \
-  cudaError_t NAME##_prepare(int* perm_occ, int* minors_occ) {                                           \
+  cudaError_t NAME##_prepare(int* perm_occ, int* minors_occ) { /* minors_occ: 8 rows of 33 */           \
     cudaError_t e;                                                                                       \
-    for (int k = 0; k < 8; ++k) perm_occ[k] = minors_occ[k] = 1;                                         \
-    if ((e = sweep_prepare_t<(LO) + 0>(perm_occ + 0, minors_occ + 0)) != cudaSuccess) return e;          \
-    if ((e = sweep_prepare_t<(LO) + 1>(perm_occ + 1, minors_occ + 1)) != cudaSuccess) return e;          \
-    if ((e = sweep_prepare_t<(LO) + 2>(perm_occ + 2, minors_occ + 2)) != cudaSuccess) return e;          \
-    if ((e = sweep_prepare_t<(LO) + 3>(perm_occ + 3, minors_occ + 3)) != cudaSuccess) return e;          \
-    if ((e = sweep_prepare_t<(LO) + 4>(perm_occ + 4, minors_occ + 4)) != cudaSuccess) return e;          \
-    if ((e = sweep_prepare_t<(LO) + 5>(perm_occ + 5, minors_occ + 5)) != cudaSuccess) return e;          \
-    if ((e = sweep_prepare_t<(LO) + 6>(perm_occ + 6, minors_occ + 6)) != cudaSuccess) return e;          \
-    return sweep_prepare_t<(LO) + 7>(perm_occ + 7, minors_occ + 7);                                      \
+    for (int k = 0; k < 8; ++k) perm_occ[k] = 1;                                                         \
+    for (int k = 0; k < 8 * 33; ++k) minors_occ[k] = 1;                                                  \
+    if ((e = sweep_prepare_t<(LO) + 0>(perm_occ + 0, minors_occ + 0 * 33)) != cudaSuccess) return e;     \
+    if ((e = sweep_prepare_t<(LO) + 1>(perm_occ + 1, minors_occ + 1 * 33)) != cudaSuccess) return e;     \
+    if ((e = sweep_prepare_t<(LO) + 2>(perm_occ + 2, minors_occ + 2 * 33)) != cudaSuccess) return e;     \
+    if ((e = sweep_prepare_t<(LO) + 3>(perm_occ + 3, minors_occ + 3 * 33)) != cudaSuccess) return e;     \
+    if ((e = sweep_prepare_t<(LO) + 4>(perm_occ + 4, minors_occ + 4 * 33)) != cudaSuccess) return e;     \
+    if ((e = sweep_prepare_t<(LO) + 5>(perm_occ + 5, minors_occ + 5 * 33)) != cudaSuccess) return e;     \
+    if ((e = sweep_prepare_t<(LO) + 6>(perm_occ + 6, minors_occ + 6 * 33)) != cudaSuccess) return e;     \
+    return sweep_prepare_t<(LO) + 7>(perm_occ + 7, minors_occ + 7 * 33);                                 \
   }                                                                                                      \
   }
