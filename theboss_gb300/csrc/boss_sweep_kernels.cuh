@@ -56,28 +56,30 @@ __global__ void __launch_bounds__(128) perm_sweep_kernel(const SweepProblem* __r
 // Closes the current segment of an all-minors sweep: every digit receives R
 // times its weight w_j = mult_j - 2 r_j (binary digits: +-1) times prod C(mult, r),
 // the held digit (row nd) R times 1 -- halved, see minors_sweep_kernel.
+// M: this thread's minors, row j at M[j * STRIDE].
+template <int STRIDE>
 __device__ __forceinline__ void settle_minors(const SweepProblem& P, double2* M, double Rr, double Ri, double w,
-                                                   uint64_t g, uint64_t t_seg) {
+                                              uint64_t g, uint64_t t_seg) {
   const double wr = 0.5 * w * Rr, wi = 0.5 * w * Ri;
   for (int j = 0; j < P.nb; ++j) {
     const uint32_t neg = (uint32_t)((g >> j) & 1ull) << 31;
-    double2 v = M[j * 128];
+    double2 v = M[j * STRIDE];
     v.x += xor_sign(wr, neg);
     v.y += xor_sign(wi, neg);
-    M[j * 128] = v;
+    M[j * STRIDE] = v;
   }
   for (int j = P.nb; j < P.nd; ++j) {
     const double f = (double)P.mult[j] - 2.0 * (double)digit_value(P, t_seg, j);
-    double2 v = M[j * 128];
+    double2 v = M[j * STRIDE];
     v.x = fma(wr, f, v.x);
     v.y = fma(wi, f, v.y);
-    M[j * 128] = v;
+    M[j * STRIDE] = v;
   }
   if (P.fixed_digit) {
-    double2 v = M[P.nd * 128];
+    double2 v = M[P.nd * STRIDE];
     v.x += wr;
     v.y += wi;
-    M[P.nd * 128] = v;
+    M[P.nd * STRIDE] = v;
   }
 }
 
@@ -94,25 +96,17 @@ __device__ __forceinline__ void settle_minors(const SweepProblem& P, double2* M,
 // (w_before - w_after) R = +-2R.  The kernel accumulates half of every minor
 // (flips add +-R, settles w R / 2); the problem's scale carries the factor 2.
 // Segments of 2^16 codes (and every change of a multi-valued digit) are closed
-// by settle_minors and R restarts from zero.  Per-thread minors live in shared memory (digit-major,
-// 128-thread stride); every thread writes nd complex partials.
-template <int NF>
-__global__ void __launch_bounds__(128) minors_sweep_kernel(const SweepProblem* __restrict__ probs, int n_probs,
-                                                           const longlong2* __restrict__ pool, int64_t total_threads,
-                                                           double2* __restrict__ partials) {
-  extern __shared__ double2 minors_smem[];
-  const int64_t gt = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (gt >= total_threads) return;
-  const SweepProblem& P = probs[find_problem(probs, n_probs, gt)];
-  const int64_t q = gt - P.thread_begin;
-  const int nd = P.nd + P.fixed_digit;  // minors written per thread
-  double2* M = minors_smem + threadIdx.x;
-  for (int j = 0; j < nd; ++j) M[j * 128] = make_double2(0.0, 0.0);
+// by settle_minors and R restarts from zero.  minors_walk is one thread's part
+// (thread q of the sweep's threads); its minors live in shared memory, row j at
+// M[j * STRIDE].
+template <int NF, int STRIDE>
+__device__ __forceinline__ void minors_walk(const SweepProblem& P, const longlong2* __restrict__ D,
+                                            const longlong2* __restrict__ base, int64_t q, double2* M) {
+  const int nd = P.nd + P.fixed_digit;
+  for (int j = 0; j < nd; ++j) M[j * STRIDE] = make_double2(0.0, 0.0);
   int64_t a, len;
   thread_range(P, q, a, len);
   if (len > 0) {
-    const longlong2* D = pool + P.mat_off;
-    const longlong2* base = pool + P.base_off;
     const int bias = 1023 + 63 - P.fx;
     const int nb = P.nb;
     const int low = nb < kSegLog ? nb : kSegLog;
@@ -134,15 +128,15 @@ __global__ void __launch_bounds__(128) minors_sweep_kernel(const SweepProblem* _
           vr *= w;
           vi *= w;
         }
-        double2 v = M[i * 128];
+        double2 v = M[i * STRIDE];
         v.x += xor_sign(vr, bit << 31);
         v.y += xor_sign(vi, bit << 31);
-        M[i * 128] = v;
+        M[i * STRIDE] = v;
         g ^= 1ull << i;
         flip_binary<NF>(D, i, bit, sr, si);
         parity ^= 1u;
       } else {
-        settle_minors(P, M, Rr, Ri, w, g, t_seg);
+        settle_minors<STRIDE>(P, M, Rr, Ri, w, g, t_seg);
         Rr = 0.0;
         Ri = 0.0;
         t_seg = t;
@@ -157,8 +151,24 @@ __global__ void __launch_bounds__(128) minors_sweep_kernel(const SweepProblem* _
       }
       accumulate_product<NF>(sr, si, bias, parity << 31, Rr, Ri);
     }
-    settle_minors(P, M, Rr, Ri, w, g, t_seg);
+    settle_minors<STRIDE>(P, M, Rr, Ri, w, g, t_seg);
   }
+}
+
+// One launch over many all-minors sweeps (128 threads per block); every thread
+// writes nd + held complex partials, or its group of `group` threads writes their sum.
+template <int NF>
+__global__ void __launch_bounds__(128) minors_sweep_kernel(const SweepProblem* __restrict__ probs, int n_probs,
+                                                           const longlong2* __restrict__ pool, int64_t total_threads,
+                                                           double2* __restrict__ partials) {
+  extern __shared__ double2 minors_smem[];
+  const int64_t gt = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (gt >= total_threads) return;
+  const SweepProblem& P = probs[find_problem(probs, n_probs, gt)];
+  const int64_t q = gt - P.thread_begin;
+  const int nd = P.nd + P.fixed_digit;  // minors written per thread
+  double2* M = minors_smem + threadIdx.x;
+  minors_walk<NF, 128>(P, pool + P.mat_off, pool + P.base_off, q, M);
   const int G = P.group;
   if (G > 1) {  // each aligned group of G lanes (one sweep's threads) sums its minors:
                 // lane l of the group adds up digits l, l + G, .. over the group, in a fixed order
