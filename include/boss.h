@@ -167,6 +167,16 @@ BOSS_API int boss_gccb_sample(const double* matrix, int32_t m, const int32_t* in
                               const double* particle_weights, int32_t n_weights, uint32_t* mt_key, int32_t* mt_pos,
                               int32_t n_samples, int32_t* samples);
 
+// Arithmetic of the all-minors sweeps (boss_submatrices_batch and the batched
+// sampler's levels, boss_gccb_sample*, boss_gccb_bench; theboss computes them in
+// numpy float64, bs_cc_ryser_submatrices_permanent_calculator.py:96-119).
+// mode 0 (default): products, running totals and minors as float pairs (two
+// FP32 values, about 47 significant bits) on the FP32 pipe, for sweeps of at
+// most 24 product-side particles; mode 1: FP64 throughout; -1: query only.
+// *previous (if not null) receives the mode in force before the call.  Row sums
+// are exact 64-bit fixed point in both.
+BOSS_API int boss_minors_arithmetic(int32_t mode, int32_t* previous);
+
 /*
  * Benchmark form of boss_gccb_sample: the random stream is replayed and the
  * inputs uploaded once, then the captured sampler graph runs n_warmup + n_steps

@@ -31,3 +31,15 @@ def oracle():
 
     O.lib()
     return O
+
+
+@pytest.fixture(params=["float_pairs", "fp64"])
+def minors_arith(request):
+    """Runs a test under both arithmetics of the all-minors sweeps, restoring the
+    previous one afterwards."""
+    from theboss_gb300 import _native
+
+    mode = _native.FLOAT_PAIRS if request.param == "float_pairs" else _native.FP64
+    prev = _native.minors_arithmetic(mode)
+    yield request.param
+    _native.minors_arithmetic(prev)

@@ -112,7 +112,7 @@ def test_mode_assignment_gcc_matches_reference_streams():
 
 
 @pytest.mark.parametrize("n,m,eta,N", [(12, 24, 0.5, 400), (20, 40, 0.5, 300), (8, 16, None, 200)])
-def test_batched_sampler_matches_oracle(oracle, n, m, eta, N):
+def test_batched_sampler_matches_oracle(oracle, n, m, eta, N, minors_arith):
     from theboss_gb300 import _native
     from theboss_gb300.utilities import haar_unitary
 
@@ -146,7 +146,27 @@ def test_plain_driver_equals_batched():
     assert [x.tolist() for x in a] == [x.tolist() for x in b]
 
 
-def test_binned_input_sampling_matches_oracle(oracle):
+def test_float_pairs_and_fp64_give_one_stream(oracle):
+    """3000 samples of the 20-photon, 40-mode uniform-loss benchmark case drawn with
+    float-pair and with FP64 all-minors sweeps are the same samples."""
+    from theboss_gb300 import _native
+    from theboss_gb300.utilities import haar_unitary
+
+    U = haar_unitary(40, 2020)
+    inp = np.array([1] * 20 + [0] * 20, dtype=np.int32)
+    w = oracle.binomial_weights(20, 0.5)
+    out = {}
+    for mode in (_native.FLOAT_PAIRS, _native.FP64):
+        prev = _native.minors_arithmetic(mode)
+        try:
+            np.random.seed(99)
+            out[mode] = _native.gccb_sample(U, inp, w, 3000)
+        finally:
+            _native.minors_arithmetic(prev)
+    assert np.array_equal(out[_native.FLOAT_PAIRS], out[_native.FP64])
+
+
+def test_binned_input_sampling_matches_oracle(oracle, minors_arith):
     from theboss_gb300 import _native
     from theboss_gb300.utilities import haar_unitary
 

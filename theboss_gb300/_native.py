@@ -95,6 +95,8 @@ def load() -> ctypes.CDLL:
         L.boss_gccb_sample_slice.restype = ctypes.c_int
         L.boss_gccb_sample_slice.argtypes = [dp, ctypes.c_int32, ip, dp, ctypes.c_int32, up, ip, ctypes.c_int32,
                                              ctypes.c_int32, ctypes.c_int32, ip]
+        L.boss_minors_arithmetic.restype = ctypes.c_int
+        L.boss_minors_arithmetic.argtypes = [ctypes.c_int32, ip]
         _lib = L
         return L
 
@@ -328,6 +330,19 @@ def fp64_peak():
     ms = np.zeros(1)
     check(L.boss_fp64_peak(_dp(t), _dp(ms)))
     return float(t[0]), float(ms[0])
+
+
+FLOAT_PAIRS = 0  # all-minors sweeps: float pairs on the FP32 pipe (default)
+FP64 = 1
+
+
+def minors_arithmetic(mode: int = -1) -> int:
+    """Sets the arithmetic of the all-minors sweeps (submatrices and the batched
+    sampler's levels: FLOAT_PAIRS or FP64; -1 only queries) and returns the
+    previous one."""
+    prev = np.zeros(1, dtype=np.int32)
+    check(load().boss_minors_arithmetic(int(mode), _ip(prev)))
+    return int(prev[0])
 
 
 def select_device(device: int) -> None:

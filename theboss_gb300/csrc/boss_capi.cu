@@ -87,6 +87,7 @@ static inline size_t align_up(size_t x, size_t a) { return (x + a - 1) & ~(a - 1
 struct SweepBatch {
   int n = 0, nf = 0;
   bool minors = false;
+  bool ff = false;  // all-minors on float pairs
   int nd_max = 1;
   SweepLaunch L;
   size_t out_elems = 0;
@@ -99,6 +100,7 @@ static int sweeps_prepare(Context* cx, const std::vector<HostSweep>& sweeps, boo
   B.nf = sweeps[0].nf;
   B.minors = minors;
   B.nd_max = nd_max;
+  B.ff = minors && g_minors_arith == 0 && minors_ff_available(B.nf);
   const SweepOp op = minors ? SweepOp::kMinors : SweepOp::kPerm;
   std::vector<uint64_t> codes(n);
   B.codes = 0.0;
@@ -110,7 +112,7 @@ static int sweeps_prepare(Context* cx, const std::vector<HostSweep>& sweeps, boo
   for (int p = 0; p < n; ++p) rows = std::max(rows, sweeps[p].nd + (sweeps[p].fixed_mode >= 0 ? 1 : 0));
   std::vector<int64_t> nthr;
   partition_threads(codes,
-                    minors ? sweep_resident_minors(B.nf, rows, cx->sm_count)
+                    minors ? sweep_resident_minors(B.nf, rows, cx->sm_count, B.ff)
                            : sweep_resident_threads(B.nf, op, cx->sm_count),
                     nthr);
   std::vector<SweepProblem> probs(n);
@@ -136,6 +138,11 @@ static int sweeps_prepare(Context* cx, const std::vector<HostSweep>& sweeps, boo
     pool_n += (int64_t)h.base.size();
     P.part_off = parts;
     P.scale = h.scale;
+    if (B.ff) {  // float-pair rows of the binary digits, then the factors' biases
+      P.ff_off = pool_n;
+      pool_n += (int64_t)h.nb * h.nf + (h.nf + 3) / 4;
+      P.scale = std::ldexp(h.scale, h.ff_exp);
+    }
     P.fixed_digit = (h.fixed_mode >= 0) ? 1 : 0;
     for (int i = 0; i < h.nd; ++i) P.mult[i] = h.mult[i];
     threads += nthr[p];
@@ -156,8 +163,21 @@ static int sweeps_prepare(Context* cx, const std::vector<HostSweep>& sweeps, boo
   memcpy(h + o_probs, probs.data(), sizeof(SweepProblem) * n);
   longlong2* hp = (longlong2*)(h + o_pool);
   for (int p = 0; p < n; ++p) {
-    std::copy(sweeps[p].D.begin(), sweeps[p].D.end(), hp + probs[p].mat_off);
-    std::copy(sweeps[p].base.begin(), sweeps[p].base.end(), hp + probs[p].base_off);
+    const HostSweep& hs = sweeps[p];
+    std::copy(hs.D.begin(), hs.D.end(), hp + probs[p].mat_off);
+    std::copy(hs.base.begin(), hs.base.end(), hp + probs[p].base_off);
+    if (B.ff) {
+      float4* df = reinterpret_cast<float4*>(hp + probs[p].ff_off);
+      for (int d = 0; d < hs.nb; ++d)
+        for (int f = 0; f < hs.nf; ++f) {
+          const longlong2 v = hs.D[(size_t)d * hs.nf + f];
+          float4& o = df[(size_t)d * hs.nf + f];
+          host_fx_to_ff(v.x, hs.fbias[f], o.x, o.y);
+          host_fx_to_ff(v.y, hs.fbias[f], o.z, o.w);
+        }
+      int* fb = reinterpret_cast<int*>(df + (size_t)hs.nb * hs.nf);
+      for (int f = 0; f < hs.nf; ++f) fb[f] = hs.fbias[f];
+    }
   }
   char* d = (char*)cx->plans.ptr;
   cudaError_t e = cudaMemcpyAsync(d, h, arena_bytes, cudaMemcpyHostToDevice, cx->stream);
@@ -173,7 +193,8 @@ static int sweeps_prepare(Context* cx, const std::vector<HostSweep>& sweeps, boo
 }
 
 static int sweeps_launch(Context* cx, const SweepBatch& B, cudaEvent_t after_sweep = nullptr) {
-  cudaError_t e = launch_sweep(B.nf, B.minors ? SweepOp::kMinors : SweepOp::kPerm, B.L, cx->stream);
+  const SweepOp op = B.minors ? (B.ff ? SweepOp::kMinorsFF : SweepOp::kMinors) : SweepOp::kPerm;
+  cudaError_t e = launch_sweep(B.nf, op, B.L, cx->stream);
   if (e != cudaSuccess) return fail_cuda(e, "sweep launch");
   if (after_sweep) cudaEventRecord(after_sweep, cx->stream);
   e = B.minors ? launch_minors_reduce(B.L.probs, B.n, B.L.partials, (double2*)cx->out.ptr, B.nd_max, cx->stream)
@@ -321,7 +342,53 @@ static int fill_sweep(HostSweep& hs, const Side& dig, const Side& col, int kind,
     hs.scale = 1.0;
     hs.parity0 = dig.n & 1;
   }
+  hs.fbias.assign(hs.nf, 189);
+  hs.ff_exp = 0;
+  for (int f = 0; f < hs.nf; ++f) {
+    unsigned long long bx = 0, by = 0;
+    for (size_t a = 0; a < dig.modes.size(); ++a) {
+      const double2 z = entry(dig.modes[a], fmode[f]);
+      bx += (unsigned long long)dig.mult[a] * (unsigned long long)std::llabs(to_fixed(z.x, hs.fx));
+      by += (unsigned long long)dig.mult[a] * (unsigned long long)std::llabs(to_fixed(z.y, hs.fx));
+    }
+    const unsigned long long b = std::max(bx, by);
+    const int p = b ? 63 - __builtin_clzll(b) : 0;
+    hs.fbias[f] = 189 - p;
+    hs.ff_exp += p + 1 - hs.fx;
+  }
   return kOk;
+}
+
+int g_minors_arith = 0;
+
+void host_fx_to_ff(long long x, int fbias, float& hi, float& lo) {
+  const unsigned long long sgn = (unsigned long long)(x >> 63);
+  const unsigned long long ax = ((unsigned long long)x ^ sgn) - sgn;
+  if (!ax) {
+    hi = lo = 0.0f;
+    return;
+  }
+  const int lz = __builtin_clzll(ax);
+  const unsigned long long y = ax << lz;
+  const uint32_t yh = (uint32_t)(y >> 32);
+  const int ex = fbias - lz;
+  const uint32_t s32 = (uint32_t)sgn & 0x80000000u;
+  const uint32_t hb = (((uint32_t)(ex - 1)) << 23) + (yh >> 8);
+  const uint32_t nxt = (uint32_t)(y >> 17) & 0x7FFFFFu;
+  const uint32_t eb = ((uint32_t)(ex - 23)) << 23;
+  auto as_f = [](uint32_t u) {
+    float f;
+    memcpy(&f, &u, 4);
+    return f;
+  };
+  auto as_u = [](float f) {
+    uint32_t u;
+    memcpy(&u, &f, 4);
+    return u;
+  };
+  const float l = as_f(eb | nxt) - as_f(eb);
+  hi = as_f(hb | s32);
+  lo = as_f(as_u(l) ^ s32);
 }
 
 // One permanent request.  Returns kOk and either fills `hs` (needs_sweep = true)

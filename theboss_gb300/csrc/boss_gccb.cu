@@ -245,6 +245,7 @@ struct FinalizeArgs {
   LevelSample next_uni;         // uniform next level: n_codes, threads per sample and the per-sample
                                 // strides of partials (part_off) and rows (pool_off)
   int next_group;               // uniform next level: threads per summed group of minors
+  int next_ff;                  // the next level's sweep runs on float pairs (float-pair rows, biases)
   int* err;
 };
 
@@ -537,14 +538,42 @@ __global__ void __launch_bounds__(kFinWarps * 32) gccb_finalize_kernel(FinalizeA
     D[e] = make_longlong2(-2 * u.x, -2 * u.y);
   }
   longlong2* B = D + (size_t)nds * nf;
+  // Float-pair sweeps: factor f is scaled by 2^-(p_f + 1), 2^p_f <= its bound
+  // max(sum_d mult_d |Re U|, sum_d mult_d |Im U|) < 2^(p_f + 1) (fixed-point units),
+  // so |s_f| < 1 in that scale; fx_to_ff takes the bias 189 - p_f.
+  float4* DF = reinterpret_cast<float4*>(B + nf);
+  int* fbias = reinterpret_cast<int*>(DF + (size_t)(nb - held) * nf);
+  int esum = 0;  // sum_f (p_f + 1)
   for (int f = lane; f < nf; f += 32) {
     long long bx = 0, by = 0;
+    unsigned long long ax = 0, ay = 0;
     for (int d = 0; d < nd; ++d) {
       const longlong2 u = Ufxs[(size_t)fm_s[w][f] * m + dm_s[w][d]];
       bx += (long long)mult_s[w][d] * u.x;
       by += (long long)mult_s[w][d] * u.y;
+      ax += (unsigned long long)mult_s[w][d] * (unsigned long long)(u.x < 0 ? -u.x : u.x);
+      ay += (unsigned long long)mult_s[w][d] * (unsigned long long)(u.y < 0 ? -u.y : u.y);
     }
     B[f] = make_longlong2(bx, by);
+    if (a.next_ff) {
+      const unsigned long long bnd = ax > ay ? ax : ay;
+      const int p = bnd ? 63 - __clzll((long long)bnd) : 0;
+      fbias[f] = 189 - p;
+      esum += p + 1;
+    }
+  }
+  if (a.next_ff) {
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) esum += __shfl_xor_sync(0xffffffffu, esum, off);
+    __syncwarp();  // fbias written by the other lanes
+    for (int e = lane; e < (nb - held) * nf; e += 32) {
+      const int d = e / nf, f = e - d * nf;
+      const longlong2 u = Ufxs[(size_t)fm_s[w][f] * m + dm_s[w][d]];
+      float4 v;
+      fx_to_ff(-2 * u.x, fbias[f], v.x, v.y);
+      fx_to_ff(-2 * u.y, fbias[f], v.z, v.w);
+      DF[e] = v;
+    }
   }
   SweepProblem& P = a.probs_next[j];
   P.mult[lane] = (lane < nd) ? mult_s[w][lane] : 0;
@@ -567,7 +596,9 @@ __global__ void __launch_bounds__(kFinWarps * 32) gccb_finalize_kernel(FinalizeA
     P.mat_off = ls.pool_off;
     P.base_off = ls.pool_off + (int64_t)nds * nf;
     P.part_off = ls.part_off;
-    P.scale = ldexp(1.0, held ? -(nf - 1) : -nf);
+    // float pairs: the factors' scales 2^(p_f + 1 - fx) multiply the product
+    P.ff_off = a.next_ff ? ls.pool_off + (int64_t)(nds + 1) * nf : 0;
+    P.scale = ldexp(1.0, (held ? -(nf - 1) : -nf) + (a.next_ff ? esum - nf * a.fx : 0));
     P.fixed_digit = held;
     P.group = a.next_tab ? 1 : a.next_group;
   }
@@ -709,12 +740,17 @@ static int gccb_prepare(Context* cx, const double* matrix, int n_mats, int m, Dr
   std::vector<char> uniform(Lmax + 2, 0);
   std::vector<LevelSample> uni_lvl(Lmax + 2);
   std::vector<int> grp(Lmax + 2, 1);
+  std::vector<char> ffl(Lmax + 2, 0);  // level k's sweep runs on float pairs
+  for (int k = 2; k <= Lmax; ++k) ffl[k] = (g_minors_arith == 0 && minors_ff_available(k - 1)) ? 1 : 0;
   for (int k = 2; k <= Lmax; ++k) {
     const int Ak = A[k];
     const std::vector<uint64_t>& codes = lvl_codes[k];
     const std::vector<int>& ndv = lvl_nd[k];
     // k input particles: at most k distinct modes, so at most k rows of minors per thread
-    const int64_t resident = sweep_resident_minors(k - 1, std::min(k, kMaxMinorDigits), cx->sm_count);
+    const int64_t resident = sweep_resident_minors(k - 1, std::min(k, kMaxMinorDigits), cx->sm_count, ffl[k]);
+    // pool per sample: rows of D and the base sums; float pairs add the float-pair
+    // rows of the binary digits and the factors' biases
+    auto pool_units = [&](int nd_) { return (int64_t)(ffl[k] ? 2 * nd_ + 2 : nd_ + 1) * (k - 1); };
     bool same = true;
     uint64_t code0 = 1ull << (k - 1);
     int nd0 = k;
@@ -738,10 +774,10 @@ static int gccb_prepare(Context* cx, const double* matrix, int n_mats, int m, Dr
       uni_lvl[k].thread_begin = 0;
       uni_lvl[k].n_threads = tps;
       uni_lvl[k].part_off = tps * nd0;
-      uni_lvl[k].pool_off = (int64_t)(nd0 + 1) * (k - 1);  // rows and base sums
+      uni_lvl[k].pool_off = pool_units(nd0);
       lvl_threads[k] = tps * Ak;
       lvl_parts[k] = tps * nd0 * Ak;
-      lvl_pool[k] = (int64_t)(nd0 + 1) * (k - 1) * Ak;
+      lvl_pool[k] = pool_units(nd0) * Ak;
       continue;
     }
     std::vector<int64_t> nthr;
@@ -758,7 +794,7 @@ static int gccb_prepare(Context* cx, const double* matrix, int n_mats, int m, Dr
       ls.pool_off = pool;
       threads += nthr[jj];
       parts += nthr[jj] * ndv[jj];
-      pool += (int64_t)(ndv[jj] + 1) * (k - 1);
+      pool += pool_units(ndv[jj]);
       t[jj] = ls;
     }
     lvl_threads[k] = threads;
@@ -854,7 +890,7 @@ static int gccb_prepare(Context* cx, const double* matrix, int n_mats, int m, Dr
       SL.grid = (int)((lvl_threads[k] + 127) / 128);
       SL.rows = std::min(k, kMaxMinorDigits);
       if (timing) le = cudaEventRecordWithFlags(R.ev[2 * (k - 2)], s, cudaEventRecordExternal);
-      if (le == cudaSuccess) le = launch_sweep(k - 1, SweepOp::kMinors, SL, s);
+      if (le == cudaSuccess) le = launch_sweep(k - 1, ffl[k] ? SweepOp::kMinorsFF : SweepOp::kMinors, SL, s);
       if (timing && le == cudaSuccess) le = cudaEventRecordWithFlags(R.ev[2 * (k - 2) + 1], s, cudaEventRecordExternal);
       if (le != cudaSuccess) break;
       ++R.kernels;
@@ -886,6 +922,7 @@ static int gccb_prepare(Context* cx, const double* matrix, int n_mats, int m, Dr
     fa.next_tab = (k < Lmax && !uniform[k + 1]) ? (const LevelSample*)(d + o_tab[k + 1]) : nullptr;
     fa.next_uni = (k < Lmax) ? uni_lvl[k + 1] : LevelSample{};
     fa.next_group = (k < Lmax) ? grp[k + 1] : 1;
+    fa.next_ff = (k < Lmax) ? ffl[k + 1] : 0;
     fa.err = R.derr;
     gccb_finalize_kernel<<<(A[k] + kFinWarps - 1) / kFinWarps, kFinWarps * 32, 0, s>>>(fa);
     le = cudaGetLastError();
@@ -1094,6 +1131,17 @@ int boss_gccb_sample_slice(const double* matrix, int32_t m, const int32_t* input
   }
   memcpy(mt_key, mt.key, sizeof(mt.key));
   *mt_pos = mt.pos;
+  return kOk;
+}
+
+int boss_minors_arithmetic(int32_t mode, int32_t* previous) {
+  if (mode < -1 || mode > 1) {
+    set_error("all-minors arithmetic: 0 float pairs, 1 FP64, -1 query");
+    return kErrArg;
+  }
+  std::lock_guard<std::mutex> lk(g_api_mutex);
+  if (previous) *previous = g_minors_arith;
+  if (mode >= 0) g_minors_arith = mode;
   return kOk;
 }
 

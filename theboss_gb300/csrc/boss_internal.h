@@ -11,7 +11,7 @@
 
 namespace boss {
 
-enum class SweepOp { kPerm = 0, kMinors = 1, kGrad = 2 };
+enum class SweepOp { kPerm = 0, kMinors = 1, kGrad = 2, kMinorsFF = 3 };  // kMinorsFF: float pairs, nf <= 24
 
 // Everything one sweep launch needs (device pointers).
 struct SweepLaunch {
@@ -29,8 +29,11 @@ struct SweepLaunch {
 cudaError_t prepare_sweep_kernels();
 // Resident threads of one full wave of the sweep kernel for `nf` factors.
 int64_t sweep_resident_threads(int nf, SweepOp op, int sm_count);
-// Resident threads of the all-minors kernel with `rows` rows of minors per thread.
-int64_t sweep_resident_minors(int nf, int rows, int sm_count);
+// Resident threads of the all-minors kernel (FP64, or the float-pair one) with
+// `rows` rows of minors per thread.
+int64_t sweep_resident_minors(int nf, int rows, int sm_count, bool ff = false);
+// Whether the float-pair all-minors kernel exists for nf factors.
+bool minors_ff_available(int nf);
 cudaError_t launch_sweep(int nf, SweepOp op, const SweepLaunch& L, cudaStream_t st);
 cudaError_t launch_perm_reduce(const SweepProblem* probs, int n_probs, const double2* partials, double2* out,
                                cudaStream_t st);
@@ -62,7 +65,17 @@ struct HostSweep {
   int factor_mode[kMaxFactors] = {};  // factor -> mode (gradients)
   int fixed_mode = -1;                // mode of the digit held at r = 0 (Glynn halving), or -1
   bool digits_are_outputs = false;    // orientation of the sweep
+  // Float-pair all-minors: factor f's bound 2^p <= max(sum mult |Re|, sum mult |Im|) < 2^(p+1)
+  // over every digit (held one included), in fixed-point units; fx_to_ff takes 189 - p.
+  std::vector<int> fbias;
+  int ff_exp = 0;  // sum_f (p_f + 1) - nf * fx: the float-pair products' scale
 };
+
+// Arithmetic of the all-minors sweeps (boss_minors_arithmetic): 0 float pairs
+// where the kernel exists for the factor count, 1 FP64.
+extern int g_minors_arith;
+// x * 2^(fbias - 190) as a float pair, the host twin of fx_to_ff (same bits).
+void host_fx_to_ff(long long x, int fbias, float& hi, float& lo);
 
 // Status codes of the C ABI (include/boss.h repeats them).
 enum Status : int {

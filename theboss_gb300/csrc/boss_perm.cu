@@ -11,10 +11,10 @@ cudaError_t sweep_nf_a_launch(int nf, SweepOp op, const SweepLaunch& L, cudaStre
 cudaError_t sweep_nf_b_launch(int nf, SweepOp op, const SweepLaunch& L, cudaStream_t st);
 cudaError_t sweep_nf_c_launch(int nf, SweepOp op, const SweepLaunch& L, cudaStream_t st);
 cudaError_t sweep_nf_d_launch(int nf, SweepOp op, const SweepLaunch& L, cudaStream_t st);
-cudaError_t sweep_nf_a_prepare(int* perm_occ, int* minors_occ);
-cudaError_t sweep_nf_b_prepare(int* perm_occ, int* minors_occ);
-cudaError_t sweep_nf_c_prepare(int* perm_occ, int* minors_occ);
-cudaError_t sweep_nf_d_prepare(int* perm_occ, int* minors_occ);
+cudaError_t sweep_nf_a_prepare(int* perm_occ, int* minors_occ, int* ff_occ);
+cudaError_t sweep_nf_b_prepare(int* perm_occ, int* minors_occ, int* ff_occ);
+cudaError_t sweep_nf_c_prepare(int* perm_occ, int* minors_occ, int* ff_occ);
+cudaError_t sweep_nf_d_prepare(int* perm_occ, int* minors_occ, int* ff_occ);
 
 cudaError_t sweep_nf_a_grad_occupancy(int nf, int* occ);
 cudaError_t sweep_nf_b_grad_occupancy(int nf, int* occ);
@@ -22,20 +22,25 @@ cudaError_t sweep_nf_c_grad_occupancy(int nf, int* occ);
 cudaError_t sweep_nf_d_grad_occupancy(int nf, int* occ);
 
 static int g_perm_occ[kMaxFactors + 1];
-static int g_minors_occ[kMaxFactors + 1][kMaxMinorDigits + 1];  // [nf][rows of minors]
+static int g_minors_occ[kMaxFactors + 1][kMaxMinorDigits + 1];     // [nf][rows of minors]
+static int g_minors_ff_occ[kMaxFactors + 1][kMaxMinorDigits + 1];  // float-pair kernel; 0: none
 
 cudaError_t prepare_sweep_kernels() {
   cudaError_t e;
-  if ((e = sweep_nf_a_prepare(g_perm_occ + 1, &g_minors_occ[1][0])) != cudaSuccess) return e;
-  if ((e = sweep_nf_b_prepare(g_perm_occ + 9, &g_minors_occ[9][0])) != cudaSuccess) return e;
-  if ((e = sweep_nf_c_prepare(g_perm_occ + 17, &g_minors_occ[17][0])) != cudaSuccess) return e;
-  return sweep_nf_d_prepare(g_perm_occ + 25, &g_minors_occ[25][0]);
+  if ((e = sweep_nf_a_prepare(g_perm_occ + 1, &g_minors_occ[1][0], &g_minors_ff_occ[1][0])) != cudaSuccess) return e;
+  if ((e = sweep_nf_b_prepare(g_perm_occ + 9, &g_minors_occ[9][0], &g_minors_ff_occ[9][0])) != cudaSuccess) return e;
+  if ((e = sweep_nf_c_prepare(g_perm_occ + 17, &g_minors_occ[17][0], &g_minors_ff_occ[17][0])) != cudaSuccess)
+    return e;
+  return sweep_nf_d_prepare(g_perm_occ + 25, &g_minors_occ[25][0], &g_minors_ff_occ[25][0]);
 }
 
-int64_t sweep_resident_minors(int nf, int rows, int sm_count) {
+bool minors_ff_available(int nf) { return nf >= 1 && nf <= kMaxFactors && g_minors_ff_occ[nf][kMaxMinorDigits] > 0; }
+
+int64_t sweep_resident_minors(int nf, int rows, int sm_count, bool ff) {
   if (nf < 1 || nf > kMaxFactors) return 128;
   rows = std::min(std::max(rows, 1), kMaxMinorDigits);
-  return (int64_t)std::max(1, g_minors_occ[nf][rows]) * sm_count * 128;
+  const int occ = ff ? g_minors_ff_occ[nf][rows] : g_minors_occ[nf][rows];
+  return (int64_t)std::max(1, occ) * sm_count * 128;
 }
 
 int64_t sweep_resident_threads(int nf, SweepOp op, int sm_count) {

@@ -61,6 +61,8 @@ struct SweepProblem {
   int64_t mat_off;   // D: nd x nf fixed-point complex (longlong2), row-major
   int64_t base_off;  // nf fixed-point complex
   int64_t part_off;  // partials: n_threads complex (perms) or n_threads x (nd + fixed_digit) (all-minors)
+  int64_t ff_off;    // float-pair all-minors only: nb x nf rows of D as float pairs (float4: re hi, re lo,
+                     // im hi, im lo, each factor in its own scale), then nf int32 exponent biases
   double scale;      // final real scale
   int32_t fixed_digit;  // gradients, all-minors: a binary digit held at r = 0 (Glynn halving) adds a weight-1 row
   int32_t group;     // all-minors: each aligned group of `group` threads (1, 2, 4, .., 32) sums its
@@ -223,6 +225,91 @@ __device__ __forceinline__ void accumulate_product(const long long (&sr)[NF], co
   ai = fma(pr, bi, ai);
   ai = fma(pi, br, ai);
 }
+
+// ---------------------------------------------------------------------------
+// Float pairs on the FP32 pipe.  GB300 issues FP32 at 64x the FP64 rate, so the
+// float-pair all-minors sweep keeps each value as an unevaluated sum hi + lo of
+// two floats (about 47 significant bits) and uses the classical error-free
+// transformations: Knuth's two-sum, the FMA two-product and Dekker's fast
+// two-sum (T. J. Dekker, "A floating-point technique for extending the available
+// precision", Numer. Math. 18, 1971).
+// ---------------------------------------------------------------------------
+
+// x * 2^(fbias - 190) as hi + lo: the 24 leading bits of |x| in hi, the next 23
+// (truncated) in lo.  With |x| < 2^(p + 1) and fbias = 189 - p the value is below
+// 1 in magnitude and every exponent field stays in [41, 126].  Integer work only.
+__device__ __forceinline__ void fx_to_ff(long long x, int fbias, float& hi, float& lo) {
+  const unsigned long long sgn = (unsigned long long)(x >> 63);
+  const unsigned long long ax = ((unsigned long long)x ^ sgn) - sgn;
+  const int lz = __clzll((long long)ax);
+  const unsigned long long y = ax << (lz & 63);
+  const uint32_t yh = (uint32_t)(y >> 32), yl = (uint32_t)y;
+  const int ex = fbias - lz;  // exponent field of the leading bit
+  const uint32_t s32 = (uint32_t)sgn & 0x80000000u;
+  const uint32_t hb = (((uint32_t)(ex - 1)) << 23) + (yh >> 8);  // the leading bit carries into the field
+  const uint32_t nxt = __funnelshift_r(yl, yh, 17) & 0x7FFFFFu;  // bits 39..17 of y
+  const uint32_t eb = ((uint32_t)(ex - 23)) << 23;
+  const float l = __uint_as_float(eb | nxt) - __uint_as_float(eb);  // exact (Sterbenz)
+  hi = ax ? __uint_as_float(hb | s32) : 0.0f;
+  lo = ax ? __uint_as_float(__float_as_uint(l) ^ s32) : 0.0f;
+}
+
+struct ffc {  // complex float pair
+  float rh, rl, ih, il;
+};
+
+// (h, l) += sg * (bh, bl), sg = +-1: two-sum of the high parts, the low parts
+// added to its error, renormalised by a fast two-sum.
+__device__ __forceinline__ void ff_acc(float& h, float& l, float sg, float bh, float bl) {
+  const float s = fmaf(sg, bh, h);
+  const float bb = s - h;
+  const float err = (h - (s - bb)) + fmaf(sg, bh, -bb);
+  const float lo = err + fmaf(sg, bl, l);
+  h = s + lo;
+  l = lo - (h - s);
+}
+
+// p + e = a * b up to the a_lo * b_lo term (the FMA two-product of the high parts
+// plus the cross terms).  __fmul_rn: p must stay a rounded product, never fused
+// into a later add.
+__device__ __forceinline__ void ff_prod(float ah, float al, float bh, float bl, float& p, float& e) {
+  p = __fmul_rn(ah, bh);
+  e = fmaf(ah, bh, -p);
+  e = fmaf(ah, bl, e);
+  e = fmaf(al, bh, e);
+}
+
+// (p1 + e1) + sg * (p2 + e2), normalised.
+__device__ __forceinline__ void ff_combine(float p1, float e1, float sg, float p2, float e2, float& h, float& l) {
+  const float s = fmaf(sg, p2, p1);
+  const float bb = s - p1;
+  const float err = (p1 - (s - bb)) + fmaf(sg, p2, -bb);
+  const float lo = err + fmaf(sg, e2, e1);
+  h = s + lo;
+  l = lo - (h - s);
+}
+
+__device__ __forceinline__ ffc ff_cmul(const ffc& a, const ffc& b) {
+  float p1, e1, p2, e2, p3, e3, p4, e4;
+  ff_prod(a.rh, a.rl, b.rh, b.rl, p1, e1);
+  ff_prod(a.ih, a.il, b.ih, b.il, p2, e2);
+  ff_prod(a.rh, a.rl, b.ih, b.il, p3, e3);
+  ff_prod(a.ih, a.il, b.rh, b.rl, p4, e4);
+  ffc r;
+  ff_combine(p1, e1, -1.0f, p2, e2, r.rh, r.rl);
+  ff_combine(p3, e3, 1.0f, p4, e4, r.ih, r.il);
+  return r;
+}
+
+// (h, l) * (bh, bl), normalised.
+__device__ __forceinline__ void ff_mul(float& h, float& l, float bh, float bl) {
+  float p, e;
+  ff_prod(h, l, bh, bl, p, e);
+  h = p + e;
+  l = e - (h - p);
+}
+
+__device__ __forceinline__ double ff_to_double(float h, float l) { return (double)h + (double)l; }
 
 __device__ __forceinline__ double warp_sum(double v) {
   // Fixed butterfly order: every lane ends with the same, run-to-run identical sum.

@@ -194,6 +194,227 @@ __global__ void __launch_bounds__(128) minors_sweep_kernel(const SweepProblem* _
   }
 }
 
+// ---------------------------------------------------------------------------
+// Float-pair all-minors sweep: the same walk as minors_walk with every product,
+// running total and minor kept as float pairs on the FP32 pipe (boss_sweep.cuh).
+//   * Each factor f has its own scale 2^-(p_f + 1), |s_f| < 2^(p_f + 1) in
+//     fixed-point units, so every float-pair factor is below 1 in magnitude and
+//     the products neither overflow nor leave the normal range at the sizes of
+//     the sampler; the planner folds 2^(sum_f (p_f + 1) - nf fx) into the scale.
+//   * The exact 64-bit sums stay the reference, in shared memory (registers hold
+//     the float-pair sums only): every kFFResync codes (counted from the
+//     thread's first code, so the lanes of a warp resynchronise together) they
+//     are brought up to the current code by the digits that flipped since, and
+//     converted (fx_to_ff); in between the float-pair sums move by the
+//     float-pair rows of D.  The drift between two resynchronisations is a few
+//     units of 2^-47 of the rows.
+// ---------------------------------------------------------------------------
+constexpr int kFFMaxFactors = 24;  // above this the float-pair sums exhaust the registers
+constexpr uint64_t kFFResync = 8;
+
+// Decodes code t into the exact sums (shared memory, SS[f * 128]) and their
+// float pairs S.
+template <int NF>
+__device__ __forceinline__ void decode_code_ff(const SweepProblem& P, const longlong2* __restrict__ D,
+                                               const longlong2* __restrict__ base, const int* __restrict__ fb,
+                                               uint64_t t, longlong2* SS, ffc (&S)[NF], uint64_t& g,
+                                               uint32_t& parity, double& w) {
+  long long sr[NF], si[NF];
+  decode_code<NF>(P, D, base, t, sr, si, g, parity, w);
+#pragma unroll
+  for (int f = 0; f < NF; ++f) {
+    SS[f * 128] = make_longlong2(sr[f], si[f]);
+    const int b = fb[f];
+    fx_to_ff(sr[f], b, S[f].rh, S[f].rl);
+    fx_to_ff(si[f], b, S[f].ih, S[f].il);
+  }
+}
+
+// Brings the exact sums from code g_int to code g (the binary digits in which
+// they differ) and reconverts the float pairs, one factor at a time.
+template <int NF>
+__device__ __forceinline__ void resync_ff(const longlong2* __restrict__ D, const int* __restrict__ fb, uint64_t g,
+                                          uint64_t g_int, longlong2* SS, ffc (&S)[NF]) {
+  const uint64_t diff = g ^ g_int;
+#pragma unroll
+  for (int f = 0; f < NF; ++f) {
+    longlong2 v = SS[f * 128];
+    for (uint64_t dd = diff; dd; dd &= dd - 1) {
+      const int j = __ffsll((long long)dd) - 1;
+      const longlong2 d = D[(size_t)j * NF + f];
+      const long long sgn = ((g_int >> j) & 1ull) ? -1ll : 0ll;  // r_j 1 -> 0 subtracts the row
+      v.x += (d.x ^ sgn) - sgn;
+      v.y += (d.y ^ sgn) - sgn;
+    }
+    SS[f * 128] = v;
+    const int b = fb[f];
+    fx_to_ff(v.x, b, S[f].rh, S[f].rl);
+    fx_to_ff(v.y, b, S[f].ih, S[f].il);
+  }
+}
+
+// settle_minors with float pairs: every digit's row receives w_j * w * R / 2.
+template <int STRIDE>
+__device__ __forceinline__ void settle_minors_ff(const SweepProblem& P, float4* M, const ffc& R, float wh, float wl,
+                                                 uint64_t g, uint64_t t_seg) {
+  float xr = R.rh, xlr = R.rl, xi = R.ih, xli = R.il;
+  ff_mul(xr, xlr, 0.5f * wh, 0.5f * wl);  // halving is exact
+  ff_mul(xi, xli, 0.5f * wh, 0.5f * wl);
+  for (int j = 0; j < P.nb; ++j) {
+    const float sg = ((g >> j) & 1ull) ? -1.0f : 1.0f;
+    float4 v = M[j * STRIDE];
+    ff_acc(v.x, v.y, sg, xr, xlr);
+    ff_acc(v.z, v.w, sg, xi, xli);
+    M[j * STRIDE] = v;
+  }
+  for (int j = P.nb; j < P.nd; ++j) {
+    const float f = (float)((int)P.mult[j] - 2 * (int)digit_value(P, t_seg, j));  // small signed integer: exact
+    float pr, er, pi, ei;
+    ff_prod(xr, xlr, f, 0.0f, pr, er);
+    ff_prod(xi, xli, f, 0.0f, pi, ei);
+    float4 v = M[j * STRIDE];
+    ff_acc(v.x, v.y, 1.0f, pr, er);
+    ff_acc(v.z, v.w, 1.0f, pi, ei);
+    M[j * STRIDE] = v;
+  }
+  if (P.fixed_digit) {
+    float4 v = M[P.nd * STRIDE];
+    ff_acc(v.x, v.y, 1.0f, xr, xlr);
+    ff_acc(v.z, v.w, 1.0f, xi, xli);
+    M[P.nd * STRIDE] = v;
+  }
+}
+
+// One thread's part of a float-pair all-minors sweep (minors_walk's walk and
+// bookkeeping).  DF: the nb x NF float-pair rows of D; fb: the factors' exponent
+// biases for fx_to_ff; SS: this thread's exact sums (stride 128).
+template <int NF, int STRIDE>
+__device__ __forceinline__ void minors_walk_ff(const SweepProblem& P, const longlong2* __restrict__ D,
+                                               const longlong2* __restrict__ base, const float4* __restrict__ DF,
+                                               const int* __restrict__ fb, int64_t q, float4* M, longlong2* SS) {
+  const int nd = P.nd + P.fixed_digit;
+  for (int j = 0; j < nd; ++j) M[j * STRIDE] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  int64_t a, len;
+  thread_range(P, q, a, len);
+  if (len <= 0) return;
+  const int nb = P.nb;
+  const int low = nb < kSegLog ? nb : kSegLog;
+  const bool weighted = P.nd > P.nb;
+  uint64_t g, t_seg = (uint64_t)a;
+  uint32_t parity;
+  double w;
+  ffc S[NF];
+  decode_code_ff<NF>(P, D, base, fb, (uint64_t)a, SS, S, g, parity, w);
+  uint64_t g_int = g;  // the code whose exact sums SS holds
+  float wh = __double2float_rn(w), wl = __double2float_rn(w - (double)wh);
+  ffc R = {0.0f, 0.0f, 0.0f, 0.0f};
+  const uint64_t end = (uint64_t)(a + len);
+  for (uint64_t t = (uint64_t)a;;) {
+    {  // this code's product into the running total
+      ffc p = S[0];
+#pragma unroll
+      for (int f = 1; f < NF; ++f) p = ff_cmul(p, S[f]);
+      const float sg = parity ? -1.0f : 1.0f;
+      ff_acc(R.rh, R.rl, sg, p.rh, p.rl);
+      ff_acc(R.ih, R.il, sg, p.ih, p.il);
+    }
+    const uint64_t tn = t + 1;
+    if (tn >= end) break;
+    const int i = __ffsll((long long)tn) - 1;
+    bool flips = true;  // false: a multi-valued digit moves and the code is re-decoded
+    uint32_t bit = 0;
+    if (i < low) {
+      bit = (uint32_t)(g >> i) & 1u;
+      float xr = R.rh, xlr = R.rl, xi = R.ih, xli = R.il;
+      if (weighted) {
+        ff_mul(xr, xlr, wh, wl);
+        ff_mul(xi, xli, wh, wl);
+      }
+      const float sg = bit ? -1.0f : 1.0f;
+      float4 v = M[i * STRIDE];
+      ff_acc(v.x, v.y, sg, xr, xlr);
+      ff_acc(v.z, v.w, sg, xi, xli);
+      M[i * STRIDE] = v;
+    } else {
+      settle_minors_ff<STRIDE>(P, M, R, wh, wl, g, t_seg);
+      R = {0.0f, 0.0f, 0.0f, 0.0f};
+      t_seg = tn;
+      if (i < nb) bit = (uint32_t)(g >> i) & 1u;
+      else flips = false;
+    }
+    if (flips) {
+      g ^= 1ull << i;
+      parity ^= 1u;
+      if (((tn - (uint64_t)a) & (kFFResync - 1)) == 0) {
+        resync_ff<NF>(D, fb, g, g_int, SS, S);
+        g_int = g;
+      } else {
+        const float sg = bit ? -1.0f : 1.0f;  // r_i 0 -> 1 adds the row
+        const float4* row = DF + (size_t)i * NF;
+#pragma unroll
+        for (int f = 0; f < NF; ++f) {
+          if (f > 0 && (f & 7) == 0) load_fence();
+          const float4 d = row[f];
+          ff_acc(S[f].rh, S[f].rl, sg, d.x, d.y);
+          ff_acc(S[f].ih, S[f].il, sg, d.z, d.w);
+        }
+      }
+    } else {
+      decode_code_ff<NF>(P, D, base, fb, tn, SS, S, g, parity, w);
+      g_int = g;
+      wh = __double2float_rn(w);
+      wl = __double2float_rn(w - (double)wh);
+    }
+    t = tn;
+  }
+  settle_minors_ff<STRIDE>(P, M, R, wh, wl, g, t_seg);
+}
+
+// minors_sweep_kernel with float pairs (NF <= kFFMaxFactors).  The group sums
+// are float-pair sums in the same fixed order; the partials are written as
+// doubles in the factors' scales (the problem's scale carries the rest).
+template <int NF>
+__global__ void __launch_bounds__(128, 3) minors_sweep_ff_kernel(const SweepProblem* __restrict__ probs, int n_probs,
+                                                              const longlong2* __restrict__ pool, int64_t total_threads,
+                                                              double2* __restrict__ partials, int rows) {
+  extern __shared__ float4 minors_ff_smem[];
+  const int64_t gt = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (gt >= total_threads) return;
+  const SweepProblem& P = probs[find_problem(probs, n_probs, gt)];
+  const int64_t q = gt - P.thread_begin;
+  const int nd = P.nd + P.fixed_digit;
+  float4* M = minors_ff_smem + threadIdx.x;
+  // exact sums after the launch's rows of minors (the launch passes rows in blockDim-sized units)
+  longlong2* SS = reinterpret_cast<longlong2*>(minors_ff_smem + (size_t)rows * 128) + threadIdx.x;
+  const float4* DF = reinterpret_cast<const float4*>(pool + P.ff_off);
+  const int* fb = reinterpret_cast<const int*>(DF + (size_t)P.nb * NF);
+  minors_walk_ff<NF, 128>(P, pool + P.mat_off, pool + P.base_off, DF, fb, q, M, SS);
+  const int G = P.group;
+  if (G > 1) {
+    const int lane = threadIdx.x & 31;
+    const int64_t warp0 = gt - lane;
+    const unsigned live = (warp0 + 32 <= total_threads) ? 0xffffffffu : ((1u << (total_threads - warp0)) - 1u);
+    __syncwarp(live);
+    const int gl = lane & (G - 1);
+    const float4* grp = minors_ff_smem + (threadIdx.x - gl);
+    double2* out = partials + P.part_off + (q / G) * nd;
+    for (int j = gl; j < nd; j += G) {
+      float rh = 0.0f, rl = 0.0f, ih = 0.0f, il = 0.0f;
+      for (int i = 0; i < G; ++i) {
+        const float4 v = grp[j * 128 + ((i + gl) & (G - 1))];
+        ff_acc(rh, rl, 1.0f, v.x, v.y);
+        ff_acc(ih, il, 1.0f, v.z, v.w);
+      }
+      out[j] = make_double2(ff_to_double(rh, rl), ff_to_double(ih, il));
+    }
+  } else {
+    double2* out = partials + P.part_off + q * nd;
+    for (int j = 0; j < nd; ++j) {
+      const float4 v = M[j * 128];
+      out[j] = make_double2(ff_to_double(v.x, v.y), ff_to_double(v.z, v.w));
+    }
+  }
+}
 
 // Gradient sweep (Glynn / Chin-Huh kind).  With s_f the factor sums and
 // w_b = mult_b - 2 r_b the weight of digit b, d perm / d U[mode f][mode b] is
@@ -399,6 +620,16 @@ cudaError_t sweep_launch_t(SweepOp op, const SweepLaunch& L, cudaStream_t st) {
         L.probs, L.n_probs, L.pool, L.total_threads, L.partials, L.partials2);
     return cudaGetLastError();
   }
+  if (op == SweepOp::kMinorsFF) {
+    if constexpr (NF <= kFFMaxFactors) {
+      const int rows = (L.rows >= 1 && L.rows <= kMaxMinorDigits) ? L.rows : kMaxMinorDigits;
+      minors_sweep_ff_kernel<NF><<<L.grid, 128, (size_t)(rows + NF) * 128 * sizeof(float4), st>>>(
+          L.probs, L.n_probs, L.pool, L.total_threads, L.partials, rows);
+      return cudaGetLastError();
+    } else {
+      return cudaErrorInvalidValue;
+    }
+  }
   if (op == SweepOp::kPerm) {
     perm_sweep_kernel<NF><<<L.grid, 128, 0, st>>>(L.probs, L.n_probs, L.pool, L.total_threads, L.partials);
   } else {  // shared memory: the launch's rows of minors per thread, 128 threads per block
@@ -416,12 +647,25 @@ cudaError_t grad_occupancy_t(int* blocks_per_sm) {
 }
 
 // minors_blocks_per_sm[r] (r = 1..kMaxMinorDigits): blocks per SM with r rows of
-// minors per thread in shared memory.
+// minors per thread in shared memory; ff_blocks_per_sm[r] the same for the
+// float-pair kernel (left at 0 above kFFMaxFactors).
 template <int NF>
-cudaError_t sweep_prepare_t(int* perm_blocks_per_sm, int* minors_blocks_per_sm) {
+cudaError_t sweep_prepare_t(int* perm_blocks_per_sm, int* minors_blocks_per_sm, int* ff_blocks_per_sm) {
   cudaError_t e = cudaFuncSetAttribute(minors_sweep_kernel<NF>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)kMinorsSmem);
   if (e != cudaSuccess) return e;
+  if constexpr (NF <= kFFMaxFactors) {
+    e = cudaFuncSetAttribute(minors_sweep_ff_kernel<NF>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)((size_t)(kMaxMinorDigits + NF) * 128 * sizeof(float4)));
+    if (e != cudaSuccess) return e;
+    for (int r = 1; r <= kMaxMinorDigits; ++r) {
+      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(ff_blocks_per_sm + r, minors_sweep_ff_kernel<NF>, 128,
+                                                        (size_t)(r + NF) * 128 * sizeof(float4));
+      if (e != cudaSuccess) return e;
+    }
+  } else {
+    for (int r = 0; r <= kMaxMinorDigits; ++r) ff_blocks_per_sm[r] = 0;
+  }
   e = cudaFuncSetAttribute(grad_sweep_kernel<NF>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kGradSmem);
   if (e != cudaSuccess) return e;
   e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(perm_blocks_per_sm, perm_sweep_kernel<NF>, 128, 0);
@@ -465,17 +709,18 @@ cudaError_t sweep_prepare_t(int* perm_blocks_per_sm, int* minors_blocks_per_sm) 
       default: return cudaErrorInvalidValue;                                                             \
     }                                                                                                    \
   }                                                                                                      \
-  cudaError_t NAME##_prepare(int* perm_occ, int* minors_occ) { /* minors_occ: 8 rows of 33 */           \
+  cudaError_t NAME##_prepare(int* perm_occ, int* minors_occ, int* ff_occ) { /* 8 rows of 33 */        \
     cudaError_t e;                                                                                       \
     for (int k = 0; k < 8; ++k) perm_occ[k] = 1;                                                         \
     for (int k = 0; k < 8 * 33; ++k) minors_occ[k] = 1;                                                  \
-    if ((e = sweep_prepare_t<(LO) + 0>(perm_occ + 0, minors_occ + 0 * 33)) != cudaSuccess) return e;     \
-    if ((e = sweep_prepare_t<(LO) + 1>(perm_occ + 1, minors_occ + 1 * 33)) != cudaSuccess) return e;     \
-    if ((e = sweep_prepare_t<(LO) + 2>(perm_occ + 2, minors_occ + 2 * 33)) != cudaSuccess) return e;     \
-    if ((e = sweep_prepare_t<(LO) + 3>(perm_occ + 3, minors_occ + 3 * 33)) != cudaSuccess) return e;     \
-    if ((e = sweep_prepare_t<(LO) + 4>(perm_occ + 4, minors_occ + 4 * 33)) != cudaSuccess) return e;     \
-    if ((e = sweep_prepare_t<(LO) + 5>(perm_occ + 5, minors_occ + 5 * 33)) != cudaSuccess) return e;     \
-    if ((e = sweep_prepare_t<(LO) + 6>(perm_occ + 6, minors_occ + 6 * 33)) != cudaSuccess) return e;     \
-    return sweep_prepare_t<(LO) + 7>(perm_occ + 7, minors_occ + 7 * 33);                                 \
+    for (int k = 0; k < 8 * 33; ++k) ff_occ[k] = 0;                                                      \
+    if ((e = sweep_prepare_t<(LO) + 0>(perm_occ + 0, minors_occ + 0 * 33, ff_occ + 0 * 33)) != cudaSuccess) return e;     \
+    if ((e = sweep_prepare_t<(LO) + 1>(perm_occ + 1, minors_occ + 1 * 33, ff_occ + 1 * 33)) != cudaSuccess) return e;     \
+    if ((e = sweep_prepare_t<(LO) + 2>(perm_occ + 2, minors_occ + 2 * 33, ff_occ + 2 * 33)) != cudaSuccess) return e;     \
+    if ((e = sweep_prepare_t<(LO) + 3>(perm_occ + 3, minors_occ + 3 * 33, ff_occ + 3 * 33)) != cudaSuccess) return e;     \
+    if ((e = sweep_prepare_t<(LO) + 4>(perm_occ + 4, minors_occ + 4 * 33, ff_occ + 4 * 33)) != cudaSuccess) return e;     \
+    if ((e = sweep_prepare_t<(LO) + 5>(perm_occ + 5, minors_occ + 5 * 33, ff_occ + 5 * 33)) != cudaSuccess) return e;     \
+    if ((e = sweep_prepare_t<(LO) + 6>(perm_occ + 6, minors_occ + 6 * 33, ff_occ + 6 * 33)) != cudaSuccess) return e;     \
+    return sweep_prepare_t<(LO) + 7>(perm_occ + 7, minors_occ + 7 * 33, ff_occ + 7 * 33);              \
   }                                                                                                      \
   }
