@@ -211,6 +211,18 @@ __global__ void __launch_bounds__(128) minors_sweep_kernel(const SweepProblem* _
 // ---------------------------------------------------------------------------
 constexpr int kFFMaxFactors = 24;  // above this the float-pair sums exhaust the registers
 constexpr uint64_t kFFResync = 8;
+// Resident blocks of 128 threads the register allocation must allow.
+#ifndef BOSS_FF_MINB_LO
+#define BOSS_FF_MINB_LO 4
+#endif
+#ifndef BOSS_FF_MINB_HI
+#define BOSS_FF_MINB_HI 2
+#endif
+#ifndef BOSS_FF_SPLIT
+#define BOSS_FF_SPLIT 12
+#endif
+template <int NF>
+constexpr int kFFMinBlocks = NF <= BOSS_FF_SPLIT ? BOSS_FF_MINB_LO : BOSS_FF_MINB_HI;
 
 // Decodes code t into the exact sums (shared memory, SS[f * 128]) and their
 // float pairs S.
@@ -374,7 +386,7 @@ __device__ __forceinline__ void minors_walk_ff(const SweepProblem& P, const long
 // are float-pair sums in the same fixed order; the partials are written as
 // doubles in the factors' scales (the problem's scale carries the rest).
 template <int NF>
-__global__ void __launch_bounds__(128, 3) minors_sweep_ff_kernel(const SweepProblem* __restrict__ probs, int n_probs,
+__global__ void __launch_bounds__(128, kFFMinBlocks<NF>) minors_sweep_ff_kernel(const SweepProblem* __restrict__ probs, int n_probs,
                                                               const longlong2* __restrict__ pool, int64_t total_threads,
                                                               double2* __restrict__ partials, int rows) {
   extern __shared__ float4 minors_ff_smem[];
@@ -657,6 +669,9 @@ cudaError_t sweep_prepare_t(int* perm_blocks_per_sm, int* minors_blocks_per_sm, 
   if constexpr (NF <= kFFMaxFactors) {
     e = cudaFuncSetAttribute(minors_sweep_ff_kernel<NF>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)((size_t)(kMaxMinorDigits + NF) * 128 * sizeof(float4)));
+    if (e != cudaSuccess) return e;
+    e = cudaFuncSetAttribute(minors_sweep_ff_kernel<NF>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                             (int)cudaSharedmemCarveoutMaxShared);
     if (e != cudaSuccess) return e;
     for (int r = 1; r <= kMaxMinorDigits; ++r) {
       e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(ff_blocks_per_sm + r, minors_sweep_ff_kernel<NF>, 128,
