@@ -408,6 +408,37 @@ def strategies_section(seed):
     return out
 
 
+# arithmetic of the path: exact int64 fixed-point row sums, float-pair (two FP32,
+# ~47-bit) products and minors in the sweeps and the Laplace step, FP64 pmf and cdf
+DTYPE = "i64 fixed point + f32x2 float pairs (~47-bit); f64 pmf/cdf"
+
+
+def roofline(b, sweep_s, achieved, peak, peak32, traffic):
+    """The dominant kernel's roofline: the float-pair all-minors sweeps against the
+    FP32 instruction peak (their FP64-equivalent rate beside it), or the FP64
+    sweeps against the FP64 peak."""
+    common = {"traffic": traffic, "sweep_ms_per_step": sweep_s * 1e3, "flops_per_step": b["sweep_flops"],
+              "flops_note": "9k - 12 flops per Guan code at level k over the codes the Glynn-form all-minors "
+                            "sweeps walk (half of theboss's Ryser-form codes for single photons); "
+                            "ryser_form_* count theboss's codes",
+              "ryser_form_flops_per_step": b["ref_flops"],
+              "ryser_form_equivalent_tflops": b["ref_flops"] / sweep_s / 1e12}
+    if b["ff_inst"] > 0:
+        ach32 = b["ff_inst"] / sweep_s / 1e12
+        return {"bound": "fp32", "kernel": "minors_sweep_ff_kernel (all levels of a step)",
+                "achieved": ach32, "peak": peak32, "unit": "T FP32 inst/s", "frac": ach32 / peak32,
+                "peak_source": "boss_fp32_peak (independent FFMA chains), measured in this run",
+                "inst_note": "float-pair arithmetic, 57.5 nf + 6 FP32 instructions per Guan code at nf = k - 1 "
+                             "factors (38 per complex product, 22 per complex sum); integer, load and "
+                             "conversion instructions not counted",
+                "fp32_inst_per_step": b["ff_inst"],
+                "fp64_equivalent": {"achieved_tflops": achieved, "fp64_peak_tflops": peak,
+                                    "ratio_to_fp64_peak": achieved / peak}, **common}
+    return {"bound": "fp64", "kernel": "minors_sweep_kernel (all levels of a step)", "achieved": achieved,
+            "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
+            "peak_source": "boss_fp64_peak, measured in this run", **common}
+
+
 def run_ours(args, rank, world):
     from theboss_gb300 import _native
     from theboss_gb300.simulation_strategies import GCCBPlainDriver
@@ -415,6 +446,7 @@ def run_ours(args, rank, world):
 
     U, inp, w = workload(args.seed)
     peak, _ = _native.fp64_peak()
+    peak32, _ = _native.fp32_peak()
     clocks = Clocks(int(os.environ.get("LOCAL_RANK", "0")))
     np.random.seed(args.seed + rank)
     _barrier(world)
@@ -449,18 +481,10 @@ def run_ours(args, rank, world):
            "h2d_bytes_per_step": b["h2d_bytes"], "d2h_bytes_per_step": b["d2h_bytes"]}
     line = {"metric": METRIC, "value": value, "unit": "samples/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded Haar unitary)",
+            "scaling": "weak", "vs_baseline": None, "dtype": DTYPE, "data": "synthetic (seeded Haar unitary)",
             "config": config(args), "clocks": clk, "e2e": e2e,
             "gpu_launches": b["kernels"] * args.steps,
-            "roofline": {"bound": "fp64", "kernel": "minors_sweep_kernel (all levels of a step)",
-                         "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
-                         "traffic": traffic, "peak_source": "boss_fp64_peak, measured in this run",
-                         "sweep_ms_per_step": sweep_s * 1e3, "flops_per_step": b["sweep_flops"],
-                         "flops_note": "9k - 12 flops per Guan code at level k over the codes the Glynn-form "
-                                       "all-minors sweeps walk (half of theboss's Ryser-form codes for single "
-                                       "photons); ryser_form_* count theboss's codes",
-                         "ryser_form_flops_per_step": b["ref_flops"],
-                         "ryser_form_equivalent_tflops": b["ref_flops"] / sweep_s / 1e12},
+            "roofline": roofline(b, sweep_s, achieved, peak, peak32, traffic),
             "wall_s_device_section": t_wall}
     if rank == 0 and not args.quick:
         # theboss's per-step loop with the GPU all-minors calculator, bounded sample

@@ -186,8 +186,12 @@ BOSS_API int boss_minors_arithmetic(int32_t mode, int32_t* previous);
  * on the library stream.  info[0..6] = flops of the sweeps per run (9k - 12 per
  * Guan code at level k, over the codes the Glynn-form sweeps walk), H2D bytes and
  * D2H bytes of one boss_gccb_sample call, kernels per run, sweep launches per
- * run, the deepest level, and the same flop count over theboss's Ryser-form codes
- * (twice as many for single photons).  info must hold 8 doubles.  samples
+ * run, the deepest level, the same flop count over theboss's Ryser-form codes
+ * (twice as many for single photons), and the FP32 instructions per run of the
+ * float-pair sweeps (57.5 nf + 6 per code at nf factors: nf - 1 float-pair
+ * complex products of 38, two complex float-pair sums of 22 for the running
+ * total and a minor, 7/8 of the codes 22 per factor to move the sums; 0 when the
+ * sweeps run in FP64).  info must hold 8 doubles.  samples
  * (optional) receives the last run's samples.  No reference counterpart.
  */
 BOSS_API int boss_gccb_bench(const double* matrix, int32_t m, const int32_t* input_state,
@@ -228,6 +232,14 @@ BOSS_API int boss_perm_batch_noalloc(const double* matrix, int32_t m, const int3
  * time.  No reference counterpart: it is the denominator of the FP64 roofline.
  */
 BOSS_API int boss_fp64_peak(double* tflops, double* milliseconds);
+
+/*
+ * FP32 FMA instruction throughput of the current device (10^12 lane
+ * instructions per second) from a stream of independent FFMA chains: the
+ * denominator of the float-pair kernels' FP32 roofline.  No reference
+ * counterpart.
+ */
+BOSS_API int boss_fp32_peak(double* tinst, double* milliseconds);
 
 /*
  * Exact probability of each outcome after particle losses, with l = sum(outcome)

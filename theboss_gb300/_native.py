@@ -64,6 +64,8 @@ def load() -> ctypes.CDLL:
         L.boss_perm_grad_batch.argtypes = [dp, ctypes.c_int32, ip, ip, ctypes.c_int32, ctypes.c_int32, dp, dp]
         L.boss_fp64_peak.restype = ctypes.c_int
         L.boss_fp64_peak.argtypes = [dp, dp]
+        L.boss_fp32_peak.restype = ctypes.c_int
+        L.boss_fp32_peak.argtypes = [dp, dp]
         up = ctypes.POINTER(ctypes.c_uint32)
         L.boss_gccb_predraw.restype = ctypes.c_int
         L.boss_gccb_predraw.argtypes = [ip, ctypes.c_int32, dp, ctypes.c_int32, up, ip, ctypes.c_int32, ip, ip, dp]
@@ -345,6 +347,14 @@ def minors_arithmetic(mode: int = -1) -> int:
     return int(prev[0])
 
 
+def fp32_peak():
+    """(T FP32 FMA instructions/s, ms) of an FFMA stream on the current device."""
+    t = np.zeros(1)
+    ms = np.zeros(1)
+    check(load().boss_fp32_peak(_dp(t), _dp(ms)))
+    return float(t[0]), float(ms[0])
+
+
 def select_device(device: int) -> None:
     check(load().boss_select_device(int(device)))
 
@@ -436,7 +446,7 @@ def gccb_bench(U: np.ndarray, input_state, weights, n_samples: int, warmup: int,
     _set_mt(st, key, pos)
     return dict(step_ms=step_ms, sweep_ms=sweep_ms, sweep_flops=float(info[0]), h2d_bytes=int(info[1]),
                 d2h_bytes=int(info[2]), kernels=int(info[3]), sweeps=int(info[4]), levels=int(info[5]),
-                ref_flops=float(info[6]), samples=samples)
+                ref_flops=float(info[6]), ff_inst=float(info[7]), samples=samples)
 
 
 def perm_bench(U: np.ndarray, S: np.ndarray, T: np.ndarray, variant: int, warmup: int, steps: int,

@@ -227,6 +227,7 @@ struct FinalizeArgs {
   int fx;      // fixed-point fraction bits of the sweep rows
   const double2* U;       // m x m
   const longlong2* Ufx;   // m x m, U * 2^fx rounded
+  const float4* Uff;      // m x m transposed, Uff[i * m + o] = U[o][i] as float pairs (re hi, re lo, im hi, im lo)
   uint8_t* S;             // [sample][m] current input occupations
   uint8_t* T;             // [sample][m] output occupations
   const uint8_t* idx;     // [sample][n] randint results (position among the particles left)
@@ -279,6 +280,7 @@ __device__ __forceinline__ int pop_particle(uint32_t* rem, int r) {
 
 __global__ void __launch_bounds__(kFinWarps * 32) gccb_finalize_kernel(FinalizeArgs a) {
   __shared__ double2 sub_s[kFinWarps][32];
+  __shared__ float4 subf_s[kFinWarps][32];
   __shared__ uint8_t dm_s[kFinWarps][32];
   __shared__ uint8_t mult_s[kFinWarps][32];
   __shared__ uint8_t fm_s[kFinWarps][32];
@@ -342,22 +344,33 @@ __global__ void __launch_bounds__(kFinWarps * 32) gccb_finalize_kernel(FinalizeA
       mult_s[w][lane] = P.mult[lane];
     }
   }
+  if (lane < nd) {
+    const double2 v = sub_s[w][lane];
+    float4 f;
+    double_to_ff(v.x, f.x, f.y);
+    double_to_ff(v.y, f.z, f.w);
+    subf_s[w][lane] = f;
+  }
   __syncwarp();
   // Laplace expansion perm(T + e_o) = sum_i S_i sub_i U[o][i]
   // (generalized_cliffords_b_simulation_strategy.py:82-89), then |.|^2.  The
-  // Glynn-form sweep already delivers S_i sub_i.
-  // FP64 instructions cost the same whatever the number of active lanes, so the
+  // Glynn-form sweep already delivers S_i sub_i.  The dot products run on the
+  // FP32 pipe as compensated float-pair sums (lane o reads column o of the
+  // transposed float-pair matrix: coalesced); |.|^2 and the cdf are FP64.  The
   // outputs that do not fill a warp split their digits over several lanes.
+  const float4* UT = a.Uff + (size_t)j * a.mstride;
   const int full = m & ~31;
   for (int o = lane; o < full; o += 32) {
-    double re = 0.0, im = 0.0;
-    const double2* Urow = Us + (size_t)o * m;
+    float sr = 0.0f, cr = 0.0f, si = 0.0f, ci = 0.0f;
     for (int d = 0; d < nd; ++d) {
-      const double2 c = sub_s[w][d];
-      const double2 u = Urow[dm_s[w][d]];
-      re = fma(c.x, u.x, fma(-c.y, u.y, re));
-      im = fma(c.x, u.y, fma(c.y, u.x, im));
+      const float4 c = subf_s[w][d];
+      const float4 u = UT[(size_t)dm_s[w][d] * m + o];
+      ff_dot_acc(sr, cr, 1.0f, c.x, c.y, u.x, u.y);
+      ff_dot_acc(sr, cr, -1.0f, c.z, c.w, u.z, u.w);
+      ff_dot_acc(si, ci, 1.0f, c.x, c.y, u.z, u.w);
+      ff_dot_acc(si, ci, 1.0f, c.z, c.w, u.x, u.y);
     }
+    const double re = ff_to_double(sr, cr), im = ff_to_double(si, ci);
     pmf_s[w][o] = fma(re, re, im * im);
   }
   if (m > full) {
@@ -367,13 +380,17 @@ __global__ void __launch_bounds__(kFinWarps * 32) gccb_finalize_kernel(FinalizeA
     const int oi = lane / s, c0 = lane & (s - 1);
     double re = 0.0, im = 0.0;
     if (oi < r) {
-      const double2* Urow = Us + (size_t)(full + oi) * m;
+      float sr = 0.0f, cr = 0.0f, si = 0.0f, ci = 0.0f;
       for (int d = c0; d < nd; d += s) {
-        const double2 c = sub_s[w][d];
-        const double2 u = Urow[dm_s[w][d]];
-        re = fma(c.x, u.x, fma(-c.y, u.y, re));
-        im = fma(c.x, u.y, fma(c.y, u.x, im));
+        const float4 c = subf_s[w][d];
+        const float4 u = UT[(size_t)dm_s[w][d] * m + full + oi];
+        ff_dot_acc(sr, cr, 1.0f, c.x, c.y, u.x, u.y);
+        ff_dot_acc(sr, cr, -1.0f, c.z, c.w, u.z, u.w);
+        ff_dot_acc(si, ci, 1.0f, c.x, c.y, u.z, u.w);
+        ff_dot_acc(si, ci, 1.0f, c.z, c.w, u.x, u.y);
       }
+      re = ff_to_double(sr, cr);
+      im = ff_to_double(si, ci);
     }
     for (int off = s >> 1; off > 0; off >>= 1) {
       re += __shfl_xor_sync(0xffffffffu, re, off);
@@ -617,6 +634,7 @@ struct GccbRun {
   int kernels = 0, sweeps = 0;
   double sweep_flops = 0.0;  // flops of all sweep launches (the Glynn form's codes)
   double ref_flops = 0.0;    // the same count over theboss's Ryser-form codes
+  double ff_inst = 0.0;      // FP32 instructions of the float-pair sweeps (model count per code)
   std::vector<cudaEvent_t> ev;  // 2 per sweep level when timing
 };
 // Two independent slots (device buffers cx->gccb[8 slot .. 8 slot + 7], a pinned
@@ -643,6 +661,20 @@ static int ensure_slot_pinned(int slot, size_t bytes) {
 static void destroy_events(GccbRun& R) {
   for (auto e : R.ev) cudaEventDestroy(e);
   R.ev.clear();
+}
+
+// out[mat][i][o] = U[mat][o][i] as float pairs (the Laplace step's coalesced layout).
+__global__ void to_ff_transposed_kernel(const double2* __restrict__ U, float4* __restrict__ out, int m, int64_t count) {
+  const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= count) return;
+  const int64_t mm = (int64_t)m * m;
+  const int64_t mat = idx / mm, r = idx - mat * mm;
+  const int o = (int)(r / m), i = (int)(r - (int64_t)o * m);
+  const double2 v = U[idx];
+  float4 f;
+  double_to_ff(v.x, f.x, f.y);
+  double_to_ff(v.y, f.z, f.w);
+  out[mat * mm + (int64_t)i * m + o] = f;
 }
 
 __global__ void to_fixed_kernel(const double* __restrict__ x, long long* __restrict__ y, int64_t count, int fx) {
@@ -700,12 +732,18 @@ static int gccb_prepare(Context* cx, const double* matrix, int n_mats, int m, Dr
   // count by (occ_a + 2) / (occ_a + 1).
   std::vector<std::vector<uint64_t>> lvl_codes(Lmax + 2);
   std::vector<std::vector<int>> lvl_nd(Lmax + 2);
+  std::vector<char> ffl(Lmax + 2, 0);  // level k's sweep runs on float pairs
+  for (int k = 2; k <= Lmax; ++k) ffl[k] = (g_minors_arith == 0 && minors_ff_available(k - 1)) ? 1 : 0;
+  // FP32 instructions per code of a float-pair sweep with nf = k - 1 factors
+  auto ff_per_code = [&](int k) { return ffl[k] ? 57.5 * (k - 1) + 6.0 : 0.0; };
   R.sweep_flops = 0.0;
   R.ref_flops = 0.0;
+  R.ff_inst = 0.0;
   if (!D.binned) {
     for (int k = 2; k <= Lmax; ++k) {
       R.sweep_flops += (double)A[k] * std::ldexp(9.0 * k - 12.0, k - 1);
       R.ref_flops += (double)A[k] * std::ldexp(9.0 * k - 12.0, k);
+      R.ff_inst += (double)A[k] * std::ldexp(ff_per_code(k), k - 1);
     }
   } else {
     for (int k = 2; k <= Lmax; ++k) {
@@ -731,6 +769,7 @@ static int gccb_prepare(Context* cx, const double* matrix, int n_mats, int m, Dr
           // products, one sign, k/2 real-weighted adds = 9k - 12; theboss's Ryser
           // form sweeps c codes, the Glynn form cg
           R.sweep_flops += (double)cg * (9.0 * k - 12.0);
+          R.ff_inst += (double)cg * ff_per_code(k);
           R.ref_flops += (double)c * (9.0 * k - 12.0);
         }
       }
@@ -740,8 +779,6 @@ static int gccb_prepare(Context* cx, const double* matrix, int n_mats, int m, Dr
   std::vector<char> uniform(Lmax + 2, 0);
   std::vector<LevelSample> uni_lvl(Lmax + 2);
   std::vector<int> grp(Lmax + 2, 1);
-  std::vector<char> ffl(Lmax + 2, 0);  // level k's sweep runs on float pairs
-  for (int k = 2; k <= Lmax; ++k) ffl[k] = (g_minors_arith == 0 && minors_ff_available(k - 1)) ? 1 : 0;
   for (int k = 2; k <= Lmax; ++k) {
     const int Ak = A[k];
     const std::vector<uint64_t>& codes = lvl_codes[k];
@@ -828,7 +865,7 @@ static int gccb_prepare(Context* cx, const double* matrix, int n_mats, int m, Dr
   if ((st = ensure(B[4], sizeof(longlong2) * (size_t)max_pool * 2 + 512))) return st;  // rows x2
   if ((st = ensure(B[5], sizeof(double2) * (size_t)max_parts))) return st;            // partials
   if ((st = ensure(B[6], sizeof(uint32_t) * 8 * (size_t)N))) return st;                // particles left
-  if ((st = ensure(B[7], sizeof(longlong2) * (size_t)m * m * n_mats))) return st;      // U fixed point
+  if ((st = ensure(B[7], 32 * (size_t)m * m * n_mats))) return st;  // U fixed point | U^T float pairs
   if ((st = ensure_slot_pinned(slot, std::max(arena, al((size_t)N * m) + 256)))) return st;
   char* h = (char*)g_gccb_pinned[slot];
   memset(h, 0, o_idx);
@@ -859,10 +896,14 @@ static int gccb_prepare(Context* cx, const double* matrix, int n_mats, int m, Dr
   cudaError_t e = cudaMemcpyAsync(d, h, arena, cudaMemcpyHostToDevice, s);
   if (e != cudaSuccess) return fail_cuda(e, "H2D sampler arena");
   longlong2* dUfx = (longlong2*)B[7].ptr;
+  float4* dUff = (float4*)(dUfx + mm * n_mats);
   {
     const int64_t cnt = (int64_t)2 * mm * n_mats;
     to_fixed_kernel<<<(unsigned)((cnt + 255) / 256), 256, 0, s>>>((const double*)(d + o_U), (long long*)dUfx, cnt, fx);
     if ((e = cudaGetLastError()) != cudaSuccess) return fail_cuda(e, "fixed-point matrices");
+    const int64_t cnt2 = (int64_t)mm * n_mats;
+    to_ff_transposed_kernel<<<(unsigned)((cnt2 + 255) / 256), 256, 0, s>>>((const double2*)(d + o_U), dUff, m, cnt2);
+    if ((e = cudaGetLastError()) != cudaSuccess) return fail_cuda(e, "float-pair matrices");
   }
   destroy_events(R);
   if (timing) {
@@ -905,6 +946,7 @@ static int gccb_prepare(Context* cx, const double* matrix, int n_mats, int m, Dr
     fa.fx = fx;
     fa.U = (const double2*)(d + o_U);
     fa.Ufx = dUfx;
+    fa.Uff = dUff;
     fa.mstride = (n_mats > 1) ? (int64_t)mm : 0;
     fa.npart = (const uint8_t*)(d + o_np);
     fa.S = dS;
@@ -1225,6 +1267,7 @@ int boss_gccb_bench(const double* matrix, int32_t m, const int32_t* input_state,
   if (st) return st;
   info[0] = R.sweep_flops;
   info[6] = R.ref_flops;
+  info[7] = R.ff_inst;
   info[1] = (double)R.h2d_bytes;
   info[2] = (double)R.d2h_bytes;
   info[3] = (double)R.kernels;

@@ -311,6 +311,25 @@ __device__ __forceinline__ void ff_mul(float& h, float& l, float bh, float bl) {
 
 __device__ __forceinline__ double ff_to_double(float h, float l) { return (double)h + (double)l; }
 
+// x as a float pair (hi = x rounded to float, lo = the rest rounded): 48 bits.
+__device__ __forceinline__ void double_to_ff(double x, float& hi, float& lo) {
+  hi = __double2float_rn(x);
+  lo = __double2float_rn(x - (double)hi);
+}
+
+// Compensated dot-product step (Ogita, Rump and Oishi, "Accurate sum and dot
+// product", SIAM J. Sci. Comput. 26, 2005): s + c accumulates sg * a * b for
+// float pairs a, b, the products' errors and the sums' errors collected in c.
+__device__ __forceinline__ void ff_dot_acc(float& s, float& c, float sg, float ah, float al, float bh, float bl) {
+  float p, e;
+  ff_prod(ah, al, bh, bl, p, e);
+  const float t = fmaf(sg, p, s);
+  const float bb = t - s;
+  const float q = (s - (t - bb)) + fmaf(sg, p, -bb);
+  c += fmaf(sg, e, q);
+  s = t;
+}
+
 __device__ __forceinline__ double warp_sum(double v) {
   // Fixed butterfly order: every lane ends with the same, run-to-run identical sum.
 #pragma unroll
