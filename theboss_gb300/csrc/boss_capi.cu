@@ -197,7 +197,7 @@ static int sweeps_launch(Context* cx, const SweepBatch& B, cudaEvent_t after_swe
   cudaError_t e = launch_sweep(B.nf, op, B.L, cx->stream);
   if (e != cudaSuccess) return fail_cuda(e, "sweep launch");
   if (after_sweep) cudaEventRecord(after_sweep, cx->stream);
-  e = B.minors ? launch_minors_reduce(B.L.probs, B.n, B.L.partials, (double2*)cx->out.ptr, B.nd_max, cx->stream)
+  e = B.minors ? launch_minors_reduce(B.L.probs, B.n, B.L.partials, (double2*)cx->out.ptr, B.nd_max, cx->stream, B.ff)
                : launch_perm_reduce(B.L.probs, B.n, B.L.partials, (double2*)cx->out.ptr, cx->stream);
   return e == cudaSuccess ? kOk : fail_cuda(e, "reduce launch");
 }

@@ -246,6 +246,7 @@ struct FinalizeArgs {
   LevelSample next_uni;         // uniform next level: n_codes, threads per sample and the per-sample
                                 // strides of partials (part_off) and rows (pool_off)
   int next_group;               // uniform next level: threads per summed group of minors
+  int cur_ff;                   // this level's sweep ran on float pairs: its partials are float4
   int next_ff;                  // the next level's sweep runs on float pairs (float-pair rows, biases)
   int* err;
 };
@@ -316,7 +317,40 @@ __global__ void __launch_bounds__(kFinWarps * 32) gccb_finalize_kernel(FinalizeA
     const SweepProblem& P = a.probs_cur[j];
     nd = P.nd + P.fixed_digit;  // the held (halved) digit's minor is the last row
     const int64_t parts = P.n_threads / P.group;
-    if (parts <= 64) {  // lane d sums digit d's partials
+    if (a.cur_ff) {
+      // float-pair partials: summed as float pairs in a fixed order, scaled by the
+      // problem's power of two (exact in float at these sizes)
+      const float4* fp = reinterpret_cast<const float4*>(a.partials) + P.part_off;
+      const float sc = __double2float_rn(P.scale);
+      if (parts <= 64) {
+        if (lane < nd) {
+          float rh = 0.0f, rl = 0.0f, ih = 0.0f, il = 0.0f;
+          for (int64_t q = 0; q < parts; ++q) {
+            const float4 v = fp[q * nd + lane];
+            ff_acc(rh, rl, 1.0f, v.x, v.y);
+            ff_acc(ih, il, 1.0f, v.z, v.w);
+          }
+          subf_s[w][lane] = make_float4(rh * sc, rl * sc, ih * sc, il * sc);
+        }
+      } else {
+        for (int d = 0; d < nd; ++d) {
+          float rh = 0.0f, rl = 0.0f, ih = 0.0f, il = 0.0f;
+          for (int64_t q = lane; q < parts; q += 32) {
+            const float4 v = fp[q * nd + d];
+            ff_acc(rh, rl, 1.0f, v.x, v.y);
+            ff_acc(ih, il, 1.0f, v.z, v.w);
+          }
+#pragma unroll
+          for (int off = 16; off > 0; off >>= 1) {  // fixed butterfly order
+            const float orh = __shfl_xor_sync(0xffffffffu, rh, off), orl = __shfl_xor_sync(0xffffffffu, rl, off);
+            const float oih = __shfl_xor_sync(0xffffffffu, ih, off), oil = __shfl_xor_sync(0xffffffffu, il, off);
+            ff_acc(rh, rl, 1.0f, orh, orl);
+            ff_acc(ih, il, 1.0f, oih, oil);
+          }
+          if (lane == d) subf_s[w][d] = make_float4(rh * sc, rl * sc, ih * sc, il * sc);
+        }
+      }
+    } else if (parts <= 64) {  // lane d sums digit d's partials
       if (lane < nd) {
         double sx = 0.0, sy = 0.0;
         for (int64_t q = 0; q < parts; ++q) {
@@ -344,7 +378,7 @@ __global__ void __launch_bounds__(kFinWarps * 32) gccb_finalize_kernel(FinalizeA
       mult_s[w][lane] = P.mult[lane];
     }
   }
-  if (lane < nd) {
+  if (!(a.k > 1 && a.cur_ff) && lane < nd) {  // FP64 minors to float pairs
     const double2 v = sub_s[w][lane];
     float4 f;
     double_to_ff(v.x, f.x, f.y);
@@ -370,17 +404,15 @@ __global__ void __launch_bounds__(kFinWarps * 32) gccb_finalize_kernel(FinalizeA
       ff_dot_acc(si, ci, 1.0f, c.x, c.y, u.z, u.w);
       ff_dot_acc(si, ci, 1.0f, c.z, c.w, u.x, u.y);
     }
-    const double re = ff_to_double(sr, cr), im = ff_to_double(si, ci);
-    pmf_s[w][o] = fma(re, re, im * im);
+    pmf_s[w][o] = ff_abs2(sr, cr, si, ci);
   }
   if (m > full) {
     const int r = m - full;
     int s = 1;  // lanes per remaining output (a power of two, r * s <= 32)
     while (r * (s << 1) <= 32) s <<= 1;
     const int oi = lane / s, c0 = lane & (s - 1);
-    double re = 0.0, im = 0.0;
+    float sr = 0.0f, cr = 0.0f, si = 0.0f, ci = 0.0f;
     if (oi < r) {
-      float sr = 0.0f, cr = 0.0f, si = 0.0f, ci = 0.0f;
       for (int d = c0; d < nd; d += s) {
         const float4 c = subf_s[w][d];
         const float4 u = UT[(size_t)dm_s[w][d] * m + full + oi];
@@ -389,14 +421,14 @@ __global__ void __launch_bounds__(kFinWarps * 32) gccb_finalize_kernel(FinalizeA
         ff_dot_acc(si, ci, 1.0f, c.x, c.y, u.z, u.w);
         ff_dot_acc(si, ci, 1.0f, c.z, c.w, u.x, u.y);
       }
-      re = ff_to_double(sr, cr);
-      im = ff_to_double(si, ci);
     }
-    for (int off = s >> 1; off > 0; off >>= 1) {
-      re += __shfl_xor_sync(0xffffffffu, re, off);
-      im += __shfl_xor_sync(0xffffffffu, im, off);
+    for (int off = s >> 1; off > 0; off >>= 1) {  // fixed butterfly order over the output's lanes
+      const float osr = __shfl_xor_sync(0xffffffffu, sr, off), ocr = __shfl_xor_sync(0xffffffffu, cr, off);
+      const float osi = __shfl_xor_sync(0xffffffffu, si, off), oci = __shfl_xor_sync(0xffffffffu, ci, off);
+      ff_acc(sr, cr, 1.0f, osr, ocr);
+      ff_acc(si, ci, 1.0f, osi, oci);
     }
-    if (oi < r && c0 == 0) pmf_s[w][full + oi] = fma(re, re, im * im);
+    if (oi < r && c0 == 0) pmf_s[w][full + oi] = ff_abs2(sr, cr, si, ci);
   }
   __syncwarp();
   // theboss normalises with Python's sequential sum, and numpy.random.choice then
@@ -965,6 +997,7 @@ static int gccb_prepare(Context* cx, const double* matrix, int n_mats, int m, Dr
     fa.next_uni = (k < Lmax) ? uni_lvl[k + 1] : LevelSample{};
     fa.next_group = (k < Lmax) ? grp[k + 1] : 1;
     fa.next_ff = (k < Lmax) ? ffl[k + 1] : 0;
+    fa.cur_ff = (k >= 2) ? ffl[k] : 0;
     fa.err = R.derr;
     gccb_finalize_kernel<<<(A[k] + kFinWarps - 1) / kFinWarps, kFinWarps * 32, 0, s>>>(fa);
     le = cudaGetLastError();

@@ -40,7 +40,7 @@ cudaError_t launch_perm_reduce(const SweepProblem* probs, int n_probs, const dou
 cudaError_t launch_grad_reduce(const SweepProblem* probs, int n_probs, const double2* gpart, const double2* ppart,
                                double2* grad_out, double2* perm_out, int row_stride, cudaStream_t st);
 cudaError_t launch_minors_reduce(const SweepProblem* probs, int n_probs, const double2* partials, double2* out,
-                                 int nd_max, cudaStream_t st);
+                                 int nd_max, cudaStream_t st, bool ff = false);
 
 // Splits `n_codes` codes over at most `resident` threads, proportionally, at
 // least one thread per sweep and at least kMinCodesPerThread codes per thread.

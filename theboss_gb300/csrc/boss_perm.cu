@@ -113,15 +113,22 @@ __global__ void perm_reduce_kernel(const SweepProblem* __restrict__ probs, const
 
 // One block per all-minors sweep; digit by digit, a fixed-order tree sum over the
 // threads' partials.
+// ff: the partials are float pairs (float4), as the float-pair sweep writes them.
 __global__ void minors_reduce_kernel(const SweepProblem* __restrict__ probs, const double2* __restrict__ partials,
-                                     double2* __restrict__ out, int nd_max) {
+                                     double2* __restrict__ out, int nd_max, int ff) {
   __shared__ double sr[256], si[256];
   const SweepProblem& P = probs[blockIdx.x];
   const int nd = P.nd + P.fixed_digit;  // the held digit's row last
   for (int j = 0; j < nd; ++j) {
     double ar = 0.0, ai = 0.0;
     for (int64_t q = threadIdx.x; q < P.n_threads; q += blockDim.x) {
-      const double2 v = partials[P.part_off + q * nd + j];
+      double2 v;
+      if (ff) {
+        const float4 f = reinterpret_cast<const float4*>(partials)[P.part_off + q * nd + j];
+        v = make_double2(ff_to_double(f.x, f.y), ff_to_double(f.z, f.w));
+      } else {
+        v = partials[P.part_off + q * nd + j];
+      }
       ar += v.x;
       ai += v.y;
     }
@@ -193,9 +200,9 @@ cudaError_t launch_perm_reduce(const SweepProblem* probs, int n_probs, const dou
 }
 
 cudaError_t launch_minors_reduce(const SweepProblem* probs, int n_probs, const double2* partials, double2* out,
-                                 int nd_max, cudaStream_t st) {
+                                 int nd_max, cudaStream_t st, bool ff) {
   if (n_probs <= 0) return cudaSuccess;
-  minors_reduce_kernel<<<n_probs, 256, 0, st>>>(probs, partials, out, nd_max);
+  minors_reduce_kernel<<<n_probs, 256, 0, st>>>(probs, partials, out, nd_max, ff ? 1 : 0);
   return cudaGetLastError();
 }
 

@@ -384,7 +384,8 @@ __device__ __forceinline__ void minors_walk_ff(const SweepProblem& P, const long
 
 // minors_sweep_kernel with float pairs (NF <= kFFMaxFactors).  The group sums
 // are float-pair sums in the same fixed order; the partials are written as
-// doubles in the factors' scales (the problem's scale carries the rest).
+// float pairs (float4: re hi, re lo, im hi, im lo) in the factors' scales (the
+// problem's scale carries the rest).
 template <int NF>
 __global__ void __launch_bounds__(128, kFFMinBlocks<NF>) minors_sweep_ff_kernel(const SweepProblem* __restrict__ probs, int n_probs,
                                                               const longlong2* __restrict__ pool, int64_t total_threads,
@@ -409,7 +410,7 @@ __global__ void __launch_bounds__(128, kFFMinBlocks<NF>) minors_sweep_ff_kernel(
     __syncwarp(live);
     const int gl = lane & (G - 1);
     const float4* grp = minors_ff_smem + (threadIdx.x - gl);
-    double2* out = partials + P.part_off + (q / G) * nd;
+    float4* out = reinterpret_cast<float4*>(partials) + P.part_off + (q / G) * nd;
     for (int j = gl; j < nd; j += G) {
       float rh = 0.0f, rl = 0.0f, ih = 0.0f, il = 0.0f;
       for (int i = 0; i < G; ++i) {
@@ -417,14 +418,11 @@ __global__ void __launch_bounds__(128, kFFMinBlocks<NF>) minors_sweep_ff_kernel(
         ff_acc(rh, rl, 1.0f, v.x, v.y);
         ff_acc(ih, il, 1.0f, v.z, v.w);
       }
-      out[j] = make_double2(ff_to_double(rh, rl), ff_to_double(ih, il));
+      out[j] = make_float4(rh, rl, ih, il);
     }
   } else {
-    double2* out = partials + P.part_off + q * nd;
-    for (int j = 0; j < nd; ++j) {
-      const float4 v = M[j * 128];
-      out[j] = make_double2(ff_to_double(v.x, v.y), ff_to_double(v.z, v.w));
-    }
+    float4* out = reinterpret_cast<float4*>(partials) + P.part_off + q * nd;
+    for (int j = 0; j < nd; ++j) out[j] = M[j * 128];
   }
 }
 
