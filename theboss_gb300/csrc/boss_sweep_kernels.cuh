@@ -325,10 +325,10 @@ __device__ __forceinline__ void minors_walk_ff(const SweepProblem& P, const long
     {  // this code's product into the running total
       ffc p = S[0];
 #pragma unroll
-      for (int f = 1; f < NF; ++f) p = ff_cmul(p, S[f]);
+      for (int f = 1; f < NF; ++f) p = ff_cmul_lazy(p, S[f]);
       const float sg = parity ? -1.0f : 1.0f;
-      ff_acc(R.rh, R.rl, sg, p.rh, p.rl);
-      ff_acc(R.ih, R.il, sg, p.ih, p.il);
+      ff_add_lazy(R.rh, R.rl, sg, p.rh, p.rl);
+      ff_add_lazy(R.ih, R.il, sg, p.ih, p.il);
     }
     const uint64_t tn = t + 1;
     if (tn >= end) break;
@@ -344,8 +344,8 @@ __device__ __forceinline__ void minors_walk_ff(const SweepProblem& P, const long
       }
       const float sg = bit ? -1.0f : 1.0f;
       float4 v = M[i * STRIDE];
-      ff_acc(v.x, v.y, sg, xr, xlr);
-      ff_acc(v.z, v.w, sg, xi, xli);
+      ff_add_lazy(v.x, v.y, sg, xr, xlr);
+      ff_add_lazy(v.z, v.w, sg, xi, xli);
       M[i * STRIDE] = v;
     } else {
       settle_minors_ff<STRIDE>(P, M, R, wh, wl, g, t_seg);
@@ -367,8 +367,8 @@ __device__ __forceinline__ void minors_walk_ff(const SweepProblem& P, const long
         for (int f = 0; f < NF; ++f) {
           if (f > 0 && (f & 7) == 0) load_fence();
           const float4 d = row[f];
-          ff_acc(S[f].rh, S[f].rl, sg, d.x, d.y);
-          ff_acc(S[f].ih, S[f].il, sg, d.z, d.w);
+          ff_add_lazy(S[f].rh, S[f].rl, sg, d.x, d.y);
+          ff_add_lazy(S[f].ih, S[f].il, sg, d.z, d.w);
         }
       }
     } else {
