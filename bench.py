@@ -213,7 +213,7 @@ def c2_patterns(n, count, seed):
     return np.array(out, dtype=np.int32)
 
 
-def single_permanents(peak_tflops, seed):
+def single_permanents(peak_tflops, seed, peak32=None):
     """C2: 64 Glynn permanents per size, device-timed; the relative error of the
     first pattern against the double-double oracle for n <= 24 (its CPU cost grows
     as 2^n: 7 s at n = 24 on 16 Arm cores, 170 s at n = 28)."""
@@ -232,6 +232,10 @@ def single_permanents(peak_tflops, seed):
         tf = b["flops"] / (ms / 1e3) / 1e12
         res[str(n)] = {"perms_per_s": 64 / (ms / 1e3), "ms_per_64": ms, "codes": b["codes"],
                        "achieved_tflops": tf, "frac_of_fp64_peak": tf / peak_tflops}
+        if b["ff_inst"] > 0 and peak32:  # float-pair sweep: its FP32 roofline
+            t32 = b["ff_inst"] / (ms / 1e3) / 1e12
+            res[str(n)].update({"arithmetic": "float pairs", "achieved_t_fp32_inst": t32,
+                                "frac_of_fp32_peak": t32 / peak32})
         if n <= 24:
             hi, lo = O.perm_dd(U, S[0], T[0])
             ref = hi + lo
@@ -428,9 +432,9 @@ def roofline(b, sweep_s, achieved, peak, peak32, traffic):
         return {"bound": "fp32", "kernel": "minors_sweep_ff_kernel (all levels of a step)",
                 "achieved": ach32, "peak": peak32, "unit": "T FP32 inst/s", "frac": ach32 / peak32,
                 "peak_source": "boss_fp32_peak (independent FFMA chains), measured in this run",
-                "inst_note": "float-pair arithmetic, 57.5 nf + 6 FP32 instructions per Guan code at nf = k - 1 "
-                             "factors (38 per complex product, 22 per complex sum); integer, load and "
-                             "conversion instructions not counted",
+                "inst_note": "float-pair arithmetic, 46.25 nf FP32 instructions per Guan code at nf = k - 1 "
+                             "factors (32 per complex product, 16 per complex sum, lazily renormalised); "
+                             "integer, load and conversion instructions not counted",
                 "fp32_inst_per_step": b["ff_inst"],
                 "fp64_equivalent": {"achieved_tflops": achieved, "fp64_peak_tflops": peak,
                                     "ratio_to_fp64_peak": achieved / peak}, **common}
@@ -495,7 +499,7 @@ def run_ours(args, rank, world):
         plain = n_plain / (time.perf_counter() - t)
         line["plain_gpu"] = {"value": plain, "unit": "samples/s", "samples": n_plain}
         line["batched_vs_plain"] = {"device": value / world / plain, "e2e": e2e["value"] / plain}
-        line["single_permanents"] = single_permanents(peak, args.seed)
+        line["single_permanents"] = single_permanents(peak, args.seed, peak32)
         line["adjoint"] = adjoint_section(args.seed)
         line["exact_distribution"] = distribution_section(peak, args.seed)
         line["strategies"] = strategies_section(args.seed)

@@ -118,10 +118,12 @@ BOSS_API int boss_perm_grad_batch(const double* matrix, int32_t m, const int32_t
  * of product-side particles: planned and uploaded once, then the sweep kernel and
  * its reduction run n_warmup + n_steps times (an L2-evicting memset of
  * flush_bytes before each).  sweep_ms receives the sweep kernel's CUDA-event time
- * per timed run; info[0..3] = codes swept per run, algorithmic flops per run
+ * per timed run; info[0..4] = codes swept per run, algorithmic flops per run
  * (codes x (8 nf - 4): nf complex adds, nf - 1 complex products and one signed
- * add per code), threads, and nf.  results (optional) receives the permanents.
- * No reference counterpart.
+ * add per code), threads, nf, and the FP32 instructions per run of the
+ * float-pair sweep (codes x (46.25 nf - 16); 0 in FP64).  info must hold 5
+ * doubles.  results (optional) receives the permanents.  No reference
+ * counterpart.
  */
 BOSS_API int boss_perm_bench(const double* matrix, int32_t m, const int32_t* input_states,
                              const int32_t* output_states, int32_t len, int32_t count, int32_t variant,
@@ -177,6 +179,14 @@ BOSS_API int boss_gccb_sample(const double* matrix, int32_t m, const int32_t* in
 // are exact 64-bit fixed point in both.
 BOSS_API int boss_minors_arithmetic(int32_t mode, int32_t* previous);
 
+// The same choice for the single-permanent sweeps of boss_perm_batch and
+// boss_perm_bench (theboss: numpy float64 in every calculator's
+// compute_permanent, bs_permanent_calculator_base.py:166-198): 0 float pairs
+// (default, up to 32 product-side particles, Glynn-kind sweeps: Glynn, Chin-Huh,
+// Classic), 1 FP64, -1 query.  Ryser-form sweeps, whose alternating sum cancels
+// far more, the allocation-free entry point and the gradients always use FP64.
+BOSS_API int boss_perm_arithmetic(int32_t mode, int32_t* previous);
+
 /*
  * Benchmark form of boss_gccb_sample: the random stream is replayed and the
  * inputs uploaded once, then the captured sampler graph runs n_warmup + n_steps
@@ -188,10 +198,10 @@ BOSS_API int boss_minors_arithmetic(int32_t mode, int32_t* previous);
  * D2H bytes of one boss_gccb_sample call, kernels per run, sweep launches per
  * run, the deepest level, the same flop count over theboss's Ryser-form codes
  * (twice as many for single photons), and the FP32 instructions per run of the
- * float-pair sweeps (57.5 nf + 6 per code at nf factors: nf - 1 float-pair
- * complex products of 38, two complex float-pair sums of 22 for the running
- * total and a minor, 7/8 of the codes 22 per factor to move the sums; 0 when the
- * sweeps run in FP64).  info must hold 8 doubles.  samples
+ * float-pair sweeps (46.25 nf per code at nf factors: nf - 1 float-pair
+ * complex products of 32, two complex float-pair sums of 16 for the running
+ * total and a minor, 7/8 of the codes 16 per factor to move the sums, 1/8 of
+ * them 2 per factor to convert; 0 when the sweeps run in FP64).  info must hold 8 doubles.  samples
  * (optional) receives the last run's samples.  No reference counterpart.
  */
 BOSS_API int boss_gccb_bench(const double* matrix, int32_t m, const int32_t* input_state,

@@ -97,6 +97,8 @@ def load() -> ctypes.CDLL:
         L.boss_gccb_sample_slice.restype = ctypes.c_int
         L.boss_gccb_sample_slice.argtypes = [dp, ctypes.c_int32, ip, dp, ctypes.c_int32, up, ip, ctypes.c_int32,
                                              ctypes.c_int32, ctypes.c_int32, ip]
+        L.boss_perm_arithmetic.restype = ctypes.c_int
+        L.boss_perm_arithmetic.argtypes = [ctypes.c_int32, ip]
         L.boss_minors_arithmetic.restype = ctypes.c_int
         L.boss_minors_arithmetic.argtypes = [ctypes.c_int32, ip]
         _lib = L
@@ -355,6 +357,14 @@ def fp32_peak():
     return float(t[0]), float(ms[0])
 
 
+def perm_arithmetic(mode: int = -1) -> int:
+    """Sets the arithmetic of the single-permanent sweeps (FLOAT_PAIRS or FP64; -1
+    only queries) and returns the previous one."""
+    prev = np.zeros(1, dtype=np.int32)
+    check(load().boss_perm_arithmetic(int(mode), _ip(prev)))
+    return int(prev[0])
+
+
 def select_device(device: int) -> None:
     check(load().boss_select_device(int(device)))
 
@@ -452,13 +462,13 @@ def gccb_bench(U: np.ndarray, input_state, weights, n_samples: int, warmup: int,
 def perm_bench(U: np.ndarray, S: np.ndarray, T: np.ndarray, variant: int, warmup: int, steps: int,
                flush_bytes: int = 256 << 20):
     """Device-timed sweeps of a batch of permanents sharing one product size.
-    Returns dict(sweep_ms, codes, flops, threads, nf, results)."""
+    Returns dict(sweep_ms, codes, flops, threads, nf, ff_inst, results)."""
     L = load()
     count, n = S.shape
     sweep_ms = np.zeros(steps)
-    info = np.zeros(4)
+    info = np.zeros(5)
     res = np.zeros(count, dtype=np.complex128)
     check(L.boss_perm_bench(_dp(U.view(np.float64)), U.shape[0], _ip(S), _ip(T), n, count, variant, warmup, steps,
                             int(flush_bytes), _dp(sweep_ms), _dp(info), _dp(res.view(np.float64))))
     return dict(sweep_ms=sweep_ms, codes=float(info[0]), flops=float(info[1]), threads=int(info[2]),
-                nf=int(info[3]), results=res)
+                nf=int(info[3]), ff_inst=float(info[4]), results=res)

@@ -100,8 +100,14 @@ static int sweeps_prepare(Context* cx, const std::vector<HostSweep>& sweeps, boo
   B.nf = sweeps[0].nf;
   B.minors = minors;
   B.nd_max = nd_max;
-  B.ff = minors && g_minors_arith == 0 && minors_ff_available(B.nf);
-  const SweepOp op = minors ? SweepOp::kMinors : SweepOp::kPerm;
+  // Float pairs only for Glynn-kind sweeps: the Ryser form's alternating sum cancels
+  // far more (its FP64 error is already ~1e-10 at n = 20), and float pairs would
+  // leave theboss's tolerance.
+  bool glynn = true;
+  for (const HostSweep& h : sweeps) glynn = glynn && h.kind == kGlynn;
+  B.ff = glynn && (minors ? (g_minors_arith == 0 && minors_ff_available(B.nf))
+                          : (g_perm_arith == 0 && perm_ff_available(B.nf)));
+  const SweepOp op = minors ? SweepOp::kMinors : (B.ff ? SweepOp::kPermFF : SweepOp::kPerm);
   std::vector<uint64_t> codes(n);
   B.codes = 0.0;
   for (int p = 0; p < n; ++p) {
@@ -193,12 +199,12 @@ static int sweeps_prepare(Context* cx, const std::vector<HostSweep>& sweeps, boo
 }
 
 static int sweeps_launch(Context* cx, const SweepBatch& B, cudaEvent_t after_sweep = nullptr) {
-  const SweepOp op = B.minors ? (B.ff ? SweepOp::kMinorsFF : SweepOp::kMinors) : SweepOp::kPerm;
+  const SweepOp op = B.minors ? (B.ff ? SweepOp::kMinorsFF : SweepOp::kMinors) : (B.ff ? SweepOp::kPermFF : SweepOp::kPerm);
   cudaError_t e = launch_sweep(B.nf, op, B.L, cx->stream);
   if (e != cudaSuccess) return fail_cuda(e, "sweep launch");
   if (after_sweep) cudaEventRecord(after_sweep, cx->stream);
   e = B.minors ? launch_minors_reduce(B.L.probs, B.n, B.L.partials, (double2*)cx->out.ptr, B.nd_max, cx->stream, B.ff)
-               : launch_perm_reduce(B.L.probs, B.n, B.L.partials, (double2*)cx->out.ptr, cx->stream);
+               : launch_perm_reduce(B.L.probs, B.n, B.L.partials, (double2*)cx->out.ptr, cx->stream, B.ff);
   return e == cudaSuccess ? kOk : fail_cuda(e, "reduce launch");
 }
 
@@ -360,6 +366,7 @@ static int fill_sweep(HostSweep& hs, const Side& dig, const Side& col, int kind,
 }
 
 int g_minors_arith = 0;
+int g_perm_arith = 0;
 
 void host_fx_to_ff(long long x, int fbias, float& hi, float& lo) {
   const unsigned long long sgn = (unsigned long long)(x >> 63);
@@ -896,6 +903,9 @@ int boss_perm_bench(const double* matrix, int32_t m, const int32_t* input_states
   info[1] = flops;
   info[2] = (double)B.L.total_threads;
   info[3] = (double)B.nf;
+  // float pairs: nf - 1 complex products of 32, one complex sum of 16, 7/8 of the
+  // codes 16 per factor to move the sums, 1/8 of them 2 per factor to convert
+  info[4] = B.ff ? B.codes * (46.25 * B.nf - 16.0) : 0.0;
   return kOk;
 }
 

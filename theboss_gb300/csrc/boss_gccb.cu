@@ -325,7 +325,8 @@ __global__ void __launch_bounds__(kFinWarps * 32) gccb_finalize_kernel(FinalizeA
       if (parts <= 64) {
         if (lane < nd) {
           float rh = 0.0f, rl = 0.0f, ih = 0.0f, il = 0.0f;
-          for (int64_t q = 0; q < parts; ++q) {
+#pragma unroll 8
+          for (int64_t q = 0; q < parts; ++q) {  // unrolled: 8 loads in flight
             const float4 v = fp[q * nd + lane];
             ff_acc(rh, rl, 1.0f, v.x, v.y);
             ff_acc(ih, il, 1.0f, v.z, v.w);
@@ -353,6 +354,7 @@ __global__ void __launch_bounds__(kFinWarps * 32) gccb_finalize_kernel(FinalizeA
     } else if (parts <= 64) {  // lane d sums digit d's partials
       if (lane < nd) {
         double sx = 0.0, sy = 0.0;
+#pragma unroll 8
         for (int64_t q = 0; q < parts; ++q) {
           const double2 v = a.partials[P.part_off + q * nd + lane];
           sx += v.x;
@@ -396,6 +398,7 @@ __global__ void __launch_bounds__(kFinWarps * 32) gccb_finalize_kernel(FinalizeA
   const int full = m & ~31;
   for (int o = lane; o < full; o += 32) {
     float sr = 0.0f, cr = 0.0f, si = 0.0f, ci = 0.0f;
+    #pragma unroll 4  // independent gathers in flight
     for (int d = 0; d < nd; ++d) {
       const float4 c = subf_s[w][d];
       const float4 u = UT[(size_t)dm_s[w][d] * m + o];
@@ -413,6 +416,7 @@ __global__ void __launch_bounds__(kFinWarps * 32) gccb_finalize_kernel(FinalizeA
     const int oi = lane / s, c0 = lane & (s - 1);
     float sr = 0.0f, cr = 0.0f, si = 0.0f, ci = 0.0f;
     if (oi < r) {
+      #pragma unroll 4  // independent gathers in flight
       for (int d = c0; d < nd; d += s) {
         const float4 c = subf_s[w][d];
         const float4 u = UT[(size_t)dm_s[w][d] * m + full + oi];
@@ -581,6 +585,7 @@ __global__ void __launch_bounds__(kFinWarps * 32) gccb_finalize_kernel(FinalizeA
   // rows: -2 U[out][in] for the sweep's digits; base sums: sum_i S_i U[out][i]
   // over every input mode (all signs +1 at r = 0), exact in fixed point
   longlong2* D = a.pool_next + ls.pool_off;
+  #pragma unroll 4  // independent gathers in flight
   for (int e = lane; e < nds * nf; e += 32) {
     const int d = e / nf, f = e - d * nf;
     const longlong2 u = Ufxs[(size_t)fm_s[w][f] * m + dm_s[w][d]];
@@ -596,6 +601,7 @@ __global__ void __launch_bounds__(kFinWarps * 32) gccb_finalize_kernel(FinalizeA
   for (int f = lane; f < nf; f += 32) {
     long long bx = 0, by = 0;
     unsigned long long ax = 0, ay = 0;
+    #pragma unroll 4  // independent gathers in flight
     for (int d = 0; d < nd; ++d) {
       const longlong2 u = Ufxs[(size_t)fm_s[w][f] * m + dm_s[w][d]];
       bx += (long long)mult_s[w][d] * u.x;
@@ -615,6 +621,7 @@ __global__ void __launch_bounds__(kFinWarps * 32) gccb_finalize_kernel(FinalizeA
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) esum += __shfl_xor_sync(0xffffffffu, esum, off);
     __syncwarp();  // fbias written by the other lanes
+    #pragma unroll 4  // independent gathers in flight
     for (int e = lane; e < (nb - held) * nf; e += 32) {
       const int d = e / nf, f = e - d * nf;
       const longlong2 u = Ufxs[(size_t)fm_s[w][f] * m + dm_s[w][d]];
@@ -767,7 +774,7 @@ static int gccb_prepare(Context* cx, const double* matrix, int n_mats, int m, Dr
   std::vector<char> ffl(Lmax + 2, 0);  // level k's sweep runs on float pairs
   for (int k = 2; k <= Lmax; ++k) ffl[k] = (g_minors_arith == 0 && minors_ff_available(k - 1)) ? 1 : 0;
   // FP32 instructions per code of a float-pair sweep with nf = k - 1 factors
-  auto ff_per_code = [&](int k) { return ffl[k] ? 57.5 * (k - 1) + 6.0 : 0.0; };
+  auto ff_per_code = [&](int k) { return ffl[k] ? 46.25 * (k - 1) : 0.0; };
   R.sweep_flops = 0.0;
   R.ref_flops = 0.0;
   R.ff_inst = 0.0;
@@ -833,9 +840,14 @@ static int gccb_prepare(Context* cx, const double* matrix, int n_mats, int m, Dr
       const double want = std::max<double>(Ak, std::min<double>((double)resident, total / kMinCodesPerThread));
       int64_t tps = std::max<int64_t>(1, std::min<int64_t>((int64_t)code0, (int64_t)(want / Ak)));
       // Each aligned group of G threads of a sample sums its minors inside the sweep:
-      // the largest G (up to a warp) that costs at most 2% of the sample's threads.
-      int G = 32;
-      while (G > 1 && !(tps >= G && (double)(tps / G * G) >= 0.98 * (double)tps)) G >>= 1;
+      // the largest G (up to a warp; up to a block of 128 for float-pair sweeps whose
+      // threads then fill whole blocks) that costs at most 2% of the sample's threads.
+      int G = ffl[k] ? 128 : 32;
+      auto ok = [&](int g) {
+        if (!(tps >= g && (double)(tps / g * g) >= 0.98 * (double)tps)) return false;
+        return g <= 32 || ((tps / g * g) * (int64_t)Ak) % 128 == 0;
+      };
+      while (G > 1 && !ok(G)) G >>= 1;
       tps = tps / G * G;
       grp[k] = G;
       uniform[k] = 1;
@@ -962,6 +974,7 @@ static int gccb_prepare(Context* cx, const double* matrix, int n_mats, int m, Dr
       SL.partials = partials;
       SL.grid = (int)((lvl_threads[k] + 127) / 128);
       SL.rows = std::min(k, kMaxMinorDigits);
+      SL.uniform_threads = uniform[k] ? uni_lvl[k].n_threads : 0;
       if (timing) le = cudaEventRecordWithFlags(R.ev[2 * (k - 2)], s, cudaEventRecordExternal);
       if (le == cudaSuccess) le = launch_sweep(k - 1, ffl[k] ? SweepOp::kMinorsFF : SweepOp::kMinors, SL, s);
       if (timing && le == cudaSuccess) le = cudaEventRecordWithFlags(R.ev[2 * (k - 2) + 1], s, cudaEventRecordExternal);
@@ -1206,6 +1219,17 @@ int boss_gccb_sample_slice(const double* matrix, int32_t m, const int32_t* input
   }
   memcpy(mt_key, mt.key, sizeof(mt.key));
   *mt_pos = mt.pos;
+  return kOk;
+}
+
+int boss_perm_arithmetic(int32_t mode, int32_t* previous) {
+  if (mode < -1 || mode > 1) {
+    set_error("permanent arithmetic: 0 float pairs, 1 FP64, -1 query");
+    return kErrArg;
+  }
+  std::lock_guard<std::mutex> lk(g_api_mutex);
+  if (previous) *previous = g_perm_arith;
+  if (mode >= 0) g_perm_arith = mode;
   return kOk;
 }
 

@@ -11,7 +11,7 @@
 
 namespace boss {
 
-enum class SweepOp { kPerm = 0, kMinors = 1, kGrad = 2, kMinorsFF = 3 };  // kMinorsFF: float pairs, nf <= 24
+enum class SweepOp { kPerm = 0, kMinors = 1, kGrad = 2, kMinorsFF = 3, kPermFF = 4 };  // FF: float pairs
 
 // Everything one sweep launch needs (device pointers).
 struct SweepLaunch {
@@ -23,6 +23,8 @@ struct SweepLaunch {
   double2* partials2 = nullptr;  // gradients: per-warp permanent partials
   int grid = 1;
   int rows = 32;  // all-minors: shared-memory rows of minors per thread (nd + held digit, at most 32)
+  int64_t uniform_threads = 0;  // all-minors: > 0 when every sweep has this many threads and sweep p
+                                // starts at thread p * uniform_threads (no search for the sweep)
 };
 
 // Sets kernel attributes and records occupancy (once per process, outside any capture).
@@ -32,11 +34,12 @@ int64_t sweep_resident_threads(int nf, SweepOp op, int sm_count);
 // Resident threads of the all-minors kernel (FP64, or the float-pair one) with
 // `rows` rows of minors per thread.
 int64_t sweep_resident_minors(int nf, int rows, int sm_count, bool ff = false);
-// Whether the float-pair all-minors kernel exists for nf factors.
+// Whether the float-pair all-minors / single-permanent kernel exists for nf factors.
 bool minors_ff_available(int nf);
+bool perm_ff_available(int nf);
 cudaError_t launch_sweep(int nf, SweepOp op, const SweepLaunch& L, cudaStream_t st);
 cudaError_t launch_perm_reduce(const SweepProblem* probs, int n_probs, const double2* partials, double2* out,
-                               cudaStream_t st);
+                               cudaStream_t st, bool ff = false);
 cudaError_t launch_grad_reduce(const SweepProblem* probs, int n_probs, const double2* gpart, const double2* ppart,
                                double2* grad_out, double2* perm_out, int row_stride, cudaStream_t st);
 cudaError_t launch_minors_reduce(const SweepProblem* probs, int n_probs, const double2* partials, double2* out,
@@ -74,6 +77,8 @@ struct HostSweep {
 // Arithmetic of the all-minors sweeps (boss_minors_arithmetic): 0 float pairs
 // where the kernel exists for the factor count, 1 FP64.
 extern int g_minors_arith;
+// Arithmetic of the single-permanent sweeps (boss_perm_arithmetic), same codes.
+extern int g_perm_arith;
 // x * 2^(fbias - 190) as a float pair, the host twin of fx_to_ff (same bits).
 void host_fx_to_ff(long long x, int fbias, float& hi, float& lo);
 

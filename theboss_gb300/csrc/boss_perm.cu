@@ -11,10 +11,10 @@ cudaError_t sweep_nf_a_launch(int nf, SweepOp op, const SweepLaunch& L, cudaStre
 cudaError_t sweep_nf_b_launch(int nf, SweepOp op, const SweepLaunch& L, cudaStream_t st);
 cudaError_t sweep_nf_c_launch(int nf, SweepOp op, const SweepLaunch& L, cudaStream_t st);
 cudaError_t sweep_nf_d_launch(int nf, SweepOp op, const SweepLaunch& L, cudaStream_t st);
-cudaError_t sweep_nf_a_prepare(int* perm_occ, int* minors_occ, int* ff_occ);
-cudaError_t sweep_nf_b_prepare(int* perm_occ, int* minors_occ, int* ff_occ);
-cudaError_t sweep_nf_c_prepare(int* perm_occ, int* minors_occ, int* ff_occ);
-cudaError_t sweep_nf_d_prepare(int* perm_occ, int* minors_occ, int* ff_occ);
+cudaError_t sweep_nf_a_prepare(int* perm_occ, int* minors_occ, int* ff_occ, int* pff_occ);
+cudaError_t sweep_nf_b_prepare(int* perm_occ, int* minors_occ, int* ff_occ, int* pff_occ);
+cudaError_t sweep_nf_c_prepare(int* perm_occ, int* minors_occ, int* ff_occ, int* pff_occ);
+cudaError_t sweep_nf_d_prepare(int* perm_occ, int* minors_occ, int* ff_occ, int* pff_occ);
 
 cudaError_t sweep_nf_a_grad_occupancy(int nf, int* occ);
 cudaError_t sweep_nf_b_grad_occupancy(int nf, int* occ);
@@ -22,17 +22,22 @@ cudaError_t sweep_nf_c_grad_occupancy(int nf, int* occ);
 cudaError_t sweep_nf_d_grad_occupancy(int nf, int* occ);
 
 static int g_perm_occ[kMaxFactors + 1];
+static int g_perm_ff_occ[kMaxFactors + 1];
 static int g_minors_occ[kMaxFactors + 1][kMaxMinorDigits + 1];     // [nf][rows of minors]
 static int g_minors_ff_occ[kMaxFactors + 1][kMaxMinorDigits + 1];  // float-pair kernel; 0: none
 
 cudaError_t prepare_sweep_kernels() {
   cudaError_t e;
-  if ((e = sweep_nf_a_prepare(g_perm_occ + 1, &g_minors_occ[1][0], &g_minors_ff_occ[1][0])) != cudaSuccess) return e;
-  if ((e = sweep_nf_b_prepare(g_perm_occ + 9, &g_minors_occ[9][0], &g_minors_ff_occ[9][0])) != cudaSuccess) return e;
-  if ((e = sweep_nf_c_prepare(g_perm_occ + 17, &g_minors_occ[17][0], &g_minors_ff_occ[17][0])) != cudaSuccess)
+  if ((e = sweep_nf_a_prepare(g_perm_occ + 1, &g_minors_occ[1][0], &g_minors_ff_occ[1][0], g_perm_ff_occ + 1)))
     return e;
-  return sweep_nf_d_prepare(g_perm_occ + 25, &g_minors_occ[25][0], &g_minors_ff_occ[25][0]);
+  if ((e = sweep_nf_b_prepare(g_perm_occ + 9, &g_minors_occ[9][0], &g_minors_ff_occ[9][0], g_perm_ff_occ + 9)))
+    return e;
+  if ((e = sweep_nf_c_prepare(g_perm_occ + 17, &g_minors_occ[17][0], &g_minors_ff_occ[17][0], g_perm_ff_occ + 17)))
+    return e;
+  return sweep_nf_d_prepare(g_perm_occ + 25, &g_minors_occ[25][0], &g_minors_ff_occ[25][0], g_perm_ff_occ + 25);
 }
+
+bool perm_ff_available(int nf) { return nf >= 1 && nf <= kMaxFactors && g_perm_ff_occ[nf] > 0; }
 
 bool minors_ff_available(int nf) { return nf >= 1 && nf <= kMaxFactors && g_minors_ff_occ[nf][kMaxMinorDigits] > 0; }
 
@@ -57,7 +62,9 @@ int64_t sweep_resident_threads(int nf, SweepOp op, int sm_count) {
     }
     return (int64_t)std::max(occ, 1) * sm_count * 64;
   }
-  const int occ = std::max(1, op == SweepOp::kPerm ? g_perm_occ[nf] : g_minors_occ[nf][kMaxMinorDigits]);
+  const int occ = std::max(1, op == SweepOp::kPerm     ? g_perm_occ[nf]
+                              : op == SweepOp::kPermFF ? g_perm_ff_occ[nf]
+                                                       : g_minors_occ[nf][kMaxMinorDigits]);
   return (int64_t)occ * sm_count * 128;
 }
 
@@ -88,13 +95,20 @@ void partition_threads(const std::vector<uint64_t>& n_codes, int64_t resident, s
 }
 
 // One block per sweep: fixed-order sum of its threads' partials.
+// ff: the partials are float pairs (float4), as the float-pair sweep writes them.
 __global__ void perm_reduce_kernel(const SweepProblem* __restrict__ probs, const double2* __restrict__ partials,
-                                   double2* __restrict__ out) {
+                                   double2* __restrict__ out, int ff) {
   __shared__ double sr[256], si[256];
   const SweepProblem& P = probs[blockIdx.x];
   double ar = 0.0, ai = 0.0;
   for (int64_t i = threadIdx.x; i < P.n_threads; i += blockDim.x) {
-    const double2 v = partials[P.part_off + i];
+    double2 v;
+    if (ff) {
+      const float4 f = reinterpret_cast<const float4*>(partials)[P.part_off + i];
+      v = make_double2(ff_to_double(f.x, f.y), ff_to_double(f.z, f.w));
+    } else {
+      v = partials[P.part_off + i];
+    }
     ar += v.x;
     ai += v.y;
   }
@@ -193,9 +207,9 @@ cudaError_t launch_grad_reduce(const SweepProblem* probs, int n_probs, const dou
 }
 
 cudaError_t launch_perm_reduce(const SweepProblem* probs, int n_probs, const double2* partials, double2* out,
-                               cudaStream_t st) {
+                               cudaStream_t st, bool ff) {
   if (n_probs <= 0) return cudaSuccess;
-  perm_reduce_kernel<<<n_probs, 256, 0, st>>>(probs, partials, out);
+  perm_reduce_kernel<<<n_probs, 256, 0, st>>>(probs, partials, out, ff ? 1 : 0);
   return cudaGetLastError();
 }
 

@@ -65,7 +65,7 @@ struct SweepProblem {
                      // im hi, im lo, each factor in its own scale), then nf int32 exponent biases
   double scale;      // final real scale
   int32_t fixed_digit;  // gradients, all-minors: a binary digit held at r = 0 (Glynn halving) adds a weight-1 row
-  int32_t group;     // all-minors: each aligned group of `group` threads (1, 2, 4, .., 32) sums its
+  int32_t group;     // all-minors: each aligned group of `group` threads (1, 2, 4, .., 32; float pairs up to 128) sums its
                      // minors, so the partials are (n_threads / group) x nd; n_threads and
                      // thread_begin are multiples of it, and every sweep of the launch has the same
   uint8_t mult[kMaxDigits];

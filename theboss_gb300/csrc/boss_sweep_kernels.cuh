@@ -160,11 +160,12 @@ __device__ __forceinline__ void minors_walk(const SweepProblem& P, const longlon
 template <int NF>
 __global__ void __launch_bounds__(128) minors_sweep_kernel(const SweepProblem* __restrict__ probs, int n_probs,
                                                            const longlong2* __restrict__ pool, int64_t total_threads,
-                                                           double2* __restrict__ partials) {
+                                                           double2* __restrict__ partials, int64_t uniform_threads) {
   extern __shared__ double2 minors_smem[];
   const int64_t gt = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (gt >= total_threads) return;
-  const SweepProblem& P = probs[find_problem(probs, n_probs, gt)];
+  const SweepProblem& P =
+      probs[uniform_threads > 0 ? (int)(gt / uniform_threads) : find_problem(probs, n_probs, gt)];
   const int64_t q = gt - P.thread_begin;
   const int nd = P.nd + P.fixed_digit;  // minors written per thread
   double2* M = minors_smem + threadIdx.x;
@@ -389,11 +390,13 @@ __device__ __forceinline__ void minors_walk_ff(const SweepProblem& P, const long
 template <int NF>
 __global__ void __launch_bounds__(128, kFFMinBlocks<NF>) minors_sweep_ff_kernel(const SweepProblem* __restrict__ probs, int n_probs,
                                                               const longlong2* __restrict__ pool, int64_t total_threads,
-                                                              double2* __restrict__ partials, int rows) {
+                                                              double2* __restrict__ partials, int rows,
+                                                              int64_t uniform_threads) {
   extern __shared__ float4 minors_ff_smem[];
   const int64_t gt = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (gt >= total_threads) return;
-  const SweepProblem& P = probs[find_problem(probs, n_probs, gt)];
+  const SweepProblem& P =
+      probs[uniform_threads > 0 ? (int)(gt / uniform_threads) : find_problem(probs, n_probs, gt)];
   const int64_t q = gt - P.thread_begin;
   const int nd = P.nd + P.fixed_digit;
   float4* M = minors_ff_smem + threadIdx.x;
@@ -403,7 +406,35 @@ __global__ void __launch_bounds__(128, kFFMinBlocks<NF>) minors_sweep_ff_kernel(
   const int* fb = reinterpret_cast<const int*>(DF + (size_t)P.nb * NF);
   minors_walk_ff<NF, 128>(P, pool + P.mat_off, pool + P.base_off, DF, fb, q, M, SS);
   const int G = P.group;
-  if (G > 1) {
+  if (G > 32) {
+    // Groups of 64 or 128 threads: the planner allows them only when the launch's
+    // threads fill whole blocks, so no thread of this block has exited.  Each warp
+    // sums its lanes' minors (lane l: digit l, nd <= 32) into row l's first column
+    // of the warp, then thread t of each group adds up digit t over its warps.
+    const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
+    __syncwarp();
+    if (lane < nd) {
+      const float4* row = minors_ff_smem + lane * 128 + wp * 32;
+      float rh = 0.0f, rl = 0.0f, ih = 0.0f, il = 0.0f;
+      for (int i = 0; i < 32; ++i) {
+        const float4 v = row[(i + lane) & 31];
+        ff_acc(rh, rl, 1.0f, v.x, v.y);
+        ff_acc(ih, il, 1.0f, v.z, v.w);
+      }
+      minors_ff_smem[lane * 128 + wp * 32] = make_float4(rh, rl, ih, il);
+    }
+    __syncthreads();
+    const int tin = threadIdx.x & (G - 1), w0 = (threadIdx.x - tin) >> 5;
+    if (tin < nd) {
+      float rh = 0.0f, rl = 0.0f, ih = 0.0f, il = 0.0f;
+      for (int wv = 0; wv < (G >> 5); ++wv) {
+        const float4 v = minors_ff_smem[tin * 128 + (w0 + wv) * 32];
+        ff_acc(rh, rl, 1.0f, v.x, v.y);
+        ff_acc(ih, il, 1.0f, v.z, v.w);
+      }
+      reinterpret_cast<float4*>(partials)[P.part_off + (q / G) * nd + tin] = make_float4(rh, rl, ih, il);
+    }
+  } else if (G > 1) {
     const int lane = threadIdx.x & 31;
     const int64_t warp0 = gt - lane;
     const unsigned live = (warp0 + 32 <= total_threads) ? 0xffffffffu : ((1u << (total_threads - warp0)) - 1u);
@@ -424,6 +455,92 @@ __global__ void __launch_bounds__(128, kFFMinBlocks<NF>) minors_sweep_ff_kernel(
     float4* out = reinterpret_cast<float4*>(partials) + P.part_off + q * nd;
     for (int j = 0; j < nd; ++j) out[j] = M[j * 128];
   }
+}
+
+// Single permanents with float pairs: perm_sweep_kernel's walk with the
+// float-pair machinery of the all-minors sweep (exact sums in shared memory,
+// resynchronised every kFFResync codes, lazily renormalised sums and products).
+// Each thread writes its partial as a float pair (float4) in the factors' scales.
+constexpr int kFFPermMaxFactors = 32;
+template <int NF>
+constexpr int kFFPermMinBlocks = NF <= 12 ? 4 : (NF <= 20 ? 3 : 2);
+
+template <int NF>
+__global__ void __launch_bounds__(128, kFFPermMinBlocks<NF>) perm_sweep_ff_kernel(
+    const SweepProblem* __restrict__ probs, int n_probs, const longlong2* __restrict__ pool, int64_t total_threads,
+    double2* __restrict__ partials) {
+  extern __shared__ longlong2 perm_ff_smem[];
+  const int64_t gt = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (gt >= total_threads) return;
+  const SweepProblem& P = probs[find_problem(probs, n_probs, gt)];
+  const int64_t q = gt - P.thread_begin;
+  int64_t a, len;
+  thread_range(P, q, a, len);
+  float trh = 0.0f, trl = 0.0f, tih = 0.0f, til = 0.0f;  // weighted total of the finished segments
+  if (len > 0) {
+    const longlong2* D = pool + P.mat_off;
+    const longlong2* base = pool + P.base_off;
+    const float4* DF = reinterpret_cast<const float4*>(pool + P.ff_off);
+    const int* fb = reinterpret_cast<const int*>(DF + (size_t)P.nb * NF);
+    longlong2* SS = perm_ff_smem + threadIdx.x;
+    const int nb = P.nb;
+    ffc S[NF];
+    uint64_t g;
+    uint32_t parity;
+    double w;
+    decode_code_ff<NF>(P, D, base, fb, (uint64_t)a, SS, S, g, parity, w);
+    uint64_t g_int = g;
+    ffc A = {0.0f, 0.0f, 0.0f, 0.0f};  // this segment's signed sum of products
+    const uint64_t end = (uint64_t)(a + len);
+    for (uint64_t t = (uint64_t)a;;) {
+      {
+        ffc p = S[0];
+#pragma unroll
+        for (int f = 1; f < NF; ++f) p = ff_cmul_lazy(p, S[f]);
+        const float sg = parity ? -1.0f : 1.0f;
+        ff_add_lazy(A.rh, A.rl, sg, p.rh, p.rl);
+        ff_add_lazy(A.ih, A.il, sg, p.ih, p.il);
+      }
+      const uint64_t tn = t + 1;
+      if (tn >= end) break;
+      const int i = __ffsll((long long)tn) - 1;
+      if (i < nb) {
+        const uint32_t bit = (uint32_t)(g >> i) & 1u;
+        g ^= 1ull << i;
+        parity ^= 1u;
+        if (((tn - (uint64_t)a) & (kFFResync - 1)) == 0) {
+          resync_ff<NF>(D, fb, g, g_int, SS, S);
+          g_int = g;
+        } else {
+          const float sg = bit ? -1.0f : 1.0f;
+          const float4* row = DF + (size_t)i * NF;
+#pragma unroll
+          for (int f = 0; f < NF; ++f) {
+            if (f > 0 && (f & 7) == 0) load_fence();
+            const float4 d = row[f];
+            ff_add_lazy(S[f].rh, S[f].rl, sg, d.x, d.y);
+            ff_add_lazy(S[f].ih, S[f].il, sg, d.z, d.w);
+          }
+        }
+      } else {  // a multi-valued digit moves: settle the segment with its weight, re-decode
+        const float wh = __double2float_rn(w), wl = __double2float_rn(w - (double)wh);
+        ff_mul(A.rh, A.rl, wh, wl);
+        ff_mul(A.ih, A.il, wh, wl);
+        ff_acc(trh, trl, 1.0f, A.rh, A.rl);
+        ff_acc(tih, til, 1.0f, A.ih, A.il);
+        A = {0.0f, 0.0f, 0.0f, 0.0f};
+        decode_code_ff<NF>(P, D, base, fb, tn, SS, S, g, parity, w);
+        g_int = g;
+      }
+      t = tn;
+    }
+    const float wh = __double2float_rn(w), wl = __double2float_rn(w - (double)wh);
+    ff_mul(A.rh, A.rl, wh, wl);
+    ff_mul(A.ih, A.il, wh, wl);
+    ff_acc(trh, trl, 1.0f, A.rh, A.rl);
+    ff_acc(tih, til, 1.0f, A.ih, A.il);
+  }
+  reinterpret_cast<float4*>(partials)[P.part_off + q] = make_float4(trh, trl, tih, til);
 }
 
 // Gradient sweep (Glynn / Chin-Huh kind).  With s_f the factor sums and
@@ -634,18 +751,23 @@ cudaError_t sweep_launch_t(SweepOp op, const SweepLaunch& L, cudaStream_t st) {
     if constexpr (NF <= kFFMaxFactors) {
       const int rows = (L.rows >= 1 && L.rows <= kMaxMinorDigits) ? L.rows : kMaxMinorDigits;
       minors_sweep_ff_kernel<NF><<<L.grid, 128, (size_t)(rows + NF) * 128 * sizeof(float4), st>>>(
-          L.probs, L.n_probs, L.pool, L.total_threads, L.partials, rows);
+          L.probs, L.n_probs, L.pool, L.total_threads, L.partials, rows, L.uniform_threads);
       return cudaGetLastError();
     } else {
       return cudaErrorInvalidValue;
     }
+  }
+  if (op == SweepOp::kPermFF) {
+    perm_sweep_ff_kernel<NF><<<L.grid, 128, (size_t)NF * 128 * sizeof(longlong2), st>>>(
+        L.probs, L.n_probs, L.pool, L.total_threads, L.partials);
+    return cudaGetLastError();
   }
   if (op == SweepOp::kPerm) {
     perm_sweep_kernel<NF><<<L.grid, 128, 0, st>>>(L.probs, L.n_probs, L.pool, L.total_threads, L.partials);
   } else {  // shared memory: the launch's rows of minors per thread, 128 threads per block
     const int rows = (L.rows >= 1 && L.rows <= kMaxMinorDigits) ? L.rows : kMaxMinorDigits;
     minors_sweep_kernel<NF><<<L.grid, 128, (size_t)rows * 128 * sizeof(double2), st>>>(
-        L.probs, L.n_probs, L.pool, L.total_threads, L.partials);
+        L.probs, L.n_probs, L.pool, L.total_threads, L.partials, L.uniform_threads);
   }
   return cudaGetLastError();
 }
@@ -660,7 +782,8 @@ cudaError_t grad_occupancy_t(int* blocks_per_sm) {
 // minors per thread in shared memory; ff_blocks_per_sm[r] the same for the
 // float-pair kernel (left at 0 above kFFMaxFactors).
 template <int NF>
-cudaError_t sweep_prepare_t(int* perm_blocks_per_sm, int* minors_blocks_per_sm, int* ff_blocks_per_sm) {
+cudaError_t sweep_prepare_t(int* perm_blocks_per_sm, int* minors_blocks_per_sm, int* ff_blocks_per_sm,
+                            int* perm_ff_blocks_per_sm) {
   cudaError_t e = cudaFuncSetAttribute(minors_sweep_kernel<NF>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)kMinorsSmem);
   if (e != cudaSuccess) return e;
@@ -682,6 +805,15 @@ cudaError_t sweep_prepare_t(int* perm_blocks_per_sm, int* minors_blocks_per_sm, 
   e = cudaFuncSetAttribute(grad_sweep_kernel<NF>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kGradSmem);
   if (e != cudaSuccess) return e;
   e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(perm_blocks_per_sm, perm_sweep_kernel<NF>, 128, 0);
+  if (e != cudaSuccess) return e;
+  e = cudaFuncSetAttribute(perm_sweep_ff_kernel<NF>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)((size_t)NF * 128 * sizeof(longlong2)));
+  if (e != cudaSuccess) return e;
+  e = cudaFuncSetAttribute(perm_sweep_ff_kernel<NF>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                           (int)cudaSharedmemCarveoutMaxShared);
+  if (e != cudaSuccess) return e;
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(perm_ff_blocks_per_sm, perm_sweep_ff_kernel<NF>, 128,
+                                                    (size_t)NF * 128 * sizeof(longlong2));
   if (e != cudaSuccess) return e;
   for (int r = 1; r <= kMaxMinorDigits; ++r) {
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(minors_blocks_per_sm + r, minors_sweep_kernel<NF>, 128,
@@ -722,18 +854,19 @@ cudaError_t sweep_prepare_t(int* perm_blocks_per_sm, int* minors_blocks_per_sm, 
       default: return cudaErrorInvalidValue;                                                             \
     }                                                                                                    \
   }                                                                                                      \
-  cudaError_t NAME##_prepare(int* perm_occ, int* minors_occ, int* ff_occ) { /* 8 rows of 33 */        \
+  cudaError_t NAME##_prepare(int* perm_occ, int* minors_occ, int* ff_occ, int* pff_occ) {                 \
     cudaError_t e;                                                                                       \
     for (int k = 0; k < 8; ++k) perm_occ[k] = 1;                                                         \
+    for (int k = 0; k < 8; ++k) pff_occ[k] = 1;                                                          \
     for (int k = 0; k < 8 * 33; ++k) minors_occ[k] = 1;                                                  \
     for (int k = 0; k < 8 * 33; ++k) ff_occ[k] = 0;                                                      \
-    if ((e = sweep_prepare_t<(LO) + 0>(perm_occ + 0, minors_occ + 0 * 33, ff_occ + 0 * 33)) != cudaSuccess) return e;     \
-    if ((e = sweep_prepare_t<(LO) + 1>(perm_occ + 1, minors_occ + 1 * 33, ff_occ + 1 * 33)) != cudaSuccess) return e;     \
-    if ((e = sweep_prepare_t<(LO) + 2>(perm_occ + 2, minors_occ + 2 * 33, ff_occ + 2 * 33)) != cudaSuccess) return e;     \
-    if ((e = sweep_prepare_t<(LO) + 3>(perm_occ + 3, minors_occ + 3 * 33, ff_occ + 3 * 33)) != cudaSuccess) return e;     \
-    if ((e = sweep_prepare_t<(LO) + 4>(perm_occ + 4, minors_occ + 4 * 33, ff_occ + 4 * 33)) != cudaSuccess) return e;     \
-    if ((e = sweep_prepare_t<(LO) + 5>(perm_occ + 5, minors_occ + 5 * 33, ff_occ + 5 * 33)) != cudaSuccess) return e;     \
-    if ((e = sweep_prepare_t<(LO) + 6>(perm_occ + 6, minors_occ + 6 * 33, ff_occ + 6 * 33)) != cudaSuccess) return e;     \
-    return sweep_prepare_t<(LO) + 7>(perm_occ + 7, minors_occ + 7 * 33, ff_occ + 7 * 33);              \
+    if ((e = sweep_prepare_t<(LO) + 0>(perm_occ + 0, minors_occ + 0 * 33, ff_occ + 0 * 33, pff_occ + 0)) != cudaSuccess) return e;     \
+    if ((e = sweep_prepare_t<(LO) + 1>(perm_occ + 1, minors_occ + 1 * 33, ff_occ + 1 * 33, pff_occ + 1)) != cudaSuccess) return e;     \
+    if ((e = sweep_prepare_t<(LO) + 2>(perm_occ + 2, minors_occ + 2 * 33, ff_occ + 2 * 33, pff_occ + 2)) != cudaSuccess) return e;     \
+    if ((e = sweep_prepare_t<(LO) + 3>(perm_occ + 3, minors_occ + 3 * 33, ff_occ + 3 * 33, pff_occ + 3)) != cudaSuccess) return e;     \
+    if ((e = sweep_prepare_t<(LO) + 4>(perm_occ + 4, minors_occ + 4 * 33, ff_occ + 4 * 33, pff_occ + 4)) != cudaSuccess) return e;     \
+    if ((e = sweep_prepare_t<(LO) + 5>(perm_occ + 5, minors_occ + 5 * 33, ff_occ + 5 * 33, pff_occ + 5)) != cudaSuccess) return e;     \
+    if ((e = sweep_prepare_t<(LO) + 6>(perm_occ + 6, minors_occ + 6 * 33, ff_occ + 6 * 33, pff_occ + 6)) != cudaSuccess) return e;     \
+    return sweep_prepare_t<(LO) + 7>(perm_occ + 7, minors_occ + 7 * 33, ff_occ + 7 * 33, pff_occ + 7);              \
   }                                                                                                      \
   }
