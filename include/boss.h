@@ -121,7 +121,7 @@ BOSS_API int boss_perm_grad_batch(const double* matrix, int32_t m, const int32_t
  * per timed run; info[0..4] = codes swept per run, algorithmic flops per run
  * (codes x (8 nf - 4): nf complex adds, nf - 1 complex products and one signed
  * add per code), threads, nf, and the FP32 instructions per run of the
- * float-pair sweep (codes x (46.25 nf - 16); 0 in FP64).  info must hold 5
+ * float-pair sweep (codes x (52.25 nf - 22); 0 in FP64).  info must hold 5
  * doubles.  results (optional) receives the permanents.  No reference
  * counterpart.
  */

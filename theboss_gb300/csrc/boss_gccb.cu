@@ -308,7 +308,7 @@ __global__ void __launch_bounds__(kFinWarps * 32) gccb_finalize_kernel(FinalizeA
       }
       mode = a.pmode[(size_t)j * a.n + pop_particle(rem, a.idx[(size_t)j * a.n])];
       S[mode] = 1;
-      sub_s[w][0] = make_double2(1.0, 0.0);
+      subf_s[w][0] = make_float4(1.0f, 0.0f, 0.0f, 0.0f);
       dm_s[w][0] = (uint8_t)mode;
       mult_s[w][0] = 1;
     }
@@ -380,7 +380,7 @@ __global__ void __launch_bounds__(kFinWarps * 32) gccb_finalize_kernel(FinalizeA
       mult_s[w][lane] = P.mult[lane];
     }
   }
-  if (!(a.k > 1 && a.cur_ff) && lane < nd) {  // FP64 minors to float pairs
+  if (a.k > 1 && !a.cur_ff && lane < nd) {  // FP64 minors to float pairs
     const double2 v = sub_s[w][lane];
     float4 f;
     double_to_ff(v.x, f.x, f.y);
@@ -392,9 +392,11 @@ __global__ void __launch_bounds__(kFinWarps * 32) gccb_finalize_kernel(FinalizeA
   // (generalized_cliffords_b_simulation_strategy.py:82-89), then |.|^2.  The
   // Glynn-form sweep already delivers S_i sub_i.  The dot products run on the
   // FP32 pipe as compensated float-pair sums (lane o reads column o of the
-  // transposed float-pair matrix: coalesced); |.|^2 and the cdf are FP64.  The
-  // outputs that do not fill a warp split their digits over several lanes.
+  // transposed float-pair matrix: coalesced), |.|^2 as a float pair (stored in
+  // the warp's pmf row, float2 per output).  The outputs that do not fill a warp
+  // split their digits over several lanes.
   const float4* UT = a.Uff + (size_t)j * a.mstride;
+  float2* pf = reinterpret_cast<float2*>(pmf_s[w]);
   const int full = m & ~31;
   for (int o = lane; o < full; o += 32) {
     float sr = 0.0f, cr = 0.0f, si = 0.0f, ci = 0.0f;
@@ -407,7 +409,7 @@ __global__ void __launch_bounds__(kFinWarps * 32) gccb_finalize_kernel(FinalizeA
       ff_dot_acc(si, ci, 1.0f, c.x, c.y, u.z, u.w);
       ff_dot_acc(si, ci, 1.0f, c.z, c.w, u.x, u.y);
     }
-    pmf_s[w][o] = ff_abs2(sr, cr, si, ci);
+    pf[o] = ff_abs2(sr, cr, si, ci);
   }
   if (m > full) {
     const int r = m - full;
@@ -432,58 +434,57 @@ __global__ void __launch_bounds__(kFinWarps * 32) gccb_finalize_kernel(FinalizeA
       ff_acc(sr, cr, 1.0f, osr, ocr);
       ff_acc(si, ci, 1.0f, osi, oci);
     }
-    if (oi < r && c0 == 0) pmf_s[w][full + oi] = ff_abs2(sr, cr, si, ci);
+    if (oi < r && c0 == 0) pf[full + oi] = ff_abs2(sr, cr, si, ci);
   }
   __syncwarp();
   // theboss normalises with Python's sequential sum, and numpy.random.choice then
   // takes cdf = cumsum(p), cdf /= cdf[-1], searchsorted(cdf, u, 'right')
   // (generalized_cliffords_b_simulation_strategy.py:91-92, 107-110).  Fast path:
-  // the same decisions from a warp scan of the unnormalised pmf compared with
-  // u * total, whose rounding differs from the sequential evaluation by far less
-  // than 1e-12 relative; whenever some cdf entry lies within 1e-12 of the uniform
-  // the sequential evaluation decides.
+  // the same decisions from a float-pair warp scan of the unnormalised pmf
+  // compared with u * total (no division), accurate to ~1e-14, far inside the
+  // 1e-12 window; whenever some cdf entry lies within 1e-12 (relative) of
+  // u * total the sequential FP64 evaluation decides.
   const double uu = a.uni[(size_t)j * a.n + (a.k - 1)];
   const int K = (m + 31) >> 5;  // contiguous outputs per lane
   const int o0 = lane * K;
-  double local = 0.0;
+  float ih = 0.0f, il = 0.0f;
   for (int q = 0; q < K; ++q)
-    if (o0 + q < m) local += pmf_s[w][o0 + q];
-  double incl = local;
+    if (o0 + q < m) ff_acc(ih, il, 1.0f, pf[o0 + q].x, pf[o0 + q].y);
 #pragma unroll
   for (int off = 1; off < 32; off <<= 1) {
-    const double y = __shfl_up_sync(0xffffffffu, incl, off);
-    if (lane >= off) incl += y;
+    const float yh = __shfl_up_sync(0xffffffffu, ih, off), yl = __shfl_up_sync(0xffffffffu, il, off);
+    if (lane >= off) ff_acc(ih, il, 1.0f, yh, yl);
   }
-  const double total_fast = __shfl_sync(0xffffffffu, incl, 31);
-  double excl = __shfl_up_sync(0xffffffffu, incl, 1);
-  if (lane == 0) excl = 0.0;
+  const float th = __shfl_sync(0xffffffffu, ih, 31), tl = __shfl_sync(0xffffffffu, il, 31);
+  float ch = __shfl_up_sync(0xffffffffu, ih, 1), cl = __shfl_up_sync(0xffffffffu, il, 1);
+  if (lane == 0) ch = cl = 0.0f;
   int idx = 0;
-  const long long tb = __double_as_longlong(total_fast);
-  if (!(tb > 0 && tb < 0x7ff0000000000000ll)) {  // not a positive finite double
+  if (!(th > 0.0f && th <= 3.4e38f)) {  // not a positive finite total
     if (lane == 0) atomicOr(a.err, 1);
   } else {
-    // The comparisons are made on the unnormalised cdf against u * total (no
-    // division).  Every cdf entry and u * total are non-negative doubles, whose
-    // order is that of their bit patterns as integers: the comparisons run on the
-    // integer pipe.  An entry is "near" when it lies in [ut (1 - 1e-12), ut (1 + 1e-12)].
-    const double ut = uu * total_fast;
-    const long long ub = __double_as_longlong(ut);
-    const long long lo = __double_as_longlong(fma(-1e-12, ut, ut));
-    const long long hi = __double_as_longlong(fma(1e-12, ut, ut));
-    double c = excl;
+    float uth, utl;
+    double_to_ff(uu, uth, utl);
+    ff_mul(uth, utl, th, tl);  // u * total
+    const float window = 1e-12f * uth;
     int cnt = 0;
     bool near = false;
     for (int q = 0; q < K; ++q) {
       if (o0 + q >= m) break;
-      c += pmf_s[w][o0 + q];  // ~ cdf * total
-      const long long cb = __double_as_longlong(c);
-      near |= (o0 + q < m - 1) && cb >= lo && cb <= hi;
-      cnt += (cb <= ub) ? 1 : 0;
+      ff_acc(ch, cl, 1.0f, pf[o0 + q].x, pf[o0 + q].y);  // ~ cdf * total
+      float dh = ch, dl = cl;
+      ff_acc(dh, dl, -1.0f, uth, utl);  // normalised: its sign is dh's
+      near |= (o0 + q < m - 1) && fabsf(dh) <= window;
+      cnt += (dh <= 0.0f) ? 1 : 0;
     }
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) cnt += __shfl_xor_sync(0xffffffffu, cnt, off);
     idx = cnt < m ? cnt : m - 1;
-    if (__any_sync(0xffffffffu, near)) {  // exact sequential evaluation
+    if (__any_sync(0xffffffffu, near)) {  // exact sequential evaluation in FP64
+      for (int o = lane; o < m; o += 32) {  // the pmf as doubles, in place (same 8-byte slots)
+        const float2 v = pf[o];
+        pmf_s[w][o] = ff_to_double(v.x, v.y);
+      }
+      __syncwarp();
       double total = 0.0;
       if (lane == 0)
         for (int o = 0; o < m; ++o) total += pmf_s[w][o];
@@ -654,7 +655,8 @@ __global__ void __launch_bounds__(kFinWarps * 32) gccb_finalize_kernel(FinalizeA
     P.part_off = ls.part_off;
     // float pairs: the factors' scales 2^(p_f + 1 - fx) multiply the product
     P.ff_off = a.next_ff ? ls.pool_off + (int64_t)(nds + 1) * nf : 0;
-    P.scale = ldexp(1.0, (held ? -(nf - 1) : -nf) + (a.next_ff ? esum - nf * a.fx : 0));
+    const int e2 = (held ? -(nf - 1) : -nf) + (a.next_ff ? esum - nf * a.fx : 0);
+    P.scale = (e2 >= -1022 && e2 <= 1023) ? __longlong_as_double((long long)(e2 + 1023) << 52) : ldexp(1.0, e2);
     P.fixed_digit = held;
     P.group = a.next_tab ? 1 : a.next_group;
   }

@@ -347,15 +347,15 @@ __device__ __forceinline__ void double_to_ff(double x, float& hi, float& lo) {
 }
 
 // |re + i im|^2 for float pairs (re = rs + rc, im = is + ic, unnormalised as a
-// compensated sum leaves them), in float pairs, returned as a double.
-__device__ __forceinline__ double ff_abs2(float rs, float rc, float is, float ic) {
+// compensated sum leaves them), as a normalised float pair.
+__device__ __forceinline__ float2 ff_abs2(float rs, float rc, float is, float ic) {
   float rh = rs + rc, ih = is + ic;
   float rl = rc - (rh - rs), il = ic - (ih - is);  // fast two-sums: |s| >= |c|, or s = 0
   float p, e, q, f;
   ff_prod(rh, rl, rh, rl, p, e);
   ff_prod(ih, il, ih, il, q, f);
   ff_combine(p, e, 1.0f, q, f, rh, rl);
-  return ff_to_double(rh, rl);
+  return make_float2(rh, rl);
 }
 
 // Compensated dot-product step (Ogita, Rump and Oishi, "Accurate sum and dot

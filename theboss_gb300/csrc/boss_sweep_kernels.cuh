@@ -459,7 +459,10 @@ __global__ void __launch_bounds__(128, kFFMinBlocks<NF>) minors_sweep_ff_kernel(
 
 // Single permanents with float pairs: perm_sweep_kernel's walk with the
 // float-pair machinery of the all-minors sweep (exact sums in shared memory,
-// resynchronised every kFFResync codes, lazily renormalised sums and products).
+// resynchronised every kFFResync codes, lazily renormalised sums).  The products
+// stay renormalised: a single permanent of 26-30 particles cancels more than the
+// sampler's minors, and this keeps it 2-5x closer to double-double (n = 28:
+// ~1e-11) at no measurable cost.
 // Each thread writes its partial as a float pair (float4) in the factors' scales.
 constexpr int kFFPermMaxFactors = 32;
 template <int NF>
@@ -496,7 +499,7 @@ __global__ void __launch_bounds__(128, kFFPermMinBlocks<NF>) perm_sweep_ff_kerne
       {
         ffc p = S[0];
 #pragma unroll
-        for (int f = 1; f < NF; ++f) p = ff_cmul_lazy(p, S[f]);
+        for (int f = 1; f < NF; ++f) p = ff_cmul(p, S[f]);
         const float sg = parity ? -1.0f : 1.0f;
         ff_add_lazy(A.rh, A.rl, sg, p.rh, p.rl);
         ff_add_lazy(A.ih, A.il, sg, p.ih, p.il);
