@@ -230,12 +230,13 @@ struct FinalizeArgs {
   const float4* Uff;      // m x m transposed, Uff[i * m + o] = U[o][i] as float pairs (re hi, re lo, im hi, im lo)
   uint8_t* S;             // [sample][m] current input occupations
   uint8_t* T;             // [sample][m] output occupations
-  const uint8_t* idx;     // [sample][n] randint results (position among the particles left)
-  const uint8_t* pmode;   // [sample][n] particle -> input mode
-  const uint8_t* npart;   // [sample] input particles
+  const int32_t* order;   // [sample in level order] -> its row in the replayed (input-order) draws
+  const uint8_t* idx;     // [input-order sample][n] randint results (position among the particles left)
+  const uint8_t* pmode;   // [input-order sample][n] particle -> input mode
+  const uint8_t* npart;   // [input-order sample] input particles
   int64_t mstride;        // elements between the samples' matrices (0: one matrix for all)
   uint32_t* rem;          // [sample][8] particles not yet popped, as bits
-  const double* uni;      // [sample][n] uniforms
+  const double* uni;      // [input-order sample][n] uniforms
   const SweepProblem* probs_cur;
   const uint8_t* dmode_cur;  // [sample][32]
   const double2* partials;
@@ -290,7 +291,6 @@ __global__ void __launch_bounds__(kFinWarps * 32) gccb_finalize_kernel(FinalizeA
   const int j = blockIdx.x * kFinWarps + w;
   if (j >= a.A) return;
   const int m = a.m;
-  const double2* Us = a.U + (size_t)j * a.mstride;        // this sample's matrix
   const longlong2* Ufxs = a.Ufx + (size_t)j * a.mstride;  // and its fixed-point copy
   uint8_t* S = a.S + (size_t)j * m;
   uint8_t* T = a.T + (size_t)j * m;
@@ -301,12 +301,13 @@ __global__ void __launch_bounds__(kFinWarps * 32) gccb_finalize_kernel(FinalizeA
     int mode = 0;
     if (lane == 0) {
       uint32_t* rem = a.rem + (size_t)j * 8;
-      const int np = a.npart[j];
+      const int np = a.npart[a.order[j]];
       for (int q = 0; q < 8; ++q) {
         const int lo = q * 32;
         rem[q] = (np >= lo + 32) ? 0xffffffffu : (np > lo ? ((1u << (np - lo)) - 1u) : 0u);
       }
-      mode = a.pmode[(size_t)j * a.n + pop_particle(rem, a.idx[(size_t)j * a.n])];
+      const size_t row = (size_t)a.order[j] * a.n;
+      mode = a.pmode[row + pop_particle(rem, a.idx[row])];
       S[mode] = 1;
       subf_s[w][0] = make_float4(1.0f, 0.0f, 0.0f, 0.0f);
       dm_s[w][0] = (uint8_t)mode;
@@ -444,7 +445,8 @@ __global__ void __launch_bounds__(kFinWarps * 32) gccb_finalize_kernel(FinalizeA
   // compared with u * total (no division), accurate to ~1e-14, far inside the
   // 1e-12 window; whenever some cdf entry lies within 1e-12 (relative) of
   // u * total the sequential FP64 evaluation decides.
-  const double uu = a.uni[(size_t)j * a.n + (a.k - 1)];
+  const size_t drow = (size_t)a.order[j] * a.n;  // this sample's replayed draws
+  const double uu = a.uni[drow + (a.k - 1)];
   const int K = (m + 31) >> 5;  // contiguous outputs per lane
   const int o0 = lane * K;
   float ih = 0.0f, il = 0.0f;
@@ -513,7 +515,7 @@ __global__ void __launch_bounds__(kFinWarps * 32) gccb_finalize_kernel(FinalizeA
 
   // ---- the all-minors sweep of level k + 1 ----
   if (lane == 0) {
-    const int mode = a.pmode[(size_t)j * a.n + pop_particle(a.rem + (size_t)j * 8, a.idx[(size_t)j * a.n + a.k])];
+    const int mode = a.pmode[drow + pop_particle(a.rem + (size_t)j * 8, a.idx[drow + a.k])];
     S[mode] = (uint8_t)(S[mode] + 1);
   }
   __syncwarp();
@@ -895,6 +897,7 @@ static int gccb_prepare(Context* cx, const double* matrix, int n_mats, int m, Dr
   const size_t o_err = off; off = al(off + sizeof(int));
   std::vector<size_t> o_tab(Lmax + 2, 0);
   for (int k = 2; k <= Lmax; ++k) { o_tab[k] = off; off = al(off + sizeof(LevelSample) * tab[k].size()); }
+  const size_t o_ord = off; off = al(off + sizeof(int32_t) * (size_t)N);
   const size_t o_idx = off; off = al(off + (size_t)N * n);
   const size_t o_pm = off; off = al(off + (size_t)N * n);
   const size_t o_np = off; off = al(off + (size_t)N);
@@ -914,22 +917,22 @@ static int gccb_prepare(Context* cx, const double* matrix, int n_mats, int m, Dr
   if ((st = ensure(B[7], 32 * (size_t)m * m * n_mats))) return st;  // U fixed point | U^T float pairs
   if ((st = ensure_slot_pinned(slot, std::max(arena, al((size_t)N * m) + 256)))) return st;
   char* h = (char*)g_gccb_pinned[slot];
-  memset(h, 0, o_idx);
+  memset(h, 0, o_ord);
   for (int k = 2; k <= Lmax; ++k) memcpy(h + o_tab[k], tab[k].data(), sizeof(LevelSample) * tab[k].size());
-  uint8_t* hidx = (uint8_t*)(h + o_idx);
-  uint8_t* hpm = (uint8_t*)(h + o_pm);
-  uint8_t* hnp = (uint8_t*)(h + o_np);
-  double* huni = (double*)(h + o_uni);
+  // The draws stay in input order (bulk copies); the kernels reach a sample's
+  // row through the level-order permutation.
+  memcpy(h + o_ord, order.data(), sizeof(int32_t) * (size_t)N);
+  memcpy(h + o_idx, D.idx.data(), (size_t)N * n);
+  memcpy(h + o_pm, D.particles.data(), (size_t)N * n);
+  memcpy(h + o_np, D.nparticles.data(), (size_t)N);
+  memcpy(h + o_uni, D.u.data(), sizeof(double) * (size_t)N * n);
   const size_t mm = (size_t)m * m;
-  for (int jj = 0; jj < N; ++jj) {  // samples in level order
-    const int s = order[jj];
-    memcpy(hidx + (size_t)jj * n, &D.idx[(size_t)s * n], n);
-    memcpy(huni + (size_t)jj * n, &D.u[(size_t)s * n], sizeof(double) * n);
-    memcpy(hpm + (size_t)jj * n, &D.particles[(size_t)s * n], n);
-    hnp[jj] = D.nparticles[s];
-    if (n_mats > 1) memcpy(h + o_U + sizeof(double2) * mm * jj, matrix + 2 * mm * s, sizeof(double2) * mm);
+  if (n_mats > 1) {  // instances: matrices in level order
+    for (int jj = 0; jj < N; ++jj)
+      memcpy(h + o_U + sizeof(double2) * mm * jj, matrix + 2 * mm * order[jj], sizeof(double2) * mm);
+  } else {
+    memcpy(h + o_U, matrix, sizeof(double2) * mm);
   }
-  if (n_mats == 1) memcpy(h + o_U, matrix, sizeof(double2) * mm);
   char* d = (char*)B[0].ptr;
   uint8_t* dS = (uint8_t*)B[1].ptr;
   R.dT = dS + (size_t)N * m;
@@ -996,6 +999,7 @@ static int gccb_prepare(Context* cx, const double* matrix, int n_mats, int m, Dr
     fa.Uff = dUff;
     fa.mstride = (n_mats > 1) ? (int64_t)mm : 0;
     fa.npart = (const uint8_t*)(d + o_np);
+    fa.order = (const int32_t*)(d + o_ord);
     fa.S = dS;
     fa.T = R.dT;
     fa.idx = (const uint8_t*)(d + o_idx);
