@@ -427,7 +427,7 @@ def gccb_sample(U: np.ndarray, input_state, weights, n_samples: int) -> np.ndarr
         raise AttributeError("input state length differs from the matrix dimension")
     w, nw, wp = _weights_arg(weights)
     st, key, pos = _get_mt()
-    out = np.zeros((n_samples, m), dtype=np.int32)
+    out = np.empty((n_samples, m), dtype=np.int32)  # every row is written
     check(L.boss_gccb_sample(_dp(U.view(np.float64)), m, _ip(inp), wp, nw,
                              key.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32)), _ip(pos), n_samples, _ip(out)))
     _set_mt(st, key, pos)

@@ -1186,7 +1186,6 @@ int boss_gccb_sample_slice(const double* matrix, int32_t m, const int32_t* input
   int st = load_mt(mt, mt_key, mt_pos);
   if (st) return st;
   const int nw = particle_weights ? n_weights : 0;
-  if (count > 0) memset(samples, 0, sizeof(int32_t) * (size_t)count * m);
   // Large batches run as two parts: the host replays and plans the second part
   // while the GPU samples the first (separate buffers, pinned memory and graphs).
   // The first part is a quarter, so that the GPU starts early and the host's work
@@ -1220,8 +1219,14 @@ int boss_gccb_sample_slice(const double* matrix, int32_t m, const int32_t* input
   if (cx) {
     cudaError_t e = cudaStreamSynchronize(cx->stream);
     if (e != cudaSuccess) return fail_cuda(e, "sampler");
-    for (int h = 0; h < halves; ++h)
-      if (launched[h] && (st = gccb_read_results(R[h], samples + (size_t)(cut[h] - first) * m))) return st;
+  }
+  for (int h = 0; h < halves && count > 0; ++h) {  // every row is written: sampled, or empty
+    int32_t* rows = samples + (size_t)(cut[h] - first) * m;
+    if (launched[h]) {
+      if ((st = gccb_read_results(R[h], rows))) return st;
+    } else {
+      memset(rows, 0, sizeof(int32_t) * (size_t)(cut[h + 1] - cut[h]) * m);
+    }
   }
   memcpy(mt_key, mt.key, sizeof(mt.key));
   *mt_pos = mt.pos;
