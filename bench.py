@@ -432,9 +432,10 @@ def roofline(b, sweep_s, achieved, peak, peak32, traffic):
         return {"bound": "fp32", "kernel": "minors_sweep_ff_kernel (all levels of a step)",
                 "achieved": ach32, "peak": peak32, "unit": "T FP32 inst/s", "frac": ach32 / peak32,
                 "peak_source": "boss_fp32_peak (independent FFMA chains), measured in this run",
-                "inst_note": "float-pair arithmetic, 46.25 nf FP32 instructions per Guan code at nf = k - 1 "
-                             "factors (32 per complex product, 16 per complex sum, lazily renormalised); "
-                             "integer, load and conversion instructions not counted",
+                "inst_note": "float-pair arithmetic, 47.5625 nf FP32 instructions per Guan code at nf = k - 1 "
+                             "factors (32 per complex product, 16 per complex sum, lazily renormalised, "
+                             "resynchronised every 32 codes); integer, load and conversion instructions "
+                             "not counted",
                 "fp32_inst_per_step": b["ff_inst"],
                 "fp64_equivalent": {"achieved_tflops": achieved, "fp64_peak_tflops": peak,
                                     "ratio_to_fp64_peak": achieved / peak}, **common}

@@ -121,7 +121,7 @@ BOSS_API int boss_perm_grad_batch(const double* matrix, int32_t m, const int32_t
  * per timed run; info[0..4] = codes swept per run, algorithmic flops per run
  * (codes x (8 nf - 4): nf complex adds, nf - 1 complex products and one signed
  * add per code), threads, nf, and the FP32 instructions per run of the
- * float-pair sweep (codes x (52.25 nf - 22); 0 in FP64).  info must hold 5
+ * float-pair sweep (codes x (53.125 nf - 22); 0 in FP64).  info must hold 5
  * doubles.  results (optional) receives the permanents.  No reference
  * counterpart.
  */
@@ -198,9 +198,9 @@ BOSS_API int boss_perm_arithmetic(int32_t mode, int32_t* previous);
  * D2H bytes of one boss_gccb_sample call, kernels per run, sweep launches per
  * run, the deepest level, the same flop count over theboss's Ryser-form codes
  * (twice as many for single photons), and the FP32 instructions per run of the
- * float-pair sweeps (46.25 nf per code at nf factors: nf - 1 float-pair
+ * float-pair sweeps (47.5625 nf per code at nf factors: nf - 1 float-pair
  * complex products of 32, two complex float-pair sums of 16 for the running
- * total and a minor, 7/8 of the codes 16 per factor to move the sums, 1/8 of
+ * total and a minor, 31/32 of the codes 16 per factor to move the sums, 1/32 of
  * them 2 per factor to convert; 0 when the sweeps run in FP64).  info must hold 8 doubles.  samples
  * (optional) receives the last run's samples.  No reference counterpart.
  */

@@ -904,8 +904,8 @@ int boss_perm_bench(const double* matrix, int32_t m, const int32_t* input_states
   info[2] = (double)B.L.total_threads;
   info[3] = (double)B.nf;
   // float pairs: nf - 1 renormalised complex products of 38, one complex sum of
-  // 16, 7/8 of the codes 16 per factor to move the sums, 1/8 of them 2 per factor
-  info[4] = B.ff ? B.codes * (52.25 * B.nf - 22.0) : 0.0;
+  // 16, 15/16 of the codes 16 per factor to move the sums, 1/16 of them 2 per factor
+  info[4] = B.ff ? B.codes * (53.125 * B.nf - 22.0) : 0.0;
   return kOk;
 }
 

@@ -778,7 +778,7 @@ static int gccb_prepare(Context* cx, const double* matrix, int n_mats, int m, Dr
   std::vector<char> ffl(Lmax + 2, 0);  // level k's sweep runs on float pairs
   for (int k = 2; k <= Lmax; ++k) ffl[k] = (g_minors_arith == 0 && minors_ff_available(k - 1)) ? 1 : 0;
   // FP32 instructions per code of a float-pair sweep with nf = k - 1 factors
-  auto ff_per_code = [&](int k) { return ffl[k] ? 46.25 * (k - 1) : 0.0; };
+  auto ff_per_code = [&](int k) { return ffl[k] ? 47.5625 * (k - 1) : 0.0; };
   R.sweep_flops = 0.0;
   R.ref_flops = 0.0;
   R.ff_inst = 0.0;

@@ -208,10 +208,16 @@ __global__ void __launch_bounds__(128) minors_sweep_kernel(const SweepProblem* _
 //     are brought up to the current code by the digits that flipped since, and
 //     converted (fx_to_ff); in between the float-pair sums move by the
 //     float-pair rows of D.  The drift between two resynchronisations is a few
-//     units of 2^-47 of the rows.
+//     units of 2^-47 of the rows per code in between.
 // ---------------------------------------------------------------------------
 constexpr int kFFMaxFactors = 24;  // above this the float-pair sums exhaust the registers
-constexpr uint64_t kFFResync = 8;
+// Codes between two resynchronisations of the float-pair sums with the exact
+// ones: the all-minors sweeps 32 (measured at n = 20, 10^4 samples: 8 -> 16 -> 32
+// -> 64 gave 1.72, 1.55, 1.47, 1.43 ms per step, and max error against
+// double-double at k = 22 of 2.9e-12, 3.6e-12, 5.6e-12, 6.8e-12), single
+// permanents 16 (their larger sweeps cancel more).
+constexpr uint64_t kFFResync = 32;
+constexpr uint64_t kFFPermResync = 16;
 // Resident blocks of 128 threads the register allocation must allow.
 #ifndef BOSS_FF_MINB_LO
 #define BOSS_FF_MINB_LO 4
@@ -459,7 +465,7 @@ __global__ void __launch_bounds__(128, kFFMinBlocks<NF>) minors_sweep_ff_kernel(
 
 // Single permanents with float pairs: perm_sweep_kernel's walk with the
 // float-pair machinery of the all-minors sweep (exact sums in shared memory,
-// resynchronised every kFFResync codes, lazily renormalised sums).  The products
+// resynchronised every kFFPermResync codes, lazily renormalised sums).  The products
 // stay renormalised: a single permanent of 26-30 particles cancels more than the
 // sampler's minors, and this keeps it 2-5x closer to double-double (n = 28:
 // ~1e-11) at no measurable cost.
@@ -511,7 +517,7 @@ __global__ void __launch_bounds__(128, kFFPermMinBlocks<NF>) perm_sweep_ff_kerne
         const uint32_t bit = (uint32_t)(g >> i) & 1u;
         g ^= 1ull << i;
         parity ^= 1u;
-        if (((tn - (uint64_t)a) & (kFFResync - 1)) == 0) {
+        if (((tn - (uint64_t)a) & (kFFPermResync - 1)) == 0) {
           resync_ff<NF>(D, fb, g, g_int, SS, S);
           g_int = g;
         } else {
