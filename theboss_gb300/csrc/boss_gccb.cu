@@ -225,7 +225,6 @@ struct FinalizeArgs {
   int m;
   int n;       // row stride of idx / uni
   int fx;      // fixed-point fraction bits of the sweep rows
-  const double2* U;       // m x m
   const longlong2* Ufx;   // m x m, U * 2^fx rounded
   const float4* Uff;      // m x m transposed, Uff[i * m + o] = U[o][i] as float pairs (re hi, re lo, im hi, im lo)
   uint8_t* S;             // [sample][m] current input occupations
@@ -994,7 +993,6 @@ static int gccb_prepare(Context* cx, const double* matrix, int n_mats, int m, Dr
     fa.m = m;
     fa.n = n;
     fa.fx = fx;
-    fa.U = (const double2*)(d + o_U);
     fa.Ufx = dUfx;
     fa.Uff = dUff;
     fa.mstride = (n_mats > 1) ? (int64_t)mm : 0;
