@@ -46,3 +46,25 @@ def test_no_gpu_calls_fail_loudly_without_device():
         pytest.skip("a GPU is present")
     with pytest.raises(_native.GB300Error):
         RyserPermanentCalculator(np.eye(3, dtype=complex), [1, 1, 0], [1, 1, 0]).compute_permanent()
+
+
+def test_arithmetic_switches_set_query_and_reject_bad_modes():
+    """boss_minors_arithmetic / boss_perm_arithmetic only record the choice (no
+    GPU needed): float pairs by default, FP64 on request, -1 queries."""
+    import pytest
+    from theboss_gb300 import _native
+
+    for setter in (_native.minors_arithmetic, _native.perm_arithmetic):
+        start = setter(-1)
+        assert start in (_native.FLOAT_PAIRS, _native.FP64)
+        try:
+            assert setter(_native.FP64) == start
+            assert setter(-1) == _native.FP64
+            assert setter(_native.FLOAT_PAIRS) == _native.FP64
+            assert setter(-1) == _native.FLOAT_PAIRS
+            with pytest.raises(ValueError):  # BOSS_ERR_ARG
+                setter(2)
+            assert setter(-1) == _native.FLOAT_PAIRS
+        finally:
+            setter(start)
+    assert _native.minors_arithmetic(-1) == _native.FLOAT_PAIRS  # the library's default
