@@ -319,9 +319,12 @@ __global__ void __launch_bounds__(kFinWarps * 32) gccb_finalize_kernel(FinalizeA
     const int64_t parts = P.n_threads / P.group;
     if (a.cur_ff) {
       // float-pair partials: summed as float pairs in a fixed order, scaled by the
-      // problem's power of two (exact in float at these sizes)
+      // problem's power of two, exactly in float when that power is a normal float
+      // (always, for factors of comparable size); otherwise in FP64 below
       const float4* fp = reinterpret_cast<const float4*>(a.partials) + P.part_off;
-      const float sc = __double2float_rn(P.scale);
+      const int sc_exp = (int)((__double_as_longlong(P.scale) >> 52) & 0x7FF) - 1023;
+      const bool sc_float = sc_exp >= -126 && sc_exp <= 127;
+      const float sc = sc_float ? __double2float_rn(P.scale) : 1.0f;
       if (parts <= 64) {
         if (lane < nd) {
           float rh = 0.0f, rl = 0.0f, ih = 0.0f, il = 0.0f;
@@ -378,6 +381,17 @@ __global__ void __launch_bounds__(kFinWarps * 32) gccb_finalize_kernel(FinalizeA
     if (lane < nd) {
       dm_s[w][lane] = a.dmode_cur[(size_t)j * 32 + lane];
       mult_s[w][lane] = P.mult[lane];
+    }
+  }
+  if (a.k > 1 && a.cur_ff && lane < nd) {  // a scale beyond the float range: apply it in FP64
+    const SweepProblem& P = a.probs_cur[j];
+    const int sc_exp = (int)((__double_as_longlong(P.scale) >> 52) & 0x7FF) - 1023;
+    if (!(sc_exp >= -126 && sc_exp <= 127)) {
+      const float4 u = subf_s[w][lane];
+      float4 f;
+      double_to_ff(ff_to_double(u.x, u.y) * P.scale, f.x, f.y);
+      double_to_ff(ff_to_double(u.z, u.w) * P.scale, f.z, f.w);
+      subf_s[w][lane] = f;
     }
   }
   if (a.k > 1 && !a.cur_ff && lane < nd) {  // FP64 minors to float pairs
