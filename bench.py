@@ -216,12 +216,18 @@ def c2_patterns(n, count, seed):
 def single_permanents(peak_tflops, seed, peak32=None):
     """C2: 64 Glynn permanents per size, device-timed; the relative error of the
     first pattern against the double-double oracle for n <= 24 (its CPU cost grows
-    as 2^n: 7 s at n = 24 on 16 Arm cores, 170 s at n = 28)."""
+    as 2^n: 7 s at n = 24 on 16 Arm cores, 170 s at n = 28), and for n = 28, 30
+    against the double-double values computed once (tests/golden/c2_dd_large.json)."""
     from oracle import oracle as O
     from theboss_gb300 import _native
     from theboss_gb300.utilities import haar_unitary
 
     res = {}
+    large_dd = {}
+    fixture = os.path.join(ROOT, "tests", "golden", "c2_dd_large.json")
+    if os.path.exists(fixture):
+        for rec in json.load(open(fixture)):
+            large_dd.setdefault((rec["seed"], rec["n"]), []).append(rec)
     for n in (16, 20, 24, 28, 30):
         U = haar_unitary(2 * n, seed + n)
         T = c2_patterns(n, 64, seed + n)
@@ -240,6 +246,12 @@ def single_permanents(peak_tflops, seed, peak32=None):
             hi, lo = O.perm_dd(U, S[0], T[0])
             ref = hi + lo
             res[str(n)]["rel_err_vs_dd_pattern0"] = float(abs(b["results"][0] - ref) / abs(ref))
+        else:  # double-double values computed once (tests/golden/make_c2_dd.py)
+            for rec in large_dd.get((seed + n, n), []):
+                if abs(U[0, 0] - complex(*rec["U00"])) <= 1e-12 and list(T[rec["pattern"]]) == rec["T"]:
+                    ref = complex(rec["dd"][0], rec["dd"][1]) + complex(rec["dd"][2], rec["dd"][3])
+                    res[str(n)][f"rel_err_vs_dd_pattern{rec['pattern']}"] = float(
+                        abs(b["results"][rec["pattern"]] - ref) / abs(ref))
     return res
 
 

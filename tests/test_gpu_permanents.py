@@ -169,3 +169,34 @@ def test_submatrices_against_double_double(oracle, k, minors_arith):
     scale = max(abs(v) for v in ref)
     err = max(abs(a - b) for a, b in zip(got, ref)) / scale
     assert err <= 1e-10, (k, minors_arith, err)
+
+
+def test_large_permanents_against_double_double_fixture():
+    """C2 patterns at n = 26, 28, 30 (single photons in 2n modes, ~20% doubly
+    occupied outputs) against double-double values computed once by the oracle
+    (tests/golden/make_c2_dd.py): float pairs (the default) and FP64 both within
+    1e-10."""
+    import json
+    import os
+
+    from conftest import ROOT
+    from theboss_gb300 import _native
+    from theboss_gb300.utilities import haar_unitary
+
+    recs = json.load(open(os.path.join(ROOT, "tests", "golden", "c2_dd_large.json")))
+    assert {r["n"] for r in recs} == {26, 28, 30}
+    for r in recs:
+        n = r["n"]
+        U = haar_unitary(2 * n, r["seed"])
+        assert abs(U[0, 0] - complex(*r["U00"])) <= 1e-12, "matrix generator changed"
+        S = np.zeros((1, 2 * n), dtype=np.int32)
+        S[0, :n] = 1
+        T = np.array([r["T"]], dtype=np.int32)
+        ref = complex(r["dd"][0], r["dd"][1]) + complex(r["dd"][2], r["dd"][3])
+        for mode in (_native.FLOAT_PAIRS, _native.FP64):
+            prev = _native.perm_arithmetic(mode)
+            try:
+                got = _native.perm_batch(U, S, T, _native.GLYNN)[0]
+            finally:
+                _native.perm_arithmetic(prev)
+            assert abs(got - ref) <= 1e-10 * abs(ref), (n, r["pattern"], mode, abs(got - ref) / abs(ref))
