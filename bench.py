@@ -61,7 +61,18 @@ def parse():
                          "Glynn permanents or permanents with all n^2 derivatives, n photons in 2n modes")
     ap.add_argument("--n", type=int, default=24, help="photons of --case")
     ap.add_argument("--patterns", type=int, default=16, help="output patterns of --case")
+    ap.add_argument("--arith", choices=["ff", "fp64"], default="ff",
+                    help="arithmetic of the sweeps: float pairs on the FP32 pipe (default) or FP64 sweeps "
+                         "(boss_minors_arithmetic / boss_perm_arithmetic)")
     return ap.parse_args()
+
+
+def set_arithmetic(args):
+    if args.arith == "fp64":
+        from theboss_gb300 import _native
+
+        _native.minors_arithmetic(_native.FP64)
+        _native.perm_arithmetic(_native.FP64)
 
 
 def run_case(args):
@@ -70,6 +81,7 @@ def run_case(args):
     from theboss_gb300 import _native
     from theboss_gb300.utilities import haar_unitary
 
+    set_arithmetic(args)
     m = 2 * args.n
     U = haar_unitary(m, args.seed + args.n)
     T = c2_patterns(args.n, args.patterns, args.seed + args.n)
@@ -426,7 +438,7 @@ def strategies_section(seed):
 
 # arithmetic of the path: exact int64 fixed-point row sums, float-pair (two FP32,
 # ~47-bit) products and minors in the sweeps and the Laplace step, FP64 pmf and cdf
-DTYPE = "i64 fixed point + f32x2 float pairs (~47-bit); f64 pmf/cdf"
+DTYPE = "i64 fixed point + f32x2 float pairs (~47-bit); f64 cdf fallback"
 
 
 def roofline(b, sweep_s, achieved, peak, peak32, traffic):
@@ -461,6 +473,7 @@ def run_ours(args, rank, world):
     from theboss_gb300.simulation_strategies import GCCBPlainDriver
     from theboss_gb300.permanent_calculators import RyserPermanentCalculator
 
+    set_arithmetic(args)
     U, inp, w = workload(args.seed)
     peak, _ = _native.fp64_peak()
     peak32, _ = _native.fp32_peak()

@@ -174,7 +174,8 @@ BOSS_API int boss_gccb_sample(const double* matrix, int32_t m, const int32_t* in
 // numpy float64, bs_cc_ryser_submatrices_permanent_calculator.py:96-119).
 // mode 0 (default): products, running totals and minors as float pairs (two
 // FP32 values, about 47 significant bits) on the FP32 pipe, for sweeps of at
-// most 24 product-side particles; mode 1: FP64 throughout; -1: query only.
+// most 24 product-side particles; mode 1: FP64 sweeps (the sampler's Laplace
+// step and cdf scan stay float pairs, with the exact FP64 fallback); -1: query only.
 // *previous (if not null) receives the mode in force before the call.  Row sums
 // are exact 64-bit fixed point in both.
 BOSS_API int boss_minors_arithmetic(int32_t mode, int32_t* previous);
