@@ -61,18 +61,18 @@ def parse():
                          "Glynn permanents or permanents with all n^2 derivatives, n photons in 2n modes")
     ap.add_argument("--n", type=int, default=24, help="photons of --case")
     ap.add_argument("--patterns", type=int, default=16, help="output patterns of --case")
-    ap.add_argument("--arith", choices=["ff", "fp64"], default="ff",
-                    help="arithmetic of the sweeps: float pairs on the FP32 pipe (default) or FP64 sweeps "
-                         "(boss_minors_arithmetic / boss_perm_arithmetic)")
+    ap.add_argument("--arith", choices=["ff", "fp64"], default="fp64",
+                    help="arithmetic of the sweeps and the sampler's pmf: FP64 (default, theboss's float64) or "
+                         "float pairs on the FP32 pipe (boss_minors_arithmetic / boss_perm_arithmetic)")
     return ap.parse_args()
 
 
 def set_arithmetic(args):
-    if args.arith == "fp64":
-        from theboss_gb300 import _native
+    from theboss_gb300 import _native
 
-        _native.minors_arithmetic(_native.FP64)
-        _native.perm_arithmetic(_native.FP64)
+    mode = _native.FP64 if args.arith == "fp64" else _native.FLOAT_PAIRS
+    _native.minors_arithmetic(mode)
+    _native.perm_arithmetic(mode)
 
 
 def run_case(args):
@@ -184,9 +184,11 @@ class Clocks:
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def cpu_baseline(U, inp, w, seed, budget_s=10.0):
+def cpu_baseline(U, inp, w, seed, budget_s=10.0, gpu_samples=None):
     """theboss's sampler restated in C (oracle/) on all host threads, on a bounded
-    sample of the workload sized to about budget_s seconds."""
+    sample of the workload sized to about budget_s seconds.  The sample starts at
+    the same seed as the GPU's timed step, so its first len(gpu_samples) samples are
+    the oracle's stream for the GPU's: they are compared (the parity record)."""
     from oracle import oracle as O
 
     threads = os.cpu_count() or 1
@@ -197,16 +199,23 @@ def cpu_baseline(U, inp, w, seed, budget_s=10.0):
         np.random.seed(seed)
         L, A, Uu = O.predraw_gccb(list(inp), n, w)
         t = time.perf_counter()
-        O.gccb_run(U, L, A, Uu)
-        return time.perf_counter() - t
+        out = O.gccb_run(U, L, A, Uu)
+        return time.perf_counter() - t, (L, A, Uu, out)
 
     probe = 200
-    dt = run(probe)
+    dt, _ = run(probe)
     n = int(min(10 ** 5, max(probe, probe * budget_s / max(dt, 1e-6))))
-    dt = run(n)
-    return {"value": n / dt, "unit": "samples/s", "cores": int(os.environ["OMP_NUM_THREADS"]), "kind": "port",
-            "sample": f"{n} samples of the workload (same seed and matrix), C restatement of theboss's "
-                      f"GCC-B sampler, OpenMP over samples, {dt:.1f} s"}
+    if gpu_samples is not None:
+        n = max(n, len(gpu_samples))
+    dt, (L, A, Uu, out) = run(n)
+    res = {"value": n / dt, "unit": "samples/s", "cores": int(os.environ["OMP_NUM_THREADS"]), "kind": "port",
+           "sample": f"{n} samples of the workload (same seed and matrix), C restatement of theboss's "
+                     f"GCC-B sampler, OpenMP over samples, {dt:.1f} s"}
+    parity = None
+    if gpu_samples is not None:
+        N = len(gpu_samples)
+        parity = O.classify_mismatches(U, L[:N], A[:N], Uu[:N], gpu_samples, out[:N])
+    return res, parity
 
 
 def c2_patterns(n, count, seed):
@@ -226,10 +235,12 @@ def c2_patterns(n, count, seed):
 
 
 def single_permanents(peak_tflops, seed, peak32=None):
-    """C2: 64 Glynn permanents per size, device-timed; the relative error of the
-    first pattern against the double-double oracle for n <= 24 (its CPU cost grows
-    as 2^n: 7 s at n = 24 on 16 Arm cores, 170 s at n = 28), and for n = 28, 30
-    against the double-double values computed once (tests/golden/c2_dd_large.json)."""
+    """C2: 64 Glynn permanents per size, device-timed, FP64 (the default); the
+    relative error of the first pattern against the double-double oracle for
+    n <= 24 (its CPU cost grows as 2^n: 7 s at n = 24 on 16 Arm cores, 170 s at
+    n = 28), and for n = 26, 28, 30 against the double-double values computed once
+    (tests/golden/c2_dd_large.json).  The opt-in float-pair kernel is timed on the
+    same batches beside it, with its errors."""
     from oracle import oracle as O
     from theboss_gb300 import _native
     from theboss_gb300.utilities import haar_unitary
@@ -240,6 +251,20 @@ def single_permanents(peak_tflops, seed, peak32=None):
     if os.path.exists(fixture):
         for rec in json.load(open(fixture)):
             large_dd.setdefault((rec["seed"], rec["n"]), []).append(rec)
+
+    def errors(n, U, S, T, vals):
+        out = {}
+        if n <= 24:
+            hi, lo = O.perm_dd(U, S[0], T[0])
+            ref = hi + lo
+            out["rel_err_vs_dd_pattern0"] = float(abs(vals[0] - ref) / abs(ref))
+        else:  # double-double values computed once (tests/golden/make_c2_dd.py)
+            for rec in large_dd.get((seed + n, n), []):
+                if abs(U[0, 0] - complex(*rec["U00"])) <= 1e-12 and list(T[rec["pattern"]]) == rec["T"]:
+                    ref = complex(rec["dd"][0], rec["dd"][1]) + complex(rec["dd"][2], rec["dd"][3])
+                    out[f"rel_err_vs_dd_pattern{rec['pattern']}"] = float(abs(vals[rec["pattern"]] - ref) / abs(ref))
+        return out
+
     for n in (16, 20, 24, 28, 30):
         U = haar_unitary(2 * n, seed + n)
         T = c2_patterns(n, 64, seed + n)
@@ -248,22 +273,19 @@ def single_permanents(peak_tflops, seed, peak32=None):
         b = _native.perm_bench(U, S, T, _native.GLYNN, warmup=1, steps=2 if n >= 28 else 5)
         ms = float(np.mean(b["sweep_ms"]))
         tf = b["flops"] / (ms / 1e3) / 1e12
-        res[str(n)] = {"perms_per_s": 64 / (ms / 1e3), "ms_per_64": ms, "codes": b["codes"],
-                       "achieved_tflops": tf, "frac_of_fp64_peak": tf / peak_tflops}
-        if b["ff_inst"] > 0 and peak32:  # float-pair sweep: its FP32 roofline
-            t32 = b["ff_inst"] / (ms / 1e3) / 1e12
-            res[str(n)].update({"arithmetic": "float pairs", "achieved_t_fp32_inst": t32,
-                                "frac_of_fp32_peak": t32 / peak32})
-        if n <= 24:
-            hi, lo = O.perm_dd(U, S[0], T[0])
-            ref = hi + lo
-            res[str(n)]["rel_err_vs_dd_pattern0"] = float(abs(b["results"][0] - ref) / abs(ref))
-        else:  # double-double values computed once (tests/golden/make_c2_dd.py)
-            for rec in large_dd.get((seed + n, n), []):
-                if abs(U[0, 0] - complex(*rec["U00"])) <= 1e-12 and list(T[rec["pattern"]]) == rec["T"]:
-                    ref = complex(rec["dd"][0], rec["dd"][1]) + complex(rec["dd"][2], rec["dd"][3])
-                    res[str(n)][f"rel_err_vs_dd_pattern{rec['pattern']}"] = float(
-                        abs(b["results"][rec["pattern"]] - ref) / abs(ref))
+        res[str(n)] = {"perms_per_s": 64 / (ms / 1e3), "ms_per_64": ms, "codes": b["codes"], "arithmetic": "fp64",
+                       "achieved_tflops": tf, "frac_of_fp64_peak": tf / peak_tflops, **errors(n, U, S, T, b["results"])}
+        prev = _native.perm_arithmetic(_native.FLOAT_PAIRS)
+        try:
+            f = _native.perm_bench(U, S, T, _native.GLYNN, warmup=1, steps=2 if n >= 28 else 5)
+        finally:
+            _native.perm_arithmetic(prev)
+        fms = float(np.mean(f["sweep_ms"]))
+        fp = {"perms_per_s": 64 / (fms / 1e3), "ms_per_64": fms, **errors(n, U, S, T, f["results"])}
+        if f["ff_inst"] > 0 and peak32:  # float-pair sweep: its FP32 roofline
+            t32 = f["ff_inst"] / (fms / 1e3) / 1e12
+            fp.update({"achieved_t_fp32_inst": t32, "frac_of_fp32_peak": t32 / peak32})
+        res[str(n)]["float_pairs"] = fp
     return res
 
 
@@ -436,9 +458,11 @@ def strategies_section(seed):
     return out
 
 
-# arithmetic of the path: exact int64 fixed-point row sums, float-pair (two FP32,
-# ~47-bit) products and minors in the sweeps and the Laplace step, FP64 pmf and cdf
-DTYPE = "i64 fixed point + f32x2 float pairs (~47-bit); f64 cdf fallback"
+# arithmetic of the path (theboss computes in float64)
+DTYPE = "f64"
+DTYPE_NOTE = ("FP64 products, minors, Laplace step, |.|^2 and pmf; row sums in exact 64-bit fixed point; "
+              "cdf decisions by an exact integer scan of the FP64 pmf, theboss's sequential FP64 rule "
+              "inside the pmf's error window")
 
 
 def roofline(b, sweep_s, achieved, peak, peak32, traffic):
@@ -468,6 +492,27 @@ def roofline(b, sweep_s, achieved, peak, peak32, traffic):
             "peak_source": "boss_fp64_peak, measured in this run", **common}
 
 
+def float_pair_section(U, inp, w, args, fp64_samples):
+    """The opt-in float-pair arithmetic (boss_minors_arithmetic(0)): the same
+    workload and seed, device-timed; its stream against the FP64 one."""
+    from theboss_gb300 import _native
+
+    prev = _native.minors_arithmetic(_native.FLOAT_PAIRS)
+    try:
+        np.random.seed(args.seed)
+        _native.gccb_near_ties(reset=True)
+        b = _native.gccb_bench(U, inp, w, args.samples, args.warmup, args.steps)
+        ties = _native.gccb_near_ties(reset=True)
+    finally:
+        _native.minors_arithmetic(prev)
+    ms = float(np.mean(b["step_ms"]))
+    return {"value": args.samples / (ms / 1e3), "unit": "samples/s", "ms_per_step": ms,
+            "dtype": "i64 fixed point + f32x2 float pairs (~47-bit)",
+            "sweep_ms_per_step": float(np.mean(b["sweep_ms"])),
+            "samples_differing_from_fp64": int((b["samples"] != fp64_samples).any(axis=1).sum()),
+            "near_ties_per_step": ties / (args.warmup + args.steps)}
+
+
 def run_ours(args, rank, world):
     from theboss_gb300 import _native
     from theboss_gb300.simulation_strategies import GCCBPlainDriver
@@ -479,12 +524,14 @@ def run_ours(args, rank, world):
     peak32, _ = _native.fp32_peak()
     clocks = Clocks(int(os.environ.get("LOCAL_RANK", "0")))
     np.random.seed(args.seed + rank)
+    _native.gccb_near_ties(reset=True)
     _barrier(world)
     clocks.start()  # sampled over the device-timed steps and the e2e steps below
     t_wall = time.perf_counter()
     b = _native.gccb_bench(U, inp, w, args.samples, args.warmup, args.steps)
     t_wall = time.perf_counter() - t_wall
     _barrier(world)
+    ties = _native.gccb_near_ties(reset=True)
     total_ms = float(np.sum(b["step_ms"]))
     total_ms = _max_over_ranks(total_ms, world)
     value = world * args.samples * args.steps / (total_ms / 1e3)
@@ -511,10 +558,14 @@ def run_ours(args, rank, world):
            "h2d_bytes_per_step": b["h2d_bytes"], "d2h_bytes_per_step": b["d2h_bytes"]}
     line = {"metric": METRIC, "value": value, "unit": "samples/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": DTYPE, "data": "synthetic (seeded Haar unitary)",
+            "scaling": "weak", "vs_baseline": None,
+            "dtype": DTYPE if args.arith == "fp64" else "i64 fixed point + f32x2 float pairs (~47-bit)",
+            "dtype_note": DTYPE_NOTE if args.arith == "fp64" else "float pairs (opt-in arithmetic)",
+            "data": "synthetic (seeded Haar unitary)",
             "config": config(args), "clocks": clk, "e2e": e2e,
             "gpu_launches": b["kernels"] * args.steps,
             "roofline": roofline(b, sweep_s, achieved, peak, peak32, traffic),
+            "near_ties_per_step": ties / (args.warmup + args.steps),
             "wall_s_device_section": t_wall}
     if rank == 0 and not args.quick:
         # theboss's per-step loop with the GPU all-minors calculator, bounded sample
@@ -525,13 +576,18 @@ def run_ours(args, rank, world):
         plain = n_plain / (time.perf_counter() - t)
         line["plain_gpu"] = {"value": plain, "unit": "samples/s", "samples": n_plain}
         line["batched_vs_plain"] = {"device": value / world / plain, "e2e": e2e["value"] / plain}
+        if args.arith == "fp64":
+            line["float_pairs"] = float_pair_section(U, inp, w, args, b["samples"])
         line["single_permanents"] = single_permanents(peak, args.seed, peak32)
         line["adjoint"] = adjoint_section(args.seed)
         line["exact_distribution"] = distribution_section(peak, args.seed)
         line["strategies"] = strategies_section(args.seed)
     if rank == 0:
-        line["cpu_baseline"] = cpu_baseline(U, inp, w, args.seed)
+        line["cpu_baseline"], parity = cpu_baseline(U, inp, w, args.seed, gpu_samples=b["samples"])
+        line["parity"] = parity
         print(json.dumps(line), flush=True)
+        if parity["gpu_disagrees_with_double_double"]:
+            raise SystemExit("the device-timed samples differ from the oracle's beyond its near ties")
 
 
 def run_reference(args, rank):

@@ -171,22 +171,35 @@ BOSS_API int boss_gccb_sample(const double* matrix, int32_t m, const int32_t* in
 
 // Arithmetic of the all-minors sweeps (boss_submatrices_batch and the batched
 // sampler's levels, boss_gccb_sample*, boss_gccb_bench; theboss computes them in
-// numpy float64, bs_cc_ryser_submatrices_permanent_calculator.py:96-119).
-// mode 0 (default): products, running totals and minors as float pairs (two
-// FP32 values, about 47 significant bits) on the FP32 pipe, for sweeps of at
-// most 24 product-side particles; mode 1: FP64 sweeps (the sampler's Laplace
-// step and cdf scan stay float pairs, with the exact FP64 fallback); -1: query only.
-// *previous (if not null) receives the mode in force before the call.  Row sums
-// are exact 64-bit fixed point in both.
+// numpy float64, bs_cc_ryser_submatrices_permanent_calculator.py:96-119, and the
+// sampler's pmf in Python floats, generalized_cliffords_b_simulation_strategy.py:82-92).
+// mode 1 (default): FP64 sweeps, and the sampler's Laplace step, |.|^2 and pmf in
+// FP64; mode 0: products, running totals, minors and the sampler's pmf as float
+// pairs (two FP32 values, about 47 significant bits) on the FP32 pipe, for
+// sweeps of at most 24 product-side particles (larger ones stay FP64); -1: query
+// only.  *previous (if not null) receives the mode in force before the call.  Row
+// sums are exact 64-bit fixed point in both.
 BOSS_API int boss_minors_arithmetic(int32_t mode, int32_t* previous);
 
 // The same choice for the single-permanent sweeps of boss_perm_batch and
 // boss_perm_bench (theboss: numpy float64 in every calculator's
-// compute_permanent, bs_permanent_calculator_base.py:166-198): 0 float pairs
-// (default, up to 32 product-side particles, Glynn-kind sweeps: Glynn, Chin-Huh,
-// Classic), 1 FP64, -1 query.  Ryser-form sweeps, whose alternating sum cancels
+// compute_permanent, bs_permanent_calculator_base.py:166-198): 1 FP64 (default),
+// 0 float pairs (up to 32 product-side particles, Glynn-kind sweeps: Glynn,
+// Chin-Huh, Classic), -1 query.  Ryser-form sweeps, whose alternating sum cancels
 // far more, the allocation-free entry point and the gradients always use FP64.
 BOSS_API int boss_perm_arithmetic(int32_t mode, int32_t* previous);
+
+/*
+ * The sampler's cdf guard.  Every draw of boss_gccb_sample* is decided from the
+ * pmf the GPU computed; when a step of the cdf lies within the pmf's error bound
+ * of the uniform (a near tie, where the rounding of the minors could change the
+ * outcome), theboss's exact sequential rule on the pmf decides it (Python's sum,
+ * the division, numpy's cumsum and searchsorted:
+ * generalized_cliffords_b_simulation_strategy.py:91-92, 107-110).  *count receives
+ * the number of such draws since the last reset; reset != 0 zeroes the count.
+ * No reference counterpart.
+ */
+BOSS_API int boss_gccb_near_ties(int64_t* count, int32_t reset);
 
 /*
  * Benchmark form of boss_gccb_sample: the random stream is replayed and the

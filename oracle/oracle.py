@@ -238,6 +238,54 @@ def gccb_run(U, L, A, Uu) -> np.ndarray:
     return out
 
 
+def choice_from_minors(U, S, sub, u: float) -> int:
+    """One C&C-B draw from given minors: the Laplace expansion, |.|^2 and the
+    normalisation of generalized_cliffords_b_simulation_strategy.py:82-92 in
+    Python floats, then numpy.random.choice's rule (cumsum, divided by the last
+    entry, searchsorted 'right')."""
+    U = _mat(U)
+    m = U.shape[0]
+    pmf = []
+    for o in range(m):
+        p = 0j
+        for i in range(m):
+            p += S[i] * sub[i] * U[o][i]
+        pmf.append(abs(p) ** 2)
+    total = sum(pmf)
+    cdf = np.cumsum([v / total for v in pmf])
+    cdf /= cdf[-1]
+    return min(int(np.searchsorted(cdf, u, side="right")), m - 1)
+
+
+def classify_mismatches(U, L, A, Uu, got, ref, max_check: int = 4) -> dict:
+    """Compares GPU samples `got` with the oracle's `ref` for the same pre-drawn
+    stream (predraw_gccb's L, A, Uu).  theboss's Ryser-form minors carry rounding
+    errors (about 1e-10 relative at 20 particles), so a uniform that falls that
+    close to a cdf step can be decided by the rounding.  Each differing sample (up
+    to max_check) is re-sampled with minors from the double-double evaluator
+    (accurate to far below 1e-15): `oracle_near_ties` counts samples the GPU draws
+    as the accurate minors do; `gpu_disagrees_with_double_double` counts the rest
+    and every differing sample left unchecked."""
+    U = _mat(U)
+    m = U.shape[0]
+    got = np.asarray(got)
+    bad = np.nonzero((got != np.asarray(ref)).any(axis=1))[0]
+    rep = {"samples": int(len(got)), "mismatches": int(len(bad)), "oracle_near_ties": 0,
+           "gpu_disagrees_with_double_double": 0}
+    for s in bad[:max_check]:
+        S = np.zeros(m, dtype=np.int32)
+        T = np.zeros(m, dtype=np.int32)
+        for k in range(int(L[s])):
+            S[int(A[s, k])] += 1
+            T[choice_from_minors(U, S, submatrices_dd(U, list(S), list(T)), float(Uu[s, k]))] += 1
+        if np.array_equal(T, got[s]):
+            rep["oracle_near_ties"] += 1
+        else:
+            rep["gpu_disagrees_with_double_double"] += 1
+    rep["gpu_disagrees_with_double_double"] += max(0, len(bad) - max_check)
+    return rep
+
+
 def gccb_simulate(U, input_state, samples_number: int, transmissivity: Optional[float] = None) -> np.ndarray:
     """Reference-order GCC-B (uniform losses when ``transmissivity`` is given)."""
     n = int(sum(int(v) for v in input_state))

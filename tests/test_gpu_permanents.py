@@ -174,8 +174,8 @@ def test_submatrices_against_double_double(oracle, k, minors_arith):
 def test_large_permanents_against_double_double_fixture():
     """C2 patterns at n = 26, 28, 30 (single photons in 2n modes, ~20% doubly
     occupied outputs) against double-double values computed once by the oracle
-    (tests/golden/make_c2_dd.py): float pairs (the default) and FP64 both within
-    1e-10."""
+    (tests/golden/make_c2_dd.py), one permanent per call: FP64 (the default) and
+    float pairs both within 1e-10."""
     import json
     import os
 
@@ -200,3 +200,41 @@ def test_large_permanents_against_double_double_fixture():
             finally:
                 _native.perm_arithmetic(prev)
             assert abs(got - ref) <= 1e-10 * abs(ref), (n, r["pattern"], mode, abs(got - ref) / abs(ref))
+
+
+@pytest.mark.parametrize("n", [26, 28, 30])
+def test_benchmark_batches_against_double_double_fixture(n):
+    """The benchmark's own C2 batches (64 patterns per call, bench.c2_patterns with
+    the benchmark's seed): every pattern of the double-double fixture within 1e-10,
+    for Glynn in both arithmetics and for Chin-Huh (which sweeps the input side)
+    in both.  Sharing one launch among many permanents gives every thread a longer
+    code range, so this is the case that bounds a thread's accumulated rounding."""
+    import json
+    import os
+
+    import bench
+    from conftest import ROOT
+    from theboss_gb300 import _native
+    from theboss_gb300.utilities import haar_unitary
+
+    recs = [r for r in json.load(open(os.path.join(ROOT, "tests", "golden", "c2_dd_large.json"))) if r["n"] == n]
+    assert recs
+    seed = recs[0]["seed"]
+    U = haar_unitary(2 * n, seed)
+    assert abs(U[0, 0] - complex(*recs[0]["U00"])) <= 1e-12, "matrix generator changed"
+    T = bench.c2_patterns(n, 64, seed)
+    for r in recs:
+        assert T[r["pattern"]].tolist() == r["T"], "pattern generator changed"
+    S = np.zeros_like(T)
+    S[:, :n] = 1
+    for variant, count in ((_native.GLYNN, 64), (_native.CHIN_HUH, 64 if n < 30 else 16)):
+        for mode in (_native.FP64, _native.FLOAT_PAIRS):
+            prev = _native.perm_arithmetic(mode)
+            try:
+                got = _native.perm_batch(U, S[:count], T[:count], variant)
+            finally:
+                _native.perm_arithmetic(prev)
+            for r in recs:
+                ref = complex(r["dd"][0], r["dd"][1]) + complex(r["dd"][2], r["dd"][3])
+                err = abs(got[r["pattern"]] - ref) / abs(ref)
+                assert err <= 1e-10, (n, variant, mode, r["pattern"], err)

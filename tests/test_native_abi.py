@@ -50,7 +50,7 @@ def test_no_gpu_calls_fail_loudly_without_device():
 
 def test_arithmetic_switches_set_query_and_reject_bad_modes():
     """boss_minors_arithmetic / boss_perm_arithmetic only record the choice (no
-    GPU needed): float pairs by default, FP64 on request, -1 queries."""
+    GPU needed): FP64 by default, float pairs on request, -1 queries."""
     import pytest
     from theboss_gb300 import _native
 
@@ -67,4 +67,5 @@ def test_arithmetic_switches_set_query_and_reject_bad_modes():
             assert setter(-1) == _native.FLOAT_PAIRS
         finally:
             setter(start)
-    assert _native.minors_arithmetic(-1) == _native.FLOAT_PAIRS  # the library's default
+    assert _native.minors_arithmetic(-1) == _native.FP64  # the library's default
+    assert _native.perm_arithmetic(-1) == _native.FP64

@@ -101,6 +101,8 @@ def load() -> ctypes.CDLL:
         L.boss_perm_arithmetic.argtypes = [ctypes.c_int32, ip]
         L.boss_minors_arithmetic.restype = ctypes.c_int
         L.boss_minors_arithmetic.argtypes = [ctypes.c_int32, ip]
+        L.boss_gccb_near_ties.restype = ctypes.c_int
+        L.boss_gccb_near_ties.argtypes = [ctypes.POINTER(ctypes.c_int64), ctypes.c_int32]
         _lib = L
         return L
 
@@ -336,13 +338,13 @@ def fp64_peak():
     return float(t[0]), float(ms[0])
 
 
-FLOAT_PAIRS = 0  # all-minors sweeps: float pairs on the FP32 pipe (default)
-FP64 = 1
+FLOAT_PAIRS = 0  # float pairs on the FP32 pipe (opt-in)
+FP64 = 1         # FP64 (the default, theboss's float64)
 
 
 def minors_arithmetic(mode: int = -1) -> int:
-    """Sets the arithmetic of the all-minors sweeps (submatrices and the batched
-    sampler's levels: FLOAT_PAIRS or FP64; -1 only queries) and returns the
+    """Sets the arithmetic of the all-minors sweeps and of the batched sampler's
+    pmf (FP64, the default, or FLOAT_PAIRS; -1 only queries) and returns the
     previous one."""
     prev = np.zeros(1, dtype=np.int32)
     check(load().boss_minors_arithmetic(int(mode), _ip(prev)))
@@ -358,11 +360,20 @@ def fp32_peak():
 
 
 def perm_arithmetic(mode: int = -1) -> int:
-    """Sets the arithmetic of the single-permanent sweeps (FLOAT_PAIRS or FP64; -1
-    only queries) and returns the previous one."""
+    """Sets the arithmetic of the single-permanent sweeps (FP64, the default, or
+    FLOAT_PAIRS; -1 only queries) and returns the previous one."""
     prev = np.zeros(1, dtype=np.int32)
     check(load().boss_perm_arithmetic(int(mode), _ip(prev)))
     return int(prev[0])
+
+
+def gccb_near_ties(reset: bool = False) -> int:
+    """Draws of the batched sampler decided by the exact sequential rule because a
+    cdf step lay within the pmf's error bound of the uniform (boss_gccb_near_ties),
+    counted since the last reset."""
+    v = ctypes.c_int64(0)
+    check(load().boss_gccb_near_ties(ctypes.byref(v), int(bool(reset))))
+    return int(v.value)
 
 
 def select_device(device: int) -> None:

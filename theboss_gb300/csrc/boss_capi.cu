@@ -365,8 +365,9 @@ static int fill_sweep(HostSweep& hs, const Side& dig, const Side& col, int kind,
   return kOk;
 }
 
-int g_minors_arith = 0;
-int g_perm_arith = 0;
+// FP64 by default (theboss computes in float64); float pairs on request.
+int g_minors_arith = 1;
+int g_perm_arith = 1;
 
 void host_fx_to_ff(long long x, int fbias, float& hi, float& lo) {
   const unsigned long long sgn = (unsigned long long)(x >> 63);

@@ -226,7 +226,10 @@ struct FinalizeArgs {
   int n;       // row stride of idx / uni
   int fx;      // fixed-point fraction bits of the sweep rows
   const longlong2* Ufx;   // m x m, U * 2^fx rounded
-  const float4* Uff;      // m x m transposed, Uff[i * m + o] = U[o][i] as float pairs (re hi, re lo, im hi, im lo)
+  const float4* Uff;      // float-pair pmf: m x m transposed, Uff[i * m + o] = U[o][i] as float pairs
+                          // (re hi, re lo, im hi, im lo)
+  const double2* Ud;      // FP64 pmf: m x m transposed, Ud[i * m + o] = U[o][i]
+  const float* Uabs;      // m x m transposed, |Re U[o][i]| + |Im U[o][i]| (the pmf error bound)
   uint8_t* S;             // [sample][m] current input occupations
   uint8_t* T;             // [sample][m] output occupations
   const int32_t* order;   // [sample in level order] -> its row in the replayed (input-order) draws
@@ -248,10 +251,55 @@ struct FinalizeArgs {
   int next_group;               // uniform next level: threads per summed group of minors
   int cur_ff;                   // this level's sweep ran on float pairs: its partials are float4
   int next_ff;                  // the next level's sweep runs on float pairs (float-pair rows, biases)
-  int* err;
+  int* err;                     // err[0]: a pmf could not be normalised; err[1]: draws decided by the
+                                // exact sequential rule because a cdf step lay within the error window
 };
 
 constexpr int kFinWarps = 4;
+
+// Stated relative error bounds of the all-minors sweeps (absolute error of every
+// minor against the exact value, over the largest minor of the step), used by the
+// finalize kernel's cdf guard.  Measured against the double-double oracle at
+// k = 8..22 input particles: FP64 sweeps at most 8.1e-15, float-pair sweeps at
+// most 3.0e-12; the bounds hold 110x and 19x of margin.
+constexpr float kMinorsErrF64 = 9.094947e-13f;  // 2^-40
+constexpr float kMinorsErrFF = 5.820766e-11f;   // 2^-34
+
+__device__ __forceinline__ unsigned long long warp_max_u64(unsigned long long v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned long long y = __shfl_xor_sync(0xffffffffu, v, o);
+    v = y > v ? y : v;
+  }
+  return v;
+}
+
+__device__ __forceinline__ float warp_sum_f(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// x * 2^s in float for |s| <= 252 (two exact power-of-two factors; the product
+// over- or underflows like any float product).
+__device__ __forceinline__ float scale_pow2f(float x, int s) {
+  s = max(-252, min(s, 252));
+  const int h = s / 2, l = s - h;
+  return x * __int_as_float((h + 127) << 23) * __int_as_float((l + 127) << 23);
+}
+
+// x * 2^F rounded to the nearest integer (ties up), for a finite x >= 0 with
+// x * 2^F < 2^63; integer instructions only (the double's fields are shifted).
+__device__ __forceinline__ unsigned long long fixed_of_double(double x, int F) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const int e = (int)(b >> 52) & 0x7ff;
+  unsigned long long mant = b & 0xFFFFFFFFFFFFFull;
+  if (e) mant |= 1ull << 52;
+  const int sh = (e ? e : 1) - 1075 + F;  // x = mant * 2^((e ? e : 1) - 1075)
+  if (sh >= 0) return mant << sh;         // the caller keeps x * 2^F below 2^63
+  if (sh <= -64) return 0ull;
+  return (mant >> -sh) + ((mant >> (-sh - 1)) & 1ull);
+}
 
 // Removes and returns the r-th (0-based) particle still in the 256-bit set `rem`
 // (r is below the number of set bits: the host drew it with randint(0, remaining)).
@@ -279,6 +327,9 @@ __device__ __forceinline__ int pop_particle(uint32_t* rem, int r) {
   return q * 32 + pos;
 }
 
+// kF64: the minors, the Laplace step, |.|^2 and the pmf are FP64 (the default);
+// otherwise float pairs on the FP32 pipe (the opt-in float-pair arithmetic).
+template <bool kF64>
 __global__ void __launch_bounds__(kFinWarps * 32) gccb_finalize_kernel(FinalizeArgs a) {
   __shared__ double2 sub_s[kFinWarps][32];
   __shared__ float4 subf_s[kFinWarps][32];
@@ -286,6 +337,7 @@ __global__ void __launch_bounds__(kFinWarps * 32) gccb_finalize_kernel(FinalizeA
   __shared__ uint8_t mult_s[kFinWarps][32];
   __shared__ uint8_t fm_s[kFinWarps][32];
   __shared__ double pmf_s[kFinWarps][256];
+  __shared__ float cn_s[kFinWarps][32];  // |c_d|_1 2^-Ec (the pmf error bound)
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int j = blockIdx.x * kFinWarps + w;
   if (j >= a.A) return;
@@ -309,6 +361,7 @@ __global__ void __launch_bounds__(kFinWarps * 32) gccb_finalize_kernel(FinalizeA
       mode = a.pmode[row + pop_particle(rem, a.idx[row])];
       S[mode] = 1;
       subf_s[w][0] = make_float4(1.0f, 0.0f, 0.0f, 0.0f);
+      sub_s[w][0] = make_double2(1.0, 0.0);
       dm_s[w][0] = (uint8_t)mode;
       mult_s[w][0] = 1;
     }
@@ -383,144 +436,315 @@ __global__ void __launch_bounds__(kFinWarps * 32) gccb_finalize_kernel(FinalizeA
       mult_s[w][lane] = P.mult[lane];
     }
   }
-  if (a.k > 1 && a.cur_ff && lane < nd) {  // a scale beyond the float range: apply it in FP64
-    const SweepProblem& P = a.probs_cur[j];
-    const int sc_exp = (int)((__double_as_longlong(P.scale) >> 52) & 0x7FF) - 1023;
-    if (!(sc_exp >= -126 && sc_exp <= 127)) {
-      const float4 u = subf_s[w][lane];
+  __syncwarp();
+  const size_t drow = (size_t)a.order[j] * a.n;  // this sample's replayed draws
+  const double uu = a.uni[drow + (a.k - 1)];
+  const int K = (m + 31) >> 5;  // contiguous outputs per lane in the cdf scan
+  const int o0 = lane * K;
+  const int full = m & ~31;
+  int idx = 0;
+  bool near = false;  // some cdf step lies within the error window of u * total
+  // theboss: Laplace expansion perm(T + e_o) = sum_i S_i sub_i U[o][i], |.|^2,
+  // normalisation by Python's sequential sum
+  // (generalized_cliffords_b_simulation_strategy.py:82-92), then numpy.random.choice:
+  // cdf = cumsum(p), cdf /= cdf[-1], searchsorted(cdf, u, 'right') (:107-110).  The
+  // Glynn-form sweep already delivers S_i sub_i.  Lane o reads column o of the
+  // transposed matrix (coalesced); the outputs that do not fill a warp split their
+  // digits over several lanes.
+  //
+  // Fast path: the decision from a scan of the unnormalised pmf compared with
+  // u * total (no division).  The cdf guard: with c_d the minors, a_o =
+  // sum_d |c_d| |U[o][d]| and b_o = sum_d |U[o][d]| (1-norms of the complex
+  // entries, upper bounds), each minor is within eps_m * max_d |c_d| of its exact
+  // value (kMinorsErrF64 / kMinorsErrFF), so |p_o - exact| <= e_o = eps_m max|c| b_o
+  // + gamma a_o and |pmf_o - exact| <= e_o (2 a_o + e_o) (|p_o| <= a_o).  Their sum E
+  // plus the scan's and theboss's own rounding of the sums bounds how far every
+  // cdf step can lie from the exact one.  When a step lies within that window of
+  // u * total the draw is decided by theboss's exact sequential rule on the pmf
+  // and counted in err[1]; outside it the fast path's decision is the exact one.
+  if constexpr (kF64) {
+    // ---- FP64 pmf (the default arithmetic) ----
+    const double2* UT = a.Ud + (size_t)j * a.mstride;
+    const float* UA = a.Uabs + (size_t)j * a.mstride;
+    double* pmf = pmf_s[w];
+    // the bound's scale: 2^-Ec, 2^Ec <= max_d |c_d|_1 < 2^(Ec + 1)
+    double c1 = 0.0;
+    if (lane < nd) {
+      const double2 c = sub_s[w][lane];
+      c1 = fabs(c.x) + fabs(c.y);
+    }
+    const unsigned long long cb = warp_max_u64((unsigned long long)__double_as_longlong(c1));
+    const int Ec = (int)(cb >> 52) - 1023;  // non-negative doubles order as integers
+    const double sc = (cb >> 52) ? __longlong_as_double((long long)(1023 - Ec) << 52) : 1.0;  // 2^-Ec
+    if (lane < nd) cn_s[w][lane] = __double2float_ru(c1 * sc);  // in [0, 2)
+    __syncwarp();
+    const float eps2 = 2.0f * kMinorsErrF64;                          // eps_m * max|c| (scaled max < 2)
+    const float gam = (float)(nd + 2) * 2.220446e-16f;                // (nd + 2) 2^-52: the FMAs' rounding
+    float errsum = 0.0f;                                              // this lane's share of E * 2^-2Ec
+    for (int o = lane; o < full; o += 32) {
+      double pr = 0.0, pi = 0.0;
+      float ao = 0.0f, bo = 0.0f;
+#pragma unroll 4  // independent gathers in flight
+      for (int d = 0; d < nd; ++d) {
+        const double2 c = sub_s[w][d];
+        const int e = dm_s[w][d] * m + o;
+        const double2 u = UT[e];
+        const float ua = UA[e];
+        pr = fma(c.x, u.x, pr);
+        pr = fma(-c.y, u.y, pr);
+        pi = fma(c.x, u.y, pi);
+        pi = fma(c.y, u.x, pi);
+        ao = fmaf(cn_s[w][d], ua, ao);
+        bo += ua;
+      }
+      pmf[o] = fma(pr, pr, pi * pi);
+      const float eo = eps2 * bo + gam * ao;
+      errsum += eo * (2.0f * ao + eo);
+    }
+    if (m > full) {
+      const int r = m - full;
+      int s = 1;  // lanes per remaining output (a power of two, r * s <= 32)
+      while (r * (s << 1) <= 32) s <<= 1;
+      const int oi = lane / s, c0 = lane & (s - 1);
+      double pr = 0.0, pi = 0.0;
+      float ao = 0.0f, bo = 0.0f;
+      if (oi < r) {
+#pragma unroll 4
+        for (int d = c0; d < nd; d += s) {
+          const double2 c = sub_s[w][d];
+          const int e = dm_s[w][d] * m + full + oi;
+          const double2 u = UT[e];
+          const float ua = UA[e];
+          pr = fma(c.x, u.x, pr);
+          pr = fma(-c.y, u.y, pr);
+          pi = fma(c.x, u.y, pi);
+          pi = fma(c.y, u.x, pi);
+          ao = fmaf(cn_s[w][d], ua, ao);
+          bo += ua;
+        }
+      }
+      for (int off = s >> 1; off > 0; off >>= 1) {  // fixed butterfly order over the output's lanes
+        pr += __shfl_xor_sync(0xffffffffu, pr, off);
+        pi += __shfl_xor_sync(0xffffffffu, pi, off);
+        ao += __shfl_xor_sync(0xffffffffu, ao, off);
+        bo += __shfl_xor_sync(0xffffffffu, bo, off);
+      }
+      if (oi < r && c0 == 0) {
+        pmf[full + oi] = fma(pr, pr, pi * pi);
+        const float eo = eps2 * bo + (gam + 5.0f * 2.220446e-16f) * ao;  // + the butterfly's adds
+        errsum += eo * (2.0f * ao + eo);
+      }
+    }
+    const float E = warp_sum_f(errsum) * 1.01f;  // 1.01: the float sums' own rounding (< 2^-18)
+    __syncwarp();
+    // The cdf scan in exact 64-bit fixed point: F fraction bits with every entry
+    // below 2^54 and the total below 2^62 (m <= 256); each entry is off by at most
+    // half a unit (2^-54 of the largest entry).
+    unsigned long long pb = 0;
+    for (int o = lane; o < m; o += 32) {
+      const unsigned long long b = (unsigned long long)__double_as_longlong(pmf[o]);
+      pb = b > pb ? b : pb;
+    }
+    pb = warp_max_u64(pb);
+    if (pb == 0ull || (pb >> 52) >= 0x7ffull) {  // zero total, or an infinite / NaN entry
+      if (lane == 0) atomicOr(a.err, 1);
+    } else {
+      const int F = 53 - ((int)(pb >> 52) - 1023);
+      unsigned long long run = 0;
+      for (int q = 0; q < K; ++q)
+        if (o0 + q < m) run += fixed_of_double(pmf[o0 + q], F);
+#pragma unroll
+      for (int off = 1; off < 32; off <<= 1) {
+        const unsigned long long y = __shfl_up_sync(0xffffffffu, run, off);
+        if (lane >= off) run += y;
+      }
+      const unsigned long long tot = __shfl_sync(0xffffffffu, run, 31);
+      unsigned long long C = __shfl_up_sync(0xffffffffu, run, 1);
+      if (lane == 0) C = 0;
+      // numpy's random_sample is N / 2^53 with an integer N < 2^53, so for an
+      // integer C: C <= u * tot  <=>  C <= floor(N * tot / 2^53), exactly.
+      const unsigned long long Nu = fixed_of_double(uu, 53);
+      const unsigned long long ut = (__umul64hi(Nu, tot) << 11) | ((Nu * tot) >> 53);
+      // the window in fixed-point units: E 2^(2 Ec + F), plus the scan's and
+      // theboss's roundings ((m + 4) 2^-52 of the total, over-counted 4x) and the
+      // entries' half units
+      const float wf = scale_pow2f(E, 2 * Ec + F);
+      unsigned long long W = (wf < 4.0e18f) ? (unsigned long long)wf + 1ull : (1ull << 62);
+      W += ((tot >> 50) + 1ull) * (unsigned long long)(m + 4) + (unsigned long long)m;
+      int cnt = 0;
+      for (int q = 0; q < K; ++q) {
+        const int o = o0 + q;
+        if (o >= m) break;
+        C += fixed_of_double(pmf[o], F);  // the cdf step after output o, times total
+        const unsigned long long dlt = C > ut ? C - ut : ut - C;
+        near |= (o < m - 1) && dlt <= W;
+        cnt += (C <= ut) ? 1 : 0;
+      }
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) cnt += __shfl_xor_sync(0xffffffffu, cnt, off);
+      idx = cnt < m ? cnt : m - 1;
+    }
+  } else {
+    // ---- float pairs on the FP32 pipe (opt-in) ----
+    if (a.k > 1 && a.cur_ff && lane < nd) {  // a scale beyond the float range: apply it in FP64
+      const SweepProblem& P = a.probs_cur[j];
+      const int sc_exp = (int)((__double_as_longlong(P.scale) >> 52) & 0x7FF) - 1023;
+      if (!(sc_exp >= -126 && sc_exp <= 127)) {
+        const float4 u = subf_s[w][lane];
+        float4 f;
+        double_to_ff(ff_to_double(u.x, u.y) * P.scale, f.x, f.y);
+        double_to_ff(ff_to_double(u.z, u.w) * P.scale, f.z, f.w);
+        subf_s[w][lane] = f;
+      }
+    }
+    if (a.k > 1 && !a.cur_ff && lane < nd) {  // FP64 minors to float pairs
+      const double2 v = sub_s[w][lane];
       float4 f;
-      double_to_ff(ff_to_double(u.x, u.y) * P.scale, f.x, f.y);
-      double_to_ff(ff_to_double(u.z, u.w) * P.scale, f.z, f.w);
+      double_to_ff(v.x, f.x, f.y);
+      double_to_ff(v.y, f.z, f.w);
       subf_s[w][lane] = f;
     }
-  }
-  if (a.k > 1 && !a.cur_ff && lane < nd) {  // FP64 minors to float pairs
-    const double2 v = sub_s[w][lane];
-    float4 f;
-    double_to_ff(v.x, f.x, f.y);
-    double_to_ff(v.y, f.z, f.w);
-    subf_s[w][lane] = f;
-  }
-  __syncwarp();
-  // Laplace expansion perm(T + e_o) = sum_i S_i sub_i U[o][i]
-  // (generalized_cliffords_b_simulation_strategy.py:82-89), then |.|^2.  The
-  // Glynn-form sweep already delivers S_i sub_i.  The dot products run on the
-  // FP32 pipe as compensated float-pair sums (lane o reads column o of the
-  // transposed float-pair matrix: coalesced), |.|^2 as a float pair (stored in
-  // the warp's pmf row, float2 per output).  The outputs that do not fill a warp
-  // split their digits over several lanes.
-  const float4* UT = a.Uff + (size_t)j * a.mstride;
-  float2* pf = reinterpret_cast<float2*>(pmf_s[w]);
-  const int full = m & ~31;
-  for (int o = lane; o < full; o += 32) {
-    float sr = 0.0f, cr = 0.0f, si = 0.0f, ci = 0.0f;
-    #pragma unroll 4  // independent gathers in flight
-    for (int d = 0; d < nd; ++d) {
-      const float4 c = subf_s[w][d];
-      const float4 u = UT[(size_t)dm_s[w][d] * m + o];
-      ff_dot_acc(sr, cr, 1.0f, c.x, c.y, u.x, u.y);
-      ff_dot_acc(sr, cr, -1.0f, c.z, c.w, u.z, u.w);
-      ff_dot_acc(si, ci, 1.0f, c.x, c.y, u.z, u.w);
-      ff_dot_acc(si, ci, 1.0f, c.z, c.w, u.x, u.y);
+    __syncwarp();
+    // the bound's scale: 2^-Ec, 2^Ec <= max_d |c_d|_1 < 2^(Ec + 1)
+    float c1 = 0.0f;
+    if (lane < nd) {
+      const float4 c = subf_s[w][lane];
+      c1 = fabsf(c.x) + fabsf(c.z);
     }
-    pf[o] = ff_abs2(sr, cr, si, ci);
-  }
-  if (m > full) {
-    const int r = m - full;
-    int s = 1;  // lanes per remaining output (a power of two, r * s <= 32)
-    while (r * (s << 1) <= 32) s <<= 1;
-    const int oi = lane / s, c0 = lane & (s - 1);
-    float sr = 0.0f, cr = 0.0f, si = 0.0f, ci = 0.0f;
-    if (oi < r) {
-      #pragma unroll 4  // independent gathers in flight
-      for (int d = c0; d < nd; d += s) {
+    unsigned cbits = __float_as_uint(c1);
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) cbits = max(cbits, __shfl_xor_sync(0xffffffffu, cbits, off));
+    const int Ec = (int)(cbits >> 23) - 127;
+    if (lane < nd) cn_s[w][lane] = scale_pow2f(c1, -Ec) * 1.0000002f;  // in [0, 2); the lo parts
+    __syncwarp();
+    const float eps2 = 2.0f * kMinorsErrFF;
+    const float gam = 9.094947e-13f;  // 2^-40: the compensated dot products
+    float errsum = 0.0f;
+    // The dot products run as compensated float-pair sums, |.|^2 as a float pair
+    // (stored in the warp's pmf row, float2 per output).
+    const float4* UT = a.Uff + (size_t)j * a.mstride;
+    const float* UA = a.Uabs + (size_t)j * a.mstride;
+    float2* pf = reinterpret_cast<float2*>(pmf_s[w]);
+    for (int o = lane; o < full; o += 32) {
+      float sr = 0.0f, cr = 0.0f, si = 0.0f, ci = 0.0f, ao = 0.0f, bo = 0.0f;
+#pragma unroll 4  // independent gathers in flight
+      for (int d = 0; d < nd; ++d) {
         const float4 c = subf_s[w][d];
-        const float4 u = UT[(size_t)dm_s[w][d] * m + full + oi];
+        const int e = dm_s[w][d] * m + o;
+        const float4 u = UT[e];
+        const float ua = UA[e];
         ff_dot_acc(sr, cr, 1.0f, c.x, c.y, u.x, u.y);
         ff_dot_acc(sr, cr, -1.0f, c.z, c.w, u.z, u.w);
         ff_dot_acc(si, ci, 1.0f, c.x, c.y, u.z, u.w);
         ff_dot_acc(si, ci, 1.0f, c.z, c.w, u.x, u.y);
+        ao = fmaf(cn_s[w][d], ua, ao);
+        bo += ua;
       }
+      pf[o] = ff_abs2(sr, cr, si, ci);
+      const float eo = eps2 * bo + gam * ao;
+      errsum += eo * (2.0f * ao + eo);
     }
-    for (int off = s >> 1; off > 0; off >>= 1) {  // fixed butterfly order over the output's lanes
-      const float osr = __shfl_xor_sync(0xffffffffu, sr, off), ocr = __shfl_xor_sync(0xffffffffu, cr, off);
-      const float osi = __shfl_xor_sync(0xffffffffu, si, off), oci = __shfl_xor_sync(0xffffffffu, ci, off);
-      ff_acc(sr, cr, 1.0f, osr, ocr);
-      ff_acc(si, ci, 1.0f, osi, oci);
-    }
-    if (oi < r && c0 == 0) pf[full + oi] = ff_abs2(sr, cr, si, ci);
-  }
-  __syncwarp();
-  // theboss normalises with Python's sequential sum, and numpy.random.choice then
-  // takes cdf = cumsum(p), cdf /= cdf[-1], searchsorted(cdf, u, 'right')
-  // (generalized_cliffords_b_simulation_strategy.py:91-92, 107-110).  Fast path:
-  // the same decisions from a float-pair warp scan of the unnormalised pmf
-  // compared with u * total (no division), accurate to ~1e-14, far inside the
-  // 1e-12 window; whenever some cdf entry lies within 1e-12 (relative) of
-  // u * total the sequential FP64 evaluation decides.
-  const size_t drow = (size_t)a.order[j] * a.n;  // this sample's replayed draws
-  const double uu = a.uni[drow + (a.k - 1)];
-  const int K = (m + 31) >> 5;  // contiguous outputs per lane
-  const int o0 = lane * K;
-  float ih = 0.0f, il = 0.0f;
-  for (int q = 0; q < K; ++q)
-    if (o0 + q < m) ff_acc(ih, il, 1.0f, pf[o0 + q].x, pf[o0 + q].y);
-#pragma unroll
-  for (int off = 1; off < 32; off <<= 1) {
-    const float yh = __shfl_up_sync(0xffffffffu, ih, off), yl = __shfl_up_sync(0xffffffffu, il, off);
-    if (lane >= off) ff_acc(ih, il, 1.0f, yh, yl);
-  }
-  const float th = __shfl_sync(0xffffffffu, ih, 31), tl = __shfl_sync(0xffffffffu, il, 31);
-  float ch = __shfl_up_sync(0xffffffffu, ih, 1), cl = __shfl_up_sync(0xffffffffu, il, 1);
-  if (lane == 0) ch = cl = 0.0f;
-  int idx = 0;
-  if (!(th > 0.0f && th <= 3.4e38f)) {  // not a positive finite total
-    if (lane == 0) atomicOr(a.err, 1);
-  } else {
-    float uth, utl;
-    double_to_ff(uu, uth, utl);
-    ff_mul(uth, utl, th, tl);  // u * total
-    const float window = 1e-12f * uth;
-    int cnt = 0;
-    bool near = false;
-    for (int q = 0; q < K; ++q) {
-      if (o0 + q >= m) break;
-      ff_acc(ch, cl, 1.0f, pf[o0 + q].x, pf[o0 + q].y);  // ~ cdf * total
-      float dh = ch, dl = cl;
-      ff_acc(dh, dl, -1.0f, uth, utl);  // normalised: its sign is dh's
-      near |= (o0 + q < m - 1) && fabsf(dh) <= window;
-      cnt += (dh <= 0.0f) ? 1 : 0;
-    }
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) cnt += __shfl_xor_sync(0xffffffffu, cnt, off);
-    idx = cnt < m ? cnt : m - 1;
-    if (__any_sync(0xffffffffu, near)) {  // exact sequential evaluation in FP64
-      for (int o = lane; o < m; o += 32) {  // the pmf as doubles, in place (same 8-byte slots)
-        const float2 v = pf[o];
-        pmf_s[w][o] = ff_to_double(v.x, v.y);
-      }
-      __syncwarp();
-      double total = 0.0;
-      if (lane == 0)
-        for (int o = 0; o < m; ++o) total += pmf_s[w][o];
-      total = __shfl_sync(0xffffffffu, total, 0);
-      for (int o = lane; o < m; o += 32) pmf_s[w][o] = pmf_s[w][o] / total;
-      __syncwarp();
-      if (lane == 0) {
-        double acc = 0.0;
-        for (int o = 0; o < m; ++o) {
-          acc += pmf_s[w][o];
-          pmf_s[w][o] = acc;
+    if (m > full) {
+      const int r = m - full;
+      int s = 1;  // lanes per remaining output (a power of two, r * s <= 32)
+      while (r * (s << 1) <= 32) s <<= 1;
+      const int oi = lane / s, c0 = lane & (s - 1);
+      float sr = 0.0f, cr = 0.0f, si = 0.0f, ci = 0.0f, ao = 0.0f, bo = 0.0f;
+      if (oi < r) {
+#pragma unroll 4  // independent gathers in flight
+        for (int d = c0; d < nd; d += s) {
+          const float4 c = subf_s[w][d];
+          const int e = dm_s[w][d] * m + full + oi;
+          const float4 u = UT[e];
+          const float ua = UA[e];
+          ff_dot_acc(sr, cr, 1.0f, c.x, c.y, u.x, u.y);
+          ff_dot_acc(sr, cr, -1.0f, c.z, c.w, u.z, u.w);
+          ff_dot_acc(si, ci, 1.0f, c.x, c.y, u.z, u.w);
+          ff_dot_acc(si, ci, 1.0f, c.z, c.w, u.x, u.y);
+          ao = fmaf(cn_s[w][d], ua, ao);
+          bo += ua;
         }
       }
-      __syncwarp();
-      const double last = pmf_s[w][m - 1];
-      int cnt2 = 0;
-      for (int o = lane; o < m; o += 32) cnt2 += (pmf_s[w][o] / last <= uu) ? 1 : 0;
-#pragma unroll
-      for (int off = 16; off > 0; off >>= 1) cnt2 += __shfl_xor_sync(0xffffffffu, cnt2, off);
-      idx = cnt2 < m ? cnt2 : m - 1;
+      for (int off = s >> 1; off > 0; off >>= 1) {  // fixed butterfly order over the output's lanes
+        const float osr = __shfl_xor_sync(0xffffffffu, sr, off), ocr = __shfl_xor_sync(0xffffffffu, cr, off);
+        const float osi = __shfl_xor_sync(0xffffffffu, si, off), oci = __shfl_xor_sync(0xffffffffu, ci, off);
+        ff_acc(sr, cr, 1.0f, osr, ocr);
+        ff_acc(si, ci, 1.0f, osi, oci);
+        ao += __shfl_xor_sync(0xffffffffu, ao, off);
+        bo += __shfl_xor_sync(0xffffffffu, bo, off);
+      }
+      if (oi < r && c0 == 0) {
+        pf[full + oi] = ff_abs2(sr, cr, si, ci);
+        const float eo = eps2 * bo + gam * ao;
+        errsum += eo * (2.0f * ao + eo);
+      }
     }
+    const float E = warp_sum_f(errsum) * 1.01f;
+    __syncwarp();
+    float ih = 0.0f, il = 0.0f;
+    for (int q = 0; q < K; ++q)
+      if (o0 + q < m) ff_acc(ih, il, 1.0f, pf[o0 + q].x, pf[o0 + q].y);
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+      const float yh = __shfl_up_sync(0xffffffffu, ih, off), yl = __shfl_up_sync(0xffffffffu, il, off);
+      if (lane >= off) ff_acc(ih, il, 1.0f, yh, yl);
+    }
+    const float th = __shfl_sync(0xffffffffu, ih, 31), tl = __shfl_sync(0xffffffffu, il, 31);
+    float ch = __shfl_up_sync(0xffffffffu, ih, 1), cl = __shfl_up_sync(0xffffffffu, il, 1);
+    if (lane == 0) ch = cl = 0.0f;
+    if (!(th > 0.0f && th <= 3.4e38f)) {  // not a positive finite total
+      if (lane == 0) atomicOr(a.err, 1);
+    } else {
+      float uth, utl;
+      double_to_ff(uu, uth, utl);
+      ff_mul(uth, utl, th, tl);  // u * total
+      // the window, scaled by 2^-2Ec: E plus the float-pair scan's error (m + 4) 2^-44 of the total
+      const float win = E + (float)(m + 4) * 5.684342e-14f * scale_pow2f(th, -2 * Ec);
+      int cnt = 0;
+      for (int q = 0; q < K; ++q) {
+        if (o0 + q >= m) break;
+        ff_acc(ch, cl, 1.0f, pf[o0 + q].x, pf[o0 + q].y);  // ~ cdf * total
+        float dh = ch, dl = cl;
+        ff_acc(dh, dl, -1.0f, uth, utl);  // normalised: its sign is dh's
+        near |= (o0 + q < m - 1) && scale_pow2f(fabsf(dh), -2 * Ec) <= win;
+        cnt += (dh <= 0.0f) ? 1 : 0;
+      }
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) cnt += __shfl_xor_sync(0xffffffffu, cnt, off);
+      idx = cnt < m ? cnt : m - 1;
+      if (__any_sync(0xffffffffu, near)) {
+        for (int o = lane; o < m; o += 32) {  // the pmf as doubles, in place (same 8-byte slots)
+          const float2 v = pf[o];
+          pmf_s[w][o] = ff_to_double(v.x, v.y);
+        }
+      }
+    }
+  }
+  if (__any_sync(0xffffffffu, near)) {
+    // theboss's exact sequential evaluation in FP64 on the pmf: Python's sum, the
+    // division, numpy's cumsum, the division by the last entry, searchsorted
+    __syncwarp();
+    double total = 0.0;
+    if (lane == 0)
+      for (int o = 0; o < m; ++o) total += pmf_s[w][o];
+    total = __shfl_sync(0xffffffffu, total, 0);
+    for (int o = lane; o < m; o += 32) pmf_s[w][o] = pmf_s[w][o] / total;
+    __syncwarp();
+    if (lane == 0) {
+      double acc = 0.0;
+      for (int o = 0; o < m; ++o) {
+        acc += pmf_s[w][o];
+        pmf_s[w][o] = acc;
+      }
+      atomicAdd(a.err + 1, 1);
+    }
+    __syncwarp();
+    const double last = pmf_s[w][m - 1];
+    int cnt2 = 0;
+    for (int o = lane; o < m; o += 32) cnt2 += (pmf_s[w][o] / last <= uu) ? 1 : 0;
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) cnt2 += __shfl_xor_sync(0xffffffffu, cnt2, off);
+    idx = cnt2 < m ? cnt2 : m - 1;
   }
   if (lane == 0) T[idx] = (uint8_t)(T[idx] + 1);
   __syncwarp();
@@ -691,8 +915,12 @@ struct GccbRun {
   double sweep_flops = 0.0;  // flops of all sweep launches (the Glynn form's codes)
   double ref_flops = 0.0;    // the same count over theboss's Ryser-form codes
   double ff_inst = 0.0;      // FP32 instructions of the float-pair sweeps (model count per code)
+  bool f64 = true;           // FP64 sweeps and pmf (false: float pairs)
   std::vector<cudaEvent_t> ev;  // 2 per sweep level when timing
 };
+// Draws decided by the exact sequential rule (a cdf step within the error window
+// of the uniform), summed over the sampler's calls until read (boss_gccb_near_ties).
+static int64_t g_gccb_near_ties = 0;
 // Two independent slots (device buffers cx->gccb[8 slot .. 8 slot + 7], a pinned
 // staging buffer and a graph each): the host can plan one batch while the GPU
 // runs the other.
@@ -719,18 +947,26 @@ static void destroy_events(GccbRun& R) {
   R.ev.clear();
 }
 
-// out[mat][i][o] = U[mat][o][i] as float pairs (the Laplace step's coalesced layout).
-__global__ void to_ff_transposed_kernel(const double2* __restrict__ U, float4* __restrict__ out, int m, int64_t count) {
+// The Laplace step's coalesced layouts, out[mat][i][o] from U[mat][o][i]: as
+// doubles (FP64 pmf) or float pairs, and |Re| + |Im| in float (the pmf error bound).
+__global__ void transpose_matrices_kernel(const double2* __restrict__ U, void* __restrict__ out,
+                                          float* __restrict__ uabs, int m, int64_t count, int f64) {
   const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (idx >= count) return;
   const int64_t mm = (int64_t)m * m;
   const int64_t mat = idx / mm, r = idx - mat * mm;
   const int o = (int)(r / m), i = (int)(r - (int64_t)o * m);
   const double2 v = U[idx];
-  float4 f;
-  double_to_ff(v.x, f.x, f.y);
-  double_to_ff(v.y, f.z, f.w);
-  out[mat * mm + (int64_t)i * m + o] = f;
+  const int64_t t = mat * mm + (int64_t)i * m + o;
+  if (f64) {
+    reinterpret_cast<double2*>(out)[t] = v;
+  } else {
+    float4 f;
+    double_to_ff(v.x, f.x, f.y);
+    double_to_ff(v.y, f.z, f.w);
+    reinterpret_cast<float4*>(out)[t] = f;
+  }
+  uabs[t] = __double2float_ru(fabs(v.x) + fabs(v.y));  // rounded up: an upper bound
 }
 
 __global__ void to_fixed_kernel(const double* __restrict__ x, long long* __restrict__ y, int64_t count, int fx) {
@@ -789,7 +1025,11 @@ static int gccb_prepare(Context* cx, const double* matrix, int n_mats, int m, Dr
   std::vector<std::vector<uint64_t>> lvl_codes(Lmax + 2);
   std::vector<std::vector<int>> lvl_nd(Lmax + 2);
   std::vector<char> ffl(Lmax + 2, 0);  // level k's sweep runs on float pairs
-  for (int k = 2; k <= Lmax; ++k) ffl[k] = (g_minors_arith == 0 && minors_ff_available(k - 1)) ? 1 : 0;
+  // FP64 (the default): FP64 sweeps and an FP64 pmf; float pairs where the
+  // float-pair sweep exists for the level's factor count, and a float-pair pmf
+  const bool f64 = (g_minors_arith != 0);
+  R.f64 = f64;
+  for (int k = 2; k <= Lmax; ++k) ffl[k] = (!f64 && minors_ff_available(k - 1)) ? 1 : 0;
   // FP32 instructions per code of a float-pair sweep with nf = k - 1 factors
   auto ff_per_code = [&](int k) { return ffl[k] ? 47.5625 * (k - 1) : 0.0; };
   R.sweep_flops = 0.0;
@@ -907,7 +1147,7 @@ static int gccb_prepare(Context* cx, const double* matrix, int n_mats, int m, Dr
   // Arena (one H2D copy): err | level tables | randint results | particle modes | uniforms | U | U fixed-point
   auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
   size_t off = 0;
-  const size_t o_err = off; off = al(off + sizeof(int));
+  const size_t o_err = off; off = al(off + 2 * sizeof(int));
   std::vector<size_t> o_tab(Lmax + 2, 0);
   for (int k = 2; k <= Lmax; ++k) { o_tab[k] = off; off = al(off + sizeof(LevelSample) * tab[k].size()); }
   const size_t o_ord = off; off = al(off + sizeof(int32_t) * (size_t)N);
@@ -918,7 +1158,7 @@ static int gccb_prepare(Context* cx, const double* matrix, int n_mats, int m, Dr
   const size_t o_U = off; off = al(off + sizeof(double2) * (size_t)m * m * n_mats);
   const size_t arena = off;
   R.h2d_bytes = arena;
-  R.d2h_bytes = (size_t)N * m + sizeof(int);
+  R.d2h_bytes = (size_t)N * m + 2 * sizeof(int);
   int st;
   if ((st = ensure(B[0], arena))) return st;
   if ((st = ensure(B[1], (size_t)N * m * 2))) return st;                              // S | T
@@ -927,7 +1167,8 @@ static int gccb_prepare(Context* cx, const double* matrix, int n_mats, int m, Dr
   if ((st = ensure(B[4], sizeof(longlong2) * (size_t)max_pool * 2 + 512))) return st;  // rows x2
   if ((st = ensure(B[5], sizeof(double2) * (size_t)max_parts))) return st;            // partials
   if ((st = ensure(B[6], sizeof(uint32_t) * 8 * (size_t)N))) return st;                // particles left
-  if ((st = ensure(B[7], 32 * (size_t)m * m * n_mats))) return st;  // U fixed point | U^T float pairs
+  // U fixed point | U^T (doubles or float pairs) | U^T 1-norms
+  if ((st = ensure(B[7], 36 * (size_t)m * m * n_mats + 256))) return st;
   if ((st = ensure_slot_pinned(slot, std::max(arena, al((size_t)N * m) + 256)))) return st;
   char* h = (char*)g_gccb_pinned[slot];
   memset(h, 0, o_ord);
@@ -958,14 +1199,16 @@ static int gccb_prepare(Context* cx, const double* matrix, int n_mats, int m, Dr
   cudaError_t e = cudaMemcpyAsync(d, h, arena, cudaMemcpyHostToDevice, s);
   if (e != cudaSuccess) return fail_cuda(e, "H2D sampler arena");
   longlong2* dUfx = (longlong2*)B[7].ptr;
-  float4* dUff = (float4*)(dUfx + mm * n_mats);
+  void* dUt = (void*)(dUfx + mm * n_mats);  // 16 bytes per entry either way
+  float* dUabs = (float*)((char*)dUt + 16 * mm * n_mats);
   {
     const int64_t cnt = (int64_t)2 * mm * n_mats;
     to_fixed_kernel<<<(unsigned)((cnt + 255) / 256), 256, 0, s>>>((const double*)(d + o_U), (long long*)dUfx, cnt, fx);
     if ((e = cudaGetLastError()) != cudaSuccess) return fail_cuda(e, "fixed-point matrices");
     const int64_t cnt2 = (int64_t)mm * n_mats;
-    to_ff_transposed_kernel<<<(unsigned)((cnt2 + 255) / 256), 256, 0, s>>>((const double2*)(d + o_U), dUff, m, cnt2);
-    if ((e = cudaGetLastError()) != cudaSuccess) return fail_cuda(e, "float-pair matrices");
+    transpose_matrices_kernel<<<(unsigned)((cnt2 + 255) / 256), 256, 0, s>>>((const double2*)(d + o_U), dUt, dUabs,
+                                                                              m, cnt2, f64 ? 1 : 0);
+    if ((e = cudaGetLastError()) != cudaSuccess) return fail_cuda(e, "transposed matrices");
   }
   destroy_events(R);
   if (timing) {
@@ -1008,7 +1251,9 @@ static int gccb_prepare(Context* cx, const double* matrix, int n_mats, int m, Dr
     fa.n = n;
     fa.fx = fx;
     fa.Ufx = dUfx;
-    fa.Uff = dUff;
+    fa.Uff = f64 ? nullptr : (const float4*)dUt;
+    fa.Ud = f64 ? (const double2*)dUt : nullptr;
+    fa.Uabs = dUabs;
     fa.mstride = (n_mats > 1) ? (int64_t)mm : 0;
     fa.npart = (const uint8_t*)(d + o_np);
     fa.order = (const int32_t*)(d + o_ord);
@@ -1030,7 +1275,10 @@ static int gccb_prepare(Context* cx, const double* matrix, int n_mats, int m, Dr
     fa.next_ff = (k < Lmax) ? ffl[k + 1] : 0;
     fa.cur_ff = (k >= 2) ? ffl[k] : 0;
     fa.err = R.derr;
-    gccb_finalize_kernel<<<(A[k] + kFinWarps - 1) / kFinWarps, kFinWarps * 32, 0, s>>>(fa);
+    if (f64)
+      gccb_finalize_kernel<true><<<(A[k] + kFinWarps - 1) / kFinWarps, kFinWarps * 32, 0, s>>>(fa);
+    else
+      gccb_finalize_kernel<false><<<(A[k] + kFinWarps - 1) / kFinWarps, kFinWarps * 32, 0, s>>>(fa);
     le = cudaGetLastError();
     ++R.kernels;
   }
@@ -1076,14 +1324,16 @@ static int gccb_queue_results(Context* cx, GccbRun& R) {
   cudaError_t e = cudaMemcpyAsync(h, R.dT, (size_t)R.N * R.m, cudaMemcpyDeviceToHost, s);
   if (e != cudaSuccess) return fail_cuda(e, "D2H samples");
   int* herr = (int*)(h + (((size_t)R.N * R.m + 255) & ~(size_t)255));
-  e = cudaMemcpyAsync(herr, R.derr, sizeof(int), cudaMemcpyDeviceToHost, s);
+  e = cudaMemcpyAsync(herr, R.derr, 2 * sizeof(int), cudaMemcpyDeviceToHost, s);
   return e == cudaSuccess ? kOk : fail_cuda(e, "D2H status");
 }
 
 // After the stream is synchronised: the status, then the samples in input order.
 static int gccb_read_results(const GccbRun& R, int32_t* samples_out) {
   const char* h = (const char*)g_gccb_pinned[R.slot];
-  if (*(const int*)(h + (((size_t)R.N * R.m + 255) & ~(size_t)255))) {
+  const int* herr = (const int*)(h + (((size_t)R.N * R.m + 255) & ~(size_t)255));
+  g_gccb_near_ties += herr[1];
+  if (herr[0]) {
     set_error("probabilities contain NaN (a pmf summed to zero or a non-finite value)");
     return kErrPmf;
   }
@@ -1242,6 +1492,17 @@ int boss_gccb_sample_slice(const double* matrix, int32_t m, const int32_t* input
   }
   memcpy(mt_key, mt.key, sizeof(mt.key));
   *mt_pos = mt.pos;
+  return kOk;
+}
+
+int boss_gccb_near_ties(int64_t* count, int32_t reset) {
+  if (!count) {
+    set_error("null pointer");
+    return kErrArg;
+  }
+  std::lock_guard<std::mutex> lk(g_api_mutex);
+  *count = g_gccb_near_ties;
+  if (reset) g_gccb_near_ties = 0;
   return kOk;
 }
 

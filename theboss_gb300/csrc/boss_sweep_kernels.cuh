@@ -468,9 +468,15 @@ __global__ void __launch_bounds__(128, kFFMinBlocks<NF>) minors_sweep_ff_kernel(
 // resynchronised every kFFPermResync codes, lazily renormalised sums).  The products
 // stay renormalised: a single permanent of 26-30 particles cancels more than the
 // sampler's minors, and this keeps it 2-5x closer to double-double (n = 28:
-// ~1e-11) at no measurable cost.
+// ~1e-11) at no measurable cost.  The float-pair running sum is folded into an
+// FP64 accumulator every kFFPermFold codes: a lazily summed float pair loses
+// about 2^-48 of its magnitude per addition, so left to run over a thread's whole
+// range its error grows with the codes per thread -- with 64 permanents sharing
+// one launch (each thread walking ~64x more codes than a lone permanent) n = 30
+// measured 5.9e-10 against double-double.
 // Each thread writes its partial as a float pair (float4) in the factors' scales.
 constexpr int kFFPermMaxFactors = 32;
+constexpr uint64_t kFFPermFold = 64;
 template <int NF>
 constexpr int kFFPermMinBlocks = NF <= 12 ? 4 : (NF <= 20 ? 3 : 2);
 
@@ -485,7 +491,7 @@ __global__ void __launch_bounds__(128, kFFPermMinBlocks<NF>) perm_sweep_ff_kerne
   const int64_t q = gt - P.thread_begin;
   int64_t a, len;
   thread_range(P, q, a, len);
-  float trh = 0.0f, trl = 0.0f, tih = 0.0f, til = 0.0f;  // weighted total of the finished segments
+  double tr = 0.0, ti = 0.0;  // weighted total of the finished segments
   if (len > 0) {
     const longlong2* D = pool + P.mat_off;
     const longlong2* base = pool + P.base_off;
@@ -499,7 +505,8 @@ __global__ void __launch_bounds__(128, kFFPermMinBlocks<NF>) perm_sweep_ff_kerne
     double w;
     decode_code_ff<NF>(P, D, base, fb, (uint64_t)a, SS, S, g, parity, w);
     uint64_t g_int = g;
-    ffc A = {0.0f, 0.0f, 0.0f, 0.0f};  // this segment's signed sum of products
+    ffc A = {0.0f, 0.0f, 0.0f, 0.0f};  // signed sum of products since the last fold
+    double sr = 0.0, si = 0.0;         // this segment's folded sum
     const uint64_t end = (uint64_t)(a + len);
     for (uint64_t t = (uint64_t)a;;) {
       {
@@ -520,6 +527,11 @@ __global__ void __launch_bounds__(128, kFFPermMinBlocks<NF>) perm_sweep_ff_kerne
         if (((tn - (uint64_t)a) & (kFFPermResync - 1)) == 0) {
           resync_ff<NF>(D, fb, g, g_int, SS, S);
           g_int = g;
+          if (((tn - (uint64_t)a) & (kFFPermFold - 1)) == 0) {
+            sr += ff_to_double(A.rh, A.rl);
+            si += ff_to_double(A.ih, A.il);
+            A = {0.0f, 0.0f, 0.0f, 0.0f};
+          }
         } else {
           const float sg = bit ? -1.0f : 1.0f;
           const float4* row = DF + (size_t)i * NF;
@@ -532,24 +544,26 @@ __global__ void __launch_bounds__(128, kFFPermMinBlocks<NF>) perm_sweep_ff_kerne
           }
         }
       } else {  // a multi-valued digit moves: settle the segment with its weight, re-decode
-        const float wh = __double2float_rn(w), wl = __double2float_rn(w - (double)wh);
-        ff_mul(A.rh, A.rl, wh, wl);
-        ff_mul(A.ih, A.il, wh, wl);
-        ff_acc(trh, trl, 1.0f, A.rh, A.rl);
-        ff_acc(tih, til, 1.0f, A.ih, A.il);
+        sr += ff_to_double(A.rh, A.rl);
+        si += ff_to_double(A.ih, A.il);
+        tr = fma(w, sr, tr);
+        ti = fma(w, si, ti);
         A = {0.0f, 0.0f, 0.0f, 0.0f};
+        sr = si = 0.0;
         decode_code_ff<NF>(P, D, base, fb, tn, SS, S, g, parity, w);
         g_int = g;
       }
       t = tn;
     }
-    const float wh = __double2float_rn(w), wl = __double2float_rn(w - (double)wh);
-    ff_mul(A.rh, A.rl, wh, wl);
-    ff_mul(A.ih, A.il, wh, wl);
-    ff_acc(trh, trl, 1.0f, A.rh, A.rl);
-    ff_acc(tih, til, 1.0f, A.ih, A.il);
+    sr += ff_to_double(A.rh, A.rl);
+    si += ff_to_double(A.ih, A.il);
+    tr = fma(w, sr, tr);
+    ti = fma(w, si, ti);
   }
-  reinterpret_cast<float4*>(partials)[P.part_off + q] = make_float4(trh, trl, tih, til);
+  float4 o;
+  double_to_ff(tr, o.x, o.y);
+  double_to_ff(ti, o.z, o.w);
+  reinterpret_cast<float4*>(partials)[P.part_off + q] = o;
 }
 
 // Gradient sweep (Glynn / Chin-Huh kind).  With s_f the factor sums and
