@@ -56,9 +56,11 @@ def parse():
     ap.add_argument("--samples", type=int, default=10000)
     ap.add_argument("--seed", type=int, default=2026)
     ap.add_argument("--quick", action="store_true", help="skip the single-permanent and plain-driver sections")
-    ap.add_argument("--case", choices=["perm", "grad", "dist"],
-                    help="run one small kernel case instead of the bench (for profiler captures): "
-                         "Glynn permanents or permanents with all n^2 derivatives, n photons in 2n modes")
+    ap.add_argument("--no-tune", action="store_true", help="time the heuristic launch shapes (no autotuner)")
+    ap.add_argument("--case", choices=["perm", "grad", "dist", "c5"],
+                    help="run one kernel case instead of the bench (for profiler captures): Glynn permanents or "
+                         "permanents with all n^2 derivatives, n photons in 2n modes; c5: the full lossy-network "
+                         "run (n=30 in 60 modes, 120 expanded, 2000 samples)")
     ap.add_argument("--n", type=int, default=24, help="photons of --case")
     ap.add_argument("--patterns", type=int, default=16, help="output patterns of --case")
     ap.add_argument("--arith", choices=["ff", "fp64"], default="fp64",
@@ -82,6 +84,9 @@ def run_case(args):
     from theboss_gb300.utilities import haar_unitary
 
     set_arithmetic(args)
+    if args.case == "c5":
+        print(json.dumps(lossy_network_run(args.seed, 2000)), flush=True)
+        return
     m = 2 * args.n
     U = haar_unitary(m, args.seed + args.n)
     T = c2_patterns(args.n, args.patterns, args.seed + args.n)
@@ -398,10 +403,38 @@ def distribution_section(peak_tflops, seed):
                            "sample": f"{len(pick)} random outcomes of the same workload, {cpu_s:.1f} s"}}
 
 
+def lossy_network_run(seed, samples):
+    """C5: lossy-network C&C-B, n = 30 photons in m = 60 modes with per-mode
+    transmissivities t ~ U[0.3, 0.9] (M = U diag(sqrt(t))), expanded to 120 modes
+    (theboss's prepare_interferometer_matrix_in_expanded_space), through the
+    drop-in strategy.  Every sample runs 30 levels of all-minors sweeps in the
+    expanded space: sum_k 2^(k-1) (9k - 12) flops per sample."""
+    from theboss_gb300.permanent_calculators import RyserPermanentCalculator
+    from theboss_gb300.simulation_strategies import LossyNetworksGeneralizedCliffordsSimulationStrategy
+    from theboss_gb300.utilities import haar_unitary
+
+    m, n = 60, 30
+    V = haar_unitary(m, seed + 60)
+    tr = np.random.default_rng(seed).uniform(0.3, 0.9, m)
+    strat = LossyNetworksGeneralizedCliffordsSimulationStrategy(RyserPermanentCalculator(V @ np.diag(np.sqrt(tr))))
+    np.random.seed(seed)
+    strat.simulate([1] * n + [0] * (m - n), 4)  # warm-up
+    np.random.seed(seed)
+    t = time.perf_counter()
+    smp = strat.simulate([1] * n + [0] * (m - n), samples)
+    dt = time.perf_counter() - t
+    flops = samples * sum(2.0 ** (k - 1) * (9 * k - 12) for k in range(2, n + 1))
+    return {"workload": f"lossy network n={n} in m={m} (120 expanded), t~U[0.3,0.9], {samples} samples",
+            "samples_per_s": samples / dt, "s": dt, "samples": samples,
+            "mean_particles_detected": float(np.mean([sum(x) for x in smp])),
+            "achieved_tflops_e2e": flops / dt / 1e12}
+
+
 def strategies_section(seed):
     """The other samplers of the path, each timed through its drop-in class:
     C1 plain generalized C&C (n=8, m=16, 1000 samples), C5 lossy-network C&C-B
-    (n=30 in m=60, 120 expanded modes, 16 samples), uniform-loss BOBS (n=20, m=40,
+    (n=30 in m=60, 120 expanded modes, 64 of the configuration's 2000 samples;
+    --case c5 runs all 2000), uniform-loss BOBS (n=20, m=40,
     eta=0.5, hierarchy level 10, 2000 samples) and the GPU outcome counter
     (10^6 samples over the 12,376 outcomes of n=6, m=12)."""
     from theboss_gb300 import _native
@@ -422,17 +455,7 @@ def strategies_section(seed):
     dt = time.perf_counter() - t
     out["c1_plain_gcc_n8_m16"] = {"samples_per_s": 1000 / dt, "s": dt, "samples": 1000}
 
-    m = 60
-    V = haar_unitary(m, seed + 60)
-    tr = np.random.default_rng(seed).uniform(0.3, 0.9, m)
-    calc = RyserPermanentCalculator(V @ np.diag(np.sqrt(tr)))
-    strat = LossyNetworksGeneralizedCliffordsSimulationStrategy(calc)
-    np.random.seed(seed)
-    t = time.perf_counter()
-    smp = strat.simulate([1] * 30 + [0] * 30, 16)
-    dt = time.perf_counter() - t
-    out["c5_lossy_network_n30_m60"] = {"samples_per_s": 16 / dt, "s": dt, "samples": 16,
-                                       "mean_particles_detected": float(np.mean([sum(s) for s in smp]))}
+    out["c5_lossy_network_n30_m60"] = lossy_network_run(seed, 64)
 
     U40 = haar_unitary(40, seed + 40)
     inp = [1] * 20 + [0] * 20
@@ -524,6 +547,9 @@ def run_ours(args, rank, world):
     peak32, _ = _native.fp32_peak()
     clocks = Clocks(int(os.environ.get("LOCAL_RANK", "0")))
     np.random.seed(args.seed + rank)
+    # the autotuner picks each level's split and group size on this workload (numpy's state is not advanced)
+    tune = _native.gccb_autotune(U, inp, w, args.samples, reps=3) if not args.no_tune else None
+    np.random.seed(args.seed + rank)
     _native.gccb_near_ties(reset=True)
     _barrier(world)
     clocks.start()  # sampled over the device-timed steps and the e2e steps below
@@ -566,6 +592,7 @@ def run_ours(args, rank, world):
             "gpu_launches": b["kernels"] * args.steps,
             "roofline": roofline(b, sweep_s, achieved, peak, peak32, traffic),
             "near_ties_per_step": ties / (args.warmup + args.steps),
+            "autotune": tune,
             "wall_s_device_section": t_wall}
     if rank == 0 and not args.quick:
         # theboss's per-step loop with the GPU all-minors calculator, bounded sample

@@ -202,6 +202,28 @@ BOSS_API int boss_perm_arithmetic(int32_t mode, int32_t* previous);
 BOSS_API int boss_gccb_near_ties(int64_t* count, int32_t reset);
 
 /*
+ * The sampler's autotuner.  On the workload of a boss_gccb_sample call (the same
+ * arguments; the MT19937 state is read, not advanced) it times, per level of
+ * the sampler, power-of-two shifts of the split (threads per sample) and caps of
+ * the size of the thread groups that sum their minors inside the sweep, keeps
+ * the fastest shape of every level when the whole step gets faster, then times
+ * the size of the pipelined first part on end-to-end calls (calls of at least
+ * 4096 samples).  The winners apply to later calls whose levels have the same
+ * arithmetic, particle count and power-of-two sample count; they are kept for
+ * the process and in a cache file keyed by the GPU's name ($BOSS_TUNE_CACHE, else
+ * ~/.cache/theboss_gb300/gccb_tune.txt), which later processes load.  With the
+ * environment variable BOSS_AUTOTUNE=1, boss_gccb_sample* tune an untuned
+ * workload on its first call.  reps: timed runs per candidate (after one warm-up).
+ * report (8 doubles): step ms with the heuristic shapes, step ms with the tuned
+ * shapes, levels whose shape changed, the pipeline shift (first part = count >>
+ * shift), end-to-end ms with the quarter split and with the tuned split (0 below
+ * 4096 samples).  No reference counterpart.
+ */
+BOSS_API int boss_gccb_autotune(const double* matrix, int32_t m, const int32_t* input_state,
+                                const double* particle_weights, int32_t n_weights, const uint32_t* mt_key,
+                                const int32_t* mt_pos, int32_t n_samples, int32_t reps, double* report);
+
+/*
  * Benchmark form of boss_gccb_sample: the random stream is replayed and the
  * inputs uploaded once, then the captured sampler graph runs n_warmup + n_steps
  * times with inputs resident in GPU memory.  Before every run a flush_bytes
@@ -238,9 +260,15 @@ BOSS_API int boss_gccb_bench(const double* matrix, int32_t m, const int32_t* inp
  *     by the caller; work is queued on `stream` (a cudaStream_t, 0 for the
  *     default stream) and the call returns without waiting for it: synchronise
  *     the stream before reading the results.
- *   - The first call on each device does a one-time set-up on the current
- *     device (looks up the scratch array's device address and sets kernel
- *     attributes).
+ *   - The request is planned whole before anything is queued: a rejected
+ *     request leaves the caller's buffer untouched.
+ *   - The first call on each device does a one-time set-up with that device
+ *     current: it looks up the scratch array's device address, sets kernel
+ *     attributes and creates one event; the first call in the process also
+ *     page-locks the library's 8 MiB host staging array (cudaHostRegister, no
+ *     device memory).  Make that first call before any stream capture.
+ *   - The host staging array is refilled only after its previous copy has left
+ *     it (an event wait), so calls may be queued back to back on one stream.
  *   - Every call shares the scratch array, which keeps the last call's contents;
  *     nothing in it has to start at zero.  Calls on the same stream are ordered;
  *     calls whose work overlaps on the GPU (different streams or threads) race on

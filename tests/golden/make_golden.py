@@ -1,8 +1,9 @@
 """Generates the golden fixtures in tests/golden/ by running theboss itself.
 
-Run in a container where the reference package is importable:
+Run where the reference package is importable, giving the path of a theboss
+checkout (the directory that holds the ``theboss`` package):
 
-    python tests/golden/make_golden.py /root/reference
+    python tests/golden/make_golden.py <theboss checkout> [--only <section>]
 
 theboss's Glynn-Gray calculator imports ``guancodes`` (an un-vendored third-party
 dependency pinned ``~=0.0.3`` in the reference's requirements.txt).  It is not
@@ -249,7 +250,46 @@ def main(ref_root):
     mode_assignment_samples(ref_root)
     tvd_values(ref_root)
     bobs_samples(ref_root)
+    gcc_uniform_losses_samples(ref_root)
     print("fixtures written to", out_dir)
+
+
+def gcc_uniform_losses_samples(ref_root: str) -> None:
+    """Seeded streams of theboss's A-version uniform-loss GCC
+    (generalized_cliffords_uniform_losses_simulation_strategy.py:125-138): every
+    photon survives when Python's random.random() < transmissivity, then numpy's
+    random() picks its output.  Both generators are seeded; the value each one
+    draws next is recorded, so the state theboss leaves behind is checked too."""
+    import random
+
+    sys.path.insert(0, ref_root)
+    sys.dont_write_bytecode = True
+    _install_gray_shim()
+    from scipy.stats import unitary_group
+
+    from theboss.boson_sampling_utilities.permanent_calculators.ryser_permanent_calculator import (
+        RyserPermanentCalculator,
+    )
+    from theboss.simulation_strategies.generalized_cliffords_uniform_losses_simulation_strategy import (
+        GeneralizedCliffordsUniformLossesSimulationStrategy,
+    )
+
+    out_dir = os.path.dirname(os.path.abspath(__file__))
+    recs = []
+    for seed, py_seed, m, inp, eta, N in [(71, 171, 6, [1, 1, 1, 0, 0, 0], 0.6, 30),
+                                          (72, 172, 8, [1, 1, 1, 1, 0, 0, 0, 0], 0.5, 25),
+                                          (73, 173, 5, [2, 1, 0, 1, 0], 0.7, 25)]:
+        U = unitary_group.rvs(m, random_state=seed)
+        np.random.seed(seed)
+        random.seed(py_seed)
+        strat = GeneralizedCliffordsUniformLossesSimulationStrategy(RyserPermanentCalculator(U), eta)
+        samples = strat.simulate(inp, N)
+        recs.append({"kind": "gcc_uniform", "seed": seed, "py_seed": py_seed, "U": _m(U), "input": inp, "eta": eta,
+                     "N": N, "samples": [[int(x) for x in s] for s in samples],
+                     "dtypes": sorted({str(np.asarray(s).dtype) for s in samples}),
+                     "next_random": float(np.random.random()), "next_py_random": random.random()})
+    with open(os.path.join(out_dir, "gcc_uniform_losses_samples.json"), "w") as f:
+        json.dump(recs, f)
 
 
 def bobs_samples(ref_root: str) -> None:
@@ -418,10 +458,12 @@ def lossy_distributions(ref_root: str) -> None:
 
 
 if __name__ == "__main__":
-    # python make_golden.py <theboss checkout> [--only lossy|mode_assignment]
+    # python make_golden.py <theboss checkout> [--only lossy|mode_assignment|tvd|bobs|gcc_uniform]
     sections = {"lossy": lossy_distributions, "mode_assignment": mode_assignment_samples, "tvd": tvd_values,
-                "bobs": bobs_samples}
+                "bobs": bobs_samples, "gcc_uniform": gcc_uniform_losses_samples}
+    if len(sys.argv) < 2:
+        sys.exit("usage: make_golden.py <theboss checkout> [--only " + "|".join(sections) + "]")
     if len(sys.argv) > 3 and sys.argv[2] == "--only":
         sections[sys.argv[3]](sys.argv[1])
     else:
-        main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+        main(sys.argv[1])

@@ -125,3 +125,59 @@ def test_permanents_function_gradient_is_conjugate_derivative():
 
     _, grads = _native.perm_grad_batch(U0, S.astype(np.int32), T.astype(np.int32))
     assert np.allclose(U.grad.numpy(), np.conj(grads[0]), atol=1e-13)
+
+
+def test_clements_log_likelihood_gradient_at_benchmark_size(oracle):
+    """The adjoint benchmark's own configuration: 256 seeded output patterns of
+    n = 12 photons (doubles allowed) in m = 24 modes, a Clements mesh of 276
+    (theta, phi) phases drawn uniformly.  The autograd gradient of the
+    log-likelihood equals central finite differences (h = 1e-6) for a sample of
+    the phases, within the differences' own rounding noise: each FP64 permanent
+    perm_k is off its exact value by a relative e_k (measured here against the
+    double-double oracle), so each log-probability by 2 e_k, and the difference
+    quotient by up to sum_k 2 (2 e_k) / (2h); the bound takes twice that.  (The
+    workload holds probabilities down to ~1e-27, permanents of ~1e-13 built from
+    terms of order 2^-11, whose e_k approach 1e-10: theboss's float64 carries
+    the same noise.)  d perm / dU of some patterns equals the oracle's minors of
+    the mesh's unitary (theboss's all-minors algorithm)."""
+    torch = pytest.importorskip("torch")
+    from theboss_gb300 import _native
+    from theboss_gb300.adjoint import clements_unitary, log_likelihood
+
+    m, n, count = 24, 12, 256
+    g = torch.Generator().manual_seed(2026)
+    theta = (torch.rand(276, generator=g, dtype=torch.float64) * 2 * np.pi).requires_grad_(True)
+    phi = (torch.rand(276, generator=g, dtype=torch.float64) * 2 * np.pi).requires_grad_(True)
+    S = np.zeros((count, m), dtype=np.int32)
+    S[:, :n] = 1
+    T = _patterns(m, n, count, 2026)
+    U = np.ascontiguousarray(clements_unitary(theta.detach(), phi.detach()).numpy())
+    perms = _native.perm_batch(U, S, T, _native.GLYNN)
+    e = 0.0
+    for k in range(count):
+        hi, lo = oracle.perm_dd(U, list(S[k]), list(T[k]))
+        e += abs(perms[k] - (hi + lo)) / abs(hi + lo)
+    h = 1e-6
+    noise = 2 * (4 * e) / (2 * h)
+
+    def loss(th, ph):
+        return log_likelihood(clements_unitary(th, ph), S, T)
+
+    loss(theta, phi).backward()
+    picks = np.random.default_rng(7).choice(276, size=8, replace=False)
+    for which, param, grad in (("theta", theta, theta.grad), ("phi", phi, phi.grad)):
+        for idx in picks:
+            with torch.no_grad():
+                p = param.detach().clone()
+                p[idx] += h
+                lp = loss(p, phi.detach()) if which == "theta" else loss(theta.detach(), p)
+                p[idx] -= 2 * h
+                lm = loss(p, phi.detach()) if which == "theta" else loss(theta.detach(), p)
+            fd = (lp - lm).item() / (2 * h)
+            assert abs(fd - grad[idx].item()) <= 1e-6 * max(1.0, abs(fd)) + noise, \
+                (which, idx, fd, grad[idx].item(), noise)
+    _, grads = _native.perm_grad_batch(U, S[:4], T[:4])
+    for k in range(4):
+        ref = _minor_grad(oracle, U, S[k], T[k])
+        scale = np.abs(ref).max()
+        assert np.abs(grads[k] - ref).max() <= 1e-11 * scale

@@ -51,6 +51,27 @@ def test_gccb_fixtures_match_reference_streams():
         assert np.random.random() == rec["next_random"], rec["kind"]
 
 
+def test_uniform_loss_a_version_matches_reference_streams():
+    """generalized_cliffords_uniform_losses_simulation_strategy.py:125-138 (the
+    factory's UNIFORM_LOSSES_GCC): Python's stdlib random() decides every photon's
+    survival, numpy's random() its output.  Streams recorded from theboss with
+    both generators seeded; the samples (int64 arrays), and the next value of each
+    generator, must be theboss's."""
+    import random
+
+    from theboss_gb300 import simulation_strategies as ss
+
+    for rec in load_golden("gcc_uniform_losses_samples.json"):
+        np.random.seed(rec["seed"])
+        random.seed(rec["py_seed"])
+        strat = ss.GeneralizedCliffordsUniformLossesSimulationStrategy(_calc(as_matrix(rec["U"])), rec["eta"])
+        out = strat.simulate(rec["input"], rec["N"])
+        assert all(isinstance(x, np.ndarray) and x.dtype == np.int64 for x in out)
+        assert [x.tolist() for x in out] == rec["samples"]
+        assert np.random.random() == rec["next_random"]
+        assert random.random() == rec["next_py_random"]
+
+
 def test_stream_slices_reassemble_one_call():
     """Ranks that each sample a slice of the same stream (boss_gccb_sample_slice)
     together give exactly one process's samples and numpy state."""
@@ -217,3 +238,61 @@ def test_lossy_network_sampling_in_expanded_120_modes(oracle):
     got = _native.gccb_sample(np.ascontiguousarray(E), np.array(inp, dtype=np.int32), None, N)
     assert (got == ref).all()
     assert (got[:, :m].sum(axis=1) <= n).all()
+
+
+def test_lossy_network_n20_in_120_modes_matches_oracle(oracle):
+    """The lossy-network configuration (60 modes, per-mode transmissivities t ~
+    U[0.3, 0.9], expanded to 120 modes) at 20 photons, the largest the CPU oracle
+    samples in seconds: every step up to 20 input particles.  Samples equal the
+    oracle's (theboss's algorithm restated), up to draws within theboss's own
+    pmf error of a cdf step, which the double-double minors decide."""
+    from theboss_gb300 import _native
+    from theboss_gb300.utilities import haar_unitary, prepare_interferometer_matrix_in_expanded_space
+
+    m, n, N = 60, 20, 48
+    U = haar_unitary(m, 600)
+    t = np.random.default_rng(601).uniform(0.3, 0.9, m)
+    E = np.ascontiguousarray(prepare_interferometer_matrix_in_expanded_space(U @ np.diag(np.sqrt(t))))
+    inp = [1] * n + [0] * (2 * m - n)
+    np.random.seed(602)
+    L, A, Uu = oracle.predraw_gccb(inp, N, None)
+    ref = oracle.gccb_run(E, L, A, Uu)
+    ref_next = np.random.random()
+    np.random.seed(602)
+    got = _native.gccb_sample(E, np.array(inp, dtype=np.int32), None, N)
+    assert np.random.random() == ref_next
+    rep = oracle.classify_mismatches(E, L, A, Uu, got, ref)
+    assert rep["gpu_disagrees_with_double_double"] == 0 and rep["mismatches"] <= 1, rep
+    assert (got.sum(axis=1) == n).all()
+
+
+def test_autotuner_reports_keeps_results_and_writes_its_cache(oracle, tmp_path, monkeypatch):
+    """boss_gccb_autotune on a 12-photon, 24-mode uniform-loss workload of 5000
+    samples (large enough for the pipelined split): it reports the heuristic and
+    tuned step times, writes its cache file keyed by the GPU's name, leaves
+    numpy's generator alone, and the tuned sampler still draws the oracle's
+    samples."""
+    from theboss_gb300 import _native
+    from theboss_gb300.utilities import haar_unitary
+
+    cache = tmp_path / "tune.txt"
+    monkeypatch.setenv("BOSS_TUNE_CACHE", str(cache))
+    U = haar_unitary(24, 2424)
+    inp = [1] * 12 + [0] * 12
+    w = oracle.binomial_weights(12, 0.5)
+    np.random.seed(12)
+    state = np.random.get_state()
+    rep = _native.gccb_autotune(U, np.array(inp, dtype=np.int32), w, 5000, reps=2)
+    after = np.random.get_state()
+    assert state[2] == after[2] and np.array_equal(state[1], after[1])
+    assert 0 < rep["tuned_step_ms"] <= rep["default_step_ms"]
+    assert 1 <= rep["pipeline_shift"] <= 4 and rep["e2e_tuned_split_ms"] > 0
+    lines = cache.read_text().splitlines()
+    assert any("|pipeline|" in l for l in lines) and len(lines) >= 2
+    np.random.seed(12)
+    L, A, Uu = oracle.predraw_gccb(inp, 5000, w)
+    ref = oracle.gccb_run(U, L, A, Uu)
+    np.random.seed(12)
+    got = _native.gccb_sample(U, np.array(inp, dtype=np.int32), w, 5000)
+    rep2 = oracle.classify_mismatches(U, L, A, Uu, got, ref)
+    assert rep2["gpu_disagrees_with_double_double"] == 0 and rep2["mismatches"] <= 1, rep2

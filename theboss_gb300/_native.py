@@ -101,6 +101,9 @@ def load() -> ctypes.CDLL:
         L.boss_perm_arithmetic.argtypes = [ctypes.c_int32, ip]
         L.boss_minors_arithmetic.restype = ctypes.c_int
         L.boss_minors_arithmetic.argtypes = [ctypes.c_int32, ip]
+        L.boss_gccb_autotune.restype = ctypes.c_int
+        L.boss_gccb_autotune.argtypes = [dp, ctypes.c_int32, ip, dp, ctypes.c_int32, up, ip, ctypes.c_int32,
+                                         ctypes.c_int32, dp]
         L.boss_gccb_near_ties.restype = ctypes.c_int
         L.boss_gccb_near_ties.argtypes = [ctypes.POINTER(ctypes.c_int64), ctypes.c_int32]
         _lib = L
@@ -365,6 +368,23 @@ def perm_arithmetic(mode: int = -1) -> int:
     prev = np.zeros(1, dtype=np.int32)
     check(load().boss_perm_arithmetic(int(mode), _ip(prev)))
     return int(prev[0])
+
+
+def gccb_autotune(U: np.ndarray, input_state, weights, n_samples: int, reps: int = 3) -> dict:
+    """Tunes the sampler's launch shapes on the workload of gccb_sample(U,
+    input_state, weights, n_samples) drawn from numpy's current global state
+    (which is not advanced); boss_gccb_autotune."""
+    L = load()
+    inp = np.ascontiguousarray(input_state, dtype=np.int32)
+    m = U.shape[0]
+    w, nw, wp = _weights_arg(weights)
+    _, key, pos = _get_mt()
+    rep = np.zeros(8)
+    check(L.boss_gccb_autotune(_dp(U.view(np.float64)), m, _ip(inp), wp, nw,
+                               key.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32)), _ip(pos), n_samples, reps,
+                               _dp(rep)))
+    return {"default_step_ms": float(rep[0]), "tuned_step_ms": float(rep[1]), "levels_changed": int(rep[2]),
+            "pipeline_shift": int(rep[3]), "e2e_quarter_split_ms": float(rep[4]), "e2e_tuned_split_ms": float(rep[5])}
 
 
 def gccb_near_ties(reset: bool = False) -> int:

@@ -929,18 +929,25 @@ namespace boss {
 
 constexpr size_t kNoAllocScratchBytes = (size_t)8 << 20;  // 8 MiB, held by every GPU that loads the library
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
-alignas(256) static unsigned char g_noalloc_staging[kNoAllocScratchBytes];  // host-side copy source
+// Host-side copy source, page-locked once (cudaHostRegister: no device memory) so
+// that its copies are truly asynchronous; an event recorded after each copy is
+// waited on before the array is refilled.
+alignas(4096) static unsigned char g_noalloc_staging[kNoAllocScratchBytes];
+static bool g_noalloc_staging_pinned = false;
+static cudaEvent_t g_noalloc_staging_free = nullptr;  // recorded after the last copy out of the staging array
 
 struct NoAllocDevice {
   bool ready = false;
   int sm_count = 0;
   unsigned char* scratch = nullptr;  // device address of g_noalloc_scratch on this device
+  cudaEvent_t copied = nullptr;      // this device's staging-copy event
 };
 constexpr int kNoAllocMaxDevices = 64;
 static NoAllocDevice g_noalloc_dev[kNoAllocMaxDevices];
 
 // Once per device, with that device current: the device address of the scratch
-// array (its host-side name is only a stand-in) and the kernel attributes.
+// array (its host-side name is only a stand-in), the kernel attributes and the
+// staging-copy event; once per process, the staging array is page-locked.
 static int noalloc_setup(int device, NoAllocDevice*& out) {
   if (device < 0 || device >= kNoAllocMaxDevices) {
     set_error("device index out of range");
@@ -954,12 +961,51 @@ static int noalloc_setup(int device, NoAllocDevice*& out) {
     if ((e = cudaDeviceGetAttribute(&d.sm_count, cudaDevAttrMultiProcessorCount, device)) != cudaSuccess)
       return fail_cuda(e, "cudaDeviceGetAttribute");
     if ((e = prepare_sweep_kernels()) != cudaSuccess) return fail_cuda(e, "kernel attributes");
+    if ((e = cudaEventCreateWithFlags(&d.copied, cudaEventDisableTiming)) != cudaSuccess)
+      return fail_cuda(e, "cudaEventCreate");
+    if (!g_noalloc_staging_pinned) {
+      e = cudaHostRegister(g_noalloc_staging, sizeof(g_noalloc_staging), cudaHostRegisterPortable);
+      if (e != cudaSuccess) return fail_cuda(e, "cudaHostRegister(staging)");
+      g_noalloc_staging_pinned = true;
+    }
     d.scratch = (unsigned char*)p;
     d.ready = true;
   }
   out = &d;
   return kOk;
 }
+
+// Waits until the staging array's last copy has left it (from any device).
+static int noalloc_staging_wait() {
+  if (!g_noalloc_staging_free) return kOk;
+  cudaError_t e = cudaEventSynchronize(g_noalloc_staging_free);
+  return e == cudaSuccess ? kOk : fail_cuda(e, "staging copy");
+}
+
+// Queues the copy of the first `bytes` of the staging array into the device's
+// scratch and marks the staging array busy until it has left.
+static int noalloc_stage(NoAllocDevice* dev, size_t bytes, cudaStream_t s) {
+  cudaError_t e = cudaMemcpyAsync(dev->scratch, g_noalloc_staging, bytes, cudaMemcpyHostToDevice, s);
+  if (e != cudaSuccess) return fail_cuda(e, "H2D staging");
+  if ((e = cudaEventRecord(dev->copied, s)) != cudaSuccess) return fail_cuda(e, "event record");
+  g_noalloc_staging_free = dev->copied;
+  return kOk;
+}
+
+// Results that need no sweep (theboss's empty-state rules): out[idx[i]] = val[i].
+__global__ void noalloc_scatter_kernel(const int32_t* __restrict__ idx, const double2* __restrict__ val, int n,
+                                       double2* __restrict__ out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[idx[i]] = val[i];
+}
+
+// One product-size group of a request: its sweeps' layout in the scratch.
+struct NoAllocGroup {
+  int nf = 0;
+  std::vector<int64_t> nthr;
+  int64_t threads = 0;
+  size_t o_pool = 0, o_part = 0, bytes = 0;
+};
 
 }  // namespace boss
 
@@ -979,8 +1025,12 @@ extern "C" int boss_perm_batch_noalloc(const double* matrix, int32_t m, const in
   if (st) return st;
   cudaStream_t s = (cudaStream_t)stream;
   double2* out = (double2*)results_device;
+  // (1) Plan every permanent and lay out every scratch image; reject the request
+  // before anything is queued if one image exceeds the scratch.
   std::vector<HostSweep> by_nf[kMaxFactors + 1];
   std::vector<int> which[kMaxFactors + 1];
+  std::vector<int32_t> direct_idx;
+  std::vector<double2> direct_val;
   for (int k = 0; k < count; ++k) {
     HostSweep hs;
     bool need = false;
@@ -991,37 +1041,60 @@ extern "C" int boss_perm_batch_noalloc(const double* matrix, int32_t m, const in
     if (need) {
       which[hs.nf].push_back(k);
       by_nf[hs.nf].push_back(std::move(hs));
-    } else {  // a permanent theboss defines without a sweep (empty states): one small copy
-      if ((e = cudaMemcpyAsync(out + k, &v, sizeof(double2), cudaMemcpyHostToDevice, s)) != cudaSuccess)
-        return fail_cuda(e, "H2D direct result");
+    } else {  // a permanent theboss defines without a sweep (empty states)
+      direct_idx.push_back(k);
+      direct_val.push_back(v);
     }
   }
-  // One sweep launch per product size; each reuses the scratch from its start
-  // (stream order keeps a group's copy behind the previous group's kernels).
+  const size_t o_dval = align_up(sizeof(int32_t) * direct_idx.size(), 256);
+  const size_t direct_bytes = o_dval + sizeof(double2) * direct_val.size();
+  std::vector<NoAllocGroup> groups;
   for (int nf = 1; nf <= kMaxFactors; ++nf) {
     const std::vector<HostSweep>& sw = by_nf[nf];
     const int n = (int)sw.size();
     if (n == 0) continue;
+    NoAllocGroup G;
+    G.nf = nf;
     std::vector<uint64_t> codes(n);
     for (int p = 0; p < n; ++p) codes[p] = sw[p].total_codes;
-    std::vector<int64_t> nthr;
-    partition_threads(codes, sweep_resident_threads(nf, SweepOp::kPerm, dev->sm_count), nthr);
-    int64_t pool_n = 0, threads = 0;
+    partition_threads(codes, sweep_resident_threads(nf, SweepOp::kPerm, dev->sm_count), G.nthr);
+    int64_t pool_n = 0;
     for (int p = 0; p < n; ++p) {
       pool_n += (int64_t)(sw[p].D.size() + sw[p].base.size());
-      threads += nthr[p];
+      G.threads += G.nthr[p];
     }
-    const size_t o_probs = 0;
-    const size_t o_pool = align_up(o_probs + sizeof(SweepProblem) * n, 256);
-    const size_t o_part = align_up(o_pool + sizeof(longlong2) * (size_t)std::max<int64_t>(pool_n, 1), 256);
-    const size_t need_bytes = o_part + sizeof(double2) * (size_t)threads;
-    if (need_bytes > kNoAllocScratchBytes) {
-      set_error("request needs " + std::to_string(need_bytes) + " bytes of scratch; the allocation-free entry "
-                "point has " + std::to_string(kNoAllocScratchBytes) + " (split the batch)");
-      return kErrLimit;
-    }
-    SweepProblem* hp = (SweepProblem*)(g_noalloc_staging + o_probs);
-    longlong2* hpool = (longlong2*)(g_noalloc_staging + o_pool);
+    G.o_pool = align_up(sizeof(SweepProblem) * n, 256);
+    G.o_part = align_up(G.o_pool + sizeof(longlong2) * (size_t)std::max<int64_t>(pool_n, 1), 256);
+    G.bytes = G.o_part + sizeof(double2) * (size_t)G.threads;
+    groups.push_back(std::move(G));
+  }
+  size_t need_bytes = direct_bytes;
+  for (const NoAllocGroup& G : groups) need_bytes = std::max(need_bytes, G.bytes);
+  if (need_bytes > kNoAllocScratchBytes) {
+    set_error("request needs " + std::to_string(need_bytes) + " bytes of scratch; the allocation-free entry "
+              "point has " + std::to_string(kNoAllocScratchBytes) + " (split the batch)");
+    return kErrLimit;
+  }
+  // (2) The direct results, through the staging array and a scatter kernel.
+  if (!direct_idx.empty()) {
+    if ((st = noalloc_staging_wait())) return st;
+    memcpy(g_noalloc_staging, direct_idx.data(), sizeof(int32_t) * direct_idx.size());
+    memcpy(g_noalloc_staging + o_dval, direct_val.data(), sizeof(double2) * direct_val.size());
+    if ((st = noalloc_stage(dev, direct_bytes, s))) return st;
+    const int nd = (int)direct_idx.size();
+    noalloc_scatter_kernel<<<(nd + 127) / 128, 128, 0, s>>>((const int32_t*)dev->scratch,
+                                                            (const double2*)(dev->scratch + o_dval), nd, out);
+    if ((e = cudaGetLastError()) != cudaSuccess) return fail_cuda(e, "scatter launch");
+  }
+  // (3) One sweep launch per product size; each image reuses the scratch from its
+  // start (stream order keeps it behind the previous image's kernels).
+  for (const NoAllocGroup& G : groups) {
+    const int nf = G.nf;
+    const std::vector<HostSweep>& sw = by_nf[nf];
+    const int n = (int)sw.size();
+    if ((st = noalloc_staging_wait())) return st;
+    SweepProblem* hp = (SweepProblem*)g_noalloc_staging;
+    longlong2* hpool = (longlong2*)(g_noalloc_staging + G.o_pool);
     int64_t pool_at = 0, thread_at = 0;
     for (int p = 0; p < n; ++p) {
       const HostSweep& h = sw[p];
@@ -1037,7 +1110,7 @@ extern "C" int boss_perm_batch_noalloc(const double* matrix, int32_t m, const in
       P.out_idx = which[nf][p];  // the reduction writes straight into the caller's buffer
       P.n_codes = (int64_t)h.total_codes;
       P.thread_begin = thread_at;
-      P.n_threads = nthr[p];
+      P.n_threads = G.nthr[p];
       P.mat_off = pool_at;
       std::copy(h.D.begin(), h.D.end(), hpool + pool_at);
       pool_at += (int64_t)h.D.size();
@@ -1047,19 +1120,16 @@ extern "C" int boss_perm_batch_noalloc(const double* matrix, int32_t m, const in
       P.part_off = thread_at;
       P.scale = h.scale;
       for (int i = 0; i < h.nd; ++i) P.mult[i] = h.mult[i];
-      thread_at += nthr[p];
+      thread_at += G.nthr[p];
     }
-    // Pageable source: the copy is staged before this call returns, so the host
-    // staging array can be refilled by the next group.
-    if ((e = cudaMemcpyAsync(dev->scratch, g_noalloc_staging, o_part, cudaMemcpyHostToDevice, s)) != cudaSuccess)
-      return fail_cuda(e, "H2D sweeps");
+    if ((st = noalloc_stage(dev, G.o_part, s))) return st;
     SweepLaunch L;
-    L.probs = (const SweepProblem*)(dev->scratch + o_probs);
+    L.probs = (const SweepProblem*)dev->scratch;
     L.n_probs = n;
-    L.pool = (const longlong2*)(dev->scratch + o_pool);
-    L.total_threads = threads;
-    L.partials = (double2*)(dev->scratch + o_part);
-    L.grid = (int)((threads + 127) / 128);
+    L.pool = (const longlong2*)(dev->scratch + G.o_pool);
+    L.total_threads = G.threads;
+    L.partials = (double2*)(dev->scratch + G.o_part);
+    L.grid = (int)((G.threads + 127) / 128);
     if ((e = launch_sweep(nf, SweepOp::kPerm, L, s)) != cudaSuccess) return fail_cuda(e, "sweep launch");
     if ((e = launch_perm_reduce(L.probs, n, L.partials, out, s)) != cudaSuccess) return fail_cuda(e, "reduce launch");
   }

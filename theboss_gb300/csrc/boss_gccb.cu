@@ -19,9 +19,16 @@
 #include <stdint.h>
 #include <string.h>
 
+#include <stdio.h>
+#include <stdlib.h>
+#include <sys/stat.h>
+
 #include <algorithm>
+#include <chrono>
 #include <cmath>
+#include <map>
 #include <mutex>
+#include <string>
 #include <numeric>
 #include <vector>
 
@@ -974,9 +981,102 @@ __global__ void to_fixed_kernel(const double* __restrict__ x, long long* __restr
   if (i < count) y[i] = __double2ll_rn(ldexp(x[i], fx));  // exact scaling, round to nearest even
 }
 
+// ---------------------------------------------------------------------------
+// Autotuned launch shapes.  Per level the planner picks a split (threads per
+// sample, from the level's code count and the resident threads of the kernel)
+// and the size G of the thread groups that sum their minors inside the sweep.
+// boss_gccb_autotune times candidate shapes on the caller's workload and keeps,
+// per (arithmetic, level, sample-count bucket), the split's power-of-two shift
+// and G's cap that ran fastest; the winners are cached in-process and on disk,
+// keyed by the GPU's name.
+// ---------------------------------------------------------------------------
+struct LevelTune {
+  int shift = 0;  // threads per sample = heuristic * 2^shift (clamped to [1, codes])
+  int gmax = 0;   // cap of the group size G (0: the heuristic's)
+};
+static std::map<uint64_t, LevelTune> g_level_tune;
+static bool g_tune_loaded = false;
+static std::string g_tune_gpu;
+static int g_pipeline_shift = 2;   // the pipelined first part is count >> shift (tuned: 1..4)
+static const LevelTune* g_tune_force = nullptr;  // while tuning: one shape for every level
+static std::vector<LevelTune> g_tune_force_level;  // while tuning: a shape per level (index k)
+
+static inline int sample_bucket(int64_t A) {
+  int b = 0;
+  while ((A >> (b + 1)) > 0 && b < 40) ++b;
+  return b;  // floor(log2(A))
+}
+static inline uint64_t tune_key(bool f64, int k, int64_t A) {
+  return ((uint64_t)(f64 ? 1 : 0) << 32) | ((uint64_t)k << 16) | (uint64_t)sample_bucket(A);
+}
+static std::string tune_path() {
+  const char* p = getenv("BOSS_TUNE_CACHE");
+  if (p && *p) return p;
+  const char* h = getenv("HOME");
+  return std::string(h && *h ? h : "/tmp") + "/.cache/theboss_gb300/gccb_tune.txt";
+}
+// The cache file: one line per entry, "<gpu name>|<key>|<shift>|<gmax>", and
+// "<gpu name>|pipeline|<shift>".  Lines of other GPUs are kept as they are.
+static void tune_load(int device) {
+  if (g_tune_loaded) return;
+  g_tune_loaded = true;
+  cudaDeviceProp prop;
+  if (cudaGetDeviceProperties(&prop, device) != cudaSuccess) {
+    cudaGetLastError();
+    return;
+  }
+  g_tune_gpu = prop.name;
+  FILE* f = fopen(tune_path().c_str(), "r");
+  if (!f) return;
+  char line[512];
+  while (fgets(line, sizeof(line), f)) {
+    std::string l(line);
+    const size_t a = l.find('|');
+    if (a == std::string::npos || l.substr(0, a) != g_tune_gpu) continue;
+    const std::string rest = l.substr(a + 1);
+    unsigned long long key = 0;
+    int x = 0, y = 0;
+    if (sscanf(rest.c_str(), "pipeline|%d", &x) == 1) {
+      if (x >= 1 && x <= 4) g_pipeline_shift = x;
+    } else if (sscanf(rest.c_str(), "%llu|%d|%d", &key, &x, &y) == 3) {
+      g_level_tune[(uint64_t)key] = LevelTune{std::max(-3, std::min(x, 3)), std::max(0, std::min(y, 128))};
+    }
+  }
+  fclose(f);
+}
+static void tune_save() {
+  const std::string path = tune_path();
+  std::vector<std::string> keep;
+  if (FILE* f = fopen(path.c_str(), "r")) {
+    char line[512];
+    while (fgets(line, sizeof(line), f)) {
+      std::string l(line);
+      if (l.compare(0, g_tune_gpu.size() + 1, g_tune_gpu + "|") != 0) keep.push_back(l);
+    }
+    fclose(f);
+  }
+  for (size_t i = path.find('/', 1); i != std::string::npos; i = path.find('/', i + 1))
+    mkdir(path.substr(0, i).c_str(), 0755);  // best effort: an unwritable cache only loses the cache
+  FILE* f = fopen(path.c_str(), "w");
+  if (!f) return;
+  for (const std::string& l : keep) fputs(l.c_str(), f);
+  for (const auto& kv : g_level_tune)
+    fprintf(f, "%s|%llu|%d|%d\n", g_tune_gpu.c_str(), (unsigned long long)kv.first, kv.second.shift, kv.second.gmax);
+  fprintf(f, "%s|pipeline|%d\n", g_tune_gpu.c_str(), g_pipeline_shift);
+  fclose(f);
+}
+static LevelTune level_tune(bool f64, int k, int64_t A) {
+  if (g_tune_force) return *g_tune_force;
+  if (k < (int)g_tune_force_level.size()) return g_tune_force_level[k];
+  const auto it = g_level_tune.find(tune_key(f64, k, A));
+  return it == g_level_tune.end() ? LevelTune{} : it->second;
+}
+
 // matrices: n_mats complex m x m matrices, U[out][in]; one for every sample
 // (n_mats == 1) or one per sample (n_mats == number of samples).
-static int gccb_prepare(Context* cx, const double* matrix, int n_mats, int m, Draws& D, bool timing, GccbRun& R,
+// timing: 0 none; 1 an event pair around every sweep launch; 2 an event pair
+// around every level (its sweep and its finalize).
+static int gccb_prepare(Context* cx, const double* matrix, int n_mats, int m, Draws& D, int timing, GccbRun& R,
                         int slot = 0) {
   const int N = (int)D.L.size();
   R.slot = slot;
@@ -1096,10 +1196,14 @@ static int gccb_prepare(Context* cx, const double* matrix, int n_mats, int m, Dr
       const double total = (double)code0 * Ak;
       const double want = std::max<double>(Ak, std::min<double>((double)resident, total / kMinCodesPerThread));
       int64_t tps = std::max<int64_t>(1, std::min<int64_t>((int64_t)code0, (int64_t)(want / Ak)));
+      const LevelTune lt = level_tune(f64, k, Ak);
+      if (lt.shift > 0) tps = std::min<int64_t>((int64_t)code0, tps << lt.shift);
+      if (lt.shift < 0) tps = std::max<int64_t>(1, tps >> -lt.shift);
       // Each aligned group of G threads of a sample sums its minors inside the sweep:
       // the largest G (up to a warp; up to a block of 128 for float-pair sweeps whose
       // threads then fill whole blocks) that costs at most 2% of the sample's threads.
       int G = ffl[k] ? 128 : 32;
+      if (lt.gmax > 0) G = std::min(G, lt.gmax);
       auto ok = [&](int g) {
         if (!(tps >= g && (double)(tps / g * g) >= 0.98 * (double)tps)) return false;
         return g <= 32 || ((tps / g * g) * (int64_t)Ak) % 128 == 0;
@@ -1119,7 +1223,11 @@ static int gccb_prepare(Context* cx, const double* matrix, int n_mats, int m, Dr
       continue;
     }
     std::vector<int64_t> nthr;
-    partition_threads(codes, resident, nthr);
+    {
+      const LevelTune lt = level_tune(f64, k, Ak);
+      const int64_t res = lt.shift >= 0 ? resident << lt.shift : std::max<int64_t>(1, resident >> -lt.shift);
+      partition_threads(codes, res, nthr);
+    }
     auto& t = tab[k];
     t.resize(Ak);
     int64_t threads = 0, parts = 0, pool = 0;
@@ -1212,7 +1320,7 @@ static int gccb_prepare(Context* cx, const double* matrix, int n_mats, int m, Dr
   }
   destroy_events(R);
   if (timing) {
-    R.ev.resize(2 * (size_t)std::max(Lmax - 1, 0));
+    R.ev.resize(2 * (size_t)std::max(timing == 2 ? Lmax : Lmax - 1, 0));
     for (auto& ev : R.ev)
       if ((e = cudaEventCreate(&ev)) != cudaSuccess) return fail_cuda(e, "event create");
   }
@@ -1236,9 +1344,11 @@ static int gccb_prepare(Context* cx, const double* matrix, int n_mats, int m, Dr
       SL.grid = (int)((lvl_threads[k] + 127) / 128);
       SL.rows = std::min(k, kMaxMinorDigits);
       SL.uniform_threads = uniform[k] ? uni_lvl[k].n_threads : 0;
-      if (timing) le = cudaEventRecordWithFlags(R.ev[2 * (k - 2)], s, cudaEventRecordExternal);
+      if (timing == 1) le = cudaEventRecordWithFlags(R.ev[2 * (k - 2)], s, cudaEventRecordExternal);
+      if (timing == 2) le = cudaEventRecordWithFlags(R.ev[2 * (k - 1)], s, cudaEventRecordExternal);
       if (le == cudaSuccess) le = launch_sweep(k - 1, ffl[k] ? SweepOp::kMinorsFF : SweepOp::kMinors, SL, s);
-      if (timing && le == cudaSuccess) le = cudaEventRecordWithFlags(R.ev[2 * (k - 2) + 1], s, cudaEventRecordExternal);
+      if (timing == 1 && le == cudaSuccess)
+        le = cudaEventRecordWithFlags(R.ev[2 * (k - 2) + 1], s, cudaEventRecordExternal);
       if (le != cudaSuccess) break;
       ++R.kernels;
       ++R.sweeps;
@@ -1275,11 +1385,15 @@ static int gccb_prepare(Context* cx, const double* matrix, int n_mats, int m, Dr
     fa.next_ff = (k < Lmax) ? ffl[k + 1] : 0;
     fa.cur_ff = (k >= 2) ? ffl[k] : 0;
     fa.err = R.derr;
+    if (timing == 2 && k == 1) le = cudaEventRecordWithFlags(R.ev[0], s, cudaEventRecordExternal);
+    if (le != cudaSuccess) break;
     if (f64)
       gccb_finalize_kernel<true><<<(A[k] + kFinWarps - 1) / kFinWarps, kFinWarps * 32, 0, s>>>(fa);
     else
       gccb_finalize_kernel<false><<<(A[k] + kFinWarps - 1) / kFinWarps, kFinWarps * 32, 0, s>>>(fa);
     le = cudaGetLastError();
+    if (timing == 2 && le == cudaSuccess)
+      le = cudaEventRecordWithFlags(R.ev[2 * (k - 1) + 1], s, cudaEventRecordExternal);
     ++R.kernels;
   }
   e = cudaStreamEndCapture(s, &graph);
@@ -1358,7 +1472,7 @@ static int gccb_collect(Context* cx, GccbRun& R, int32_t* samples_out) {
 static int run_gccb(Context* cx, const double* matrix, int n_mats, int m, Draws& D, int32_t* samples_out) {
   if (D.L.empty()) return kOk;
   GccbRun R;
-  int st = gccb_prepare(cx, matrix, n_mats, m, D, false, R);
+  int st = gccb_prepare(cx, matrix, n_mats, m, D, 0, R);
   if (st) return st;
   if ((st = gccb_launch(cx))) return st;
   return gccb_collect(cx, R, samples_out);
@@ -1378,6 +1492,237 @@ static void keep_rows(Draws& D, int first, int count) {
   D.u.erase(D.u.begin(), D.u.begin() + first * rs);
   D.u.resize(count * rs);
   D.modes.clear();
+}
+
+// Samples [first, first + count) of the stream of n_samples samples drawn from
+// `mt` (advanced over the whole stream).  The API lock is held by the caller.
+static int sample_slice_locked(const double* matrix, int m, const int32_t* input_state,
+                               const double* particle_weights, int nw, MT19937& mt, int n_samples, int first,
+                               int count, int32_t* samples) {
+  // Large batches run as two parts: the host replays and plans the second part
+  // while the GPU samples the first (separate buffers, pinned memory and graphs).
+  // The first part is count >> g_pipeline_shift (a quarter unless tuned), so that
+  // the GPU starts early and the host's work on the rest (~0.1 ms per 10^3
+  // samples) still ends before the GPU finishes the first part (~0.45 ms plus
+  // ~0.3 ms per 10^3 samples).
+  const int halves = (count >= kGccbPipelineMin) ? 2 : 1;
+  const int c0 = (halves == 2) ? (count >> g_pipeline_shift) : count;
+  const int cut[3] = {first, first + c0, first + count};
+  GccbRun R[2];
+  bool launched[2] = {false, false};
+  Context* cx = nullptr;
+  int st = kOk;
+  int done = 0;  // stream samples replayed so far
+  for (int h = 0; h < halves; ++h) {
+    Draws D;
+    const int upto = (h + 1 == halves) ? n_samples : cut[h + 1];  // the last half replays the stream's tail
+    st = predraw(input_state, m, particle_weights, nw, mt, upto - done, D);
+    if (st) return st;
+    if (D.n > kMaxMinorDigits) {
+      set_error("the batched sampler supports at most 32 input particles");
+      return kErrLimit;
+    }
+    keep_rows(D, cut[h] - done, cut[h + 1] - cut[h]);
+    done = upto;
+    if (!std::any_of(D.L.begin(), D.L.end(), [](int32_t l) { return l > 0; })) continue;
+    if (!cx && !(cx = context(&st))) return st;
+    if ((st = gccb_prepare(cx, matrix, 1, m, D, 0, R[h], h))) return st;
+    if ((st = gccb_launch(cx, h))) return st;
+    if ((st = gccb_queue_results(cx, R[h]))) return st;
+    launched[h] = true;
+  }
+  if (cx) {
+    cudaError_t e = cudaStreamSynchronize(cx->stream);
+    if (e != cudaSuccess) return fail_cuda(e, "sampler");
+  }
+  for (int h = 0; h < halves && count > 0; ++h) {  // every row is written: sampled, or empty
+    int32_t* rows = samples + (size_t)(cut[h] - first) * m;
+    if (launched[h]) {
+      if ((st = gccb_read_results(R[h], rows))) return st;
+    } else {
+      memset(rows, 0, sizeof(int32_t) * (size_t)(cut[h + 1] - cut[h]) * m);
+    }
+  }
+  return kOk;
+}
+
+// Samples with at least k particles, k = 0..Lmax.
+static std::vector<int64_t> level_counts(const Draws& D) {
+  int Lmax = 0;
+  for (int32_t l : D.L) Lmax = std::max(Lmax, (int)l);
+  std::vector<int64_t> A(Lmax + 2, 0);
+  for (int32_t l : D.L) A[l]++;
+  for (int k = Lmax - 1; k >= 0; --k) A[k] += A[k + 1];
+  return A;
+}
+
+// Whether every level of this workload (the draws of `count` samples from a copy
+// of `mt`) already has a tuned entry.
+static bool workload_tuned(const int32_t* input_state, int m, const double* weights, int nw, const MT19937& mt,
+                           int count) {
+  MT19937 t = mt;
+  Draws D;
+  if (predraw(input_state, m, weights, nw, t, count, D)) return true;  // errors surface in the call itself
+  const std::vector<int64_t> A = level_counts(D);
+  const bool f64 = (g_minors_arith != 0);
+  for (int k = 2; k + 1 < (int)A.size(); ++k)
+    if (A[k] > 0 && !g_level_tune.count(tune_key(f64, k, A[k]))) return false;
+  return true;
+}
+
+// Per-level times (minimum over reps, after one warm-up run) of the graph with
+// the current forced shapes; lvl_ms[k] covers level k's sweep and finalize.
+static int tune_levels(Context* cx, const double* matrix, int m, Draws& D, int reps, std::vector<double>& lvl_ms) {
+  GccbRun R;
+  int st = gccb_prepare(cx, matrix, 1, m, D, 2, R);
+  if (st) return st;
+  lvl_ms.assign(R.Lmax + 2, 1e30);
+  for (int it = 0; it <= reps && !st; ++it) {
+    if ((st = gccb_launch(cx))) break;
+    const cudaError_t e = cudaStreamSynchronize(cx->stream);
+    if (e != cudaSuccess) {
+      st = fail_cuda(e, "autotune");
+      break;
+    }
+    for (int k = 1; it > 0 && k <= R.Lmax; ++k) {
+      float x = 0.f;
+      if (cudaEventElapsedTime(&x, R.ev[2 * (k - 1)], R.ev[2 * (k - 1) + 1]) == cudaSuccess)
+        lvl_ms[k] = std::min(lvl_ms[k], (double)x);
+      else
+        cudaGetLastError();
+    }
+  }
+  destroy_events(R);
+  return st;
+}
+
+// The plain graph's step time (minimum over reps, after one warm-up run).
+static int tune_step(Context* cx, const double* matrix, int m, Draws& D, int reps, double& ms) {
+  GccbRun R;
+  int st = gccb_prepare(cx, matrix, 1, m, D, 0, R);
+  if (st) return st;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  ms = 1e30;
+  for (int it = 0; it <= reps && !st; ++it) {
+    cudaEventRecord(e0, cx->stream);
+    if ((st = gccb_launch(cx))) break;
+    cudaEventRecord(e1, cx->stream);
+    const cudaError_t e = cudaEventSynchronize(e1);
+    if (e != cudaSuccess) {
+      st = fail_cuda(e, "autotune");
+      break;
+    }
+    float x = 0.f;
+    if (it > 0 && cudaEventElapsedTime(&x, e0, e1) == cudaSuccess) ms = std::min(ms, (double)x);
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  return st;
+}
+
+// The tuner: times the levels under power-of-two shifts of the split, then under
+// caps of the group size G, keeps each level's fastest shape if the whole step
+// gets faster, then times the pipelined first part's size on end-to-end calls.
+// report[0..5]: step ms with the heuristic shapes and with the tuned ones, levels
+// whose shape changed, the pipeline shift, end-to-end ms with the quarter split
+// and with the tuned split (0 when the call is below the pipelining size).
+static int gccb_autotune_locked(Context* cx, const double* matrix, int m, const int32_t* input_state,
+                                const double* weights, int nw, const MT19937& mt0, int n_samples, int reps,
+                                double* report) {
+  for (int i = 0; i < 8; ++i) report[i] = 0.0;
+  MT19937 mt = mt0;
+  Draws D;
+  int st = predraw(input_state, m, weights, nw, mt, n_samples, D);
+  if (st) return st;
+  if (D.n > kMaxMinorDigits || D.n < 1) {
+    set_error("the batched sampler needs 1..32 input particles");
+    return kErrLimit;
+  }
+  const std::vector<int64_t> A = level_counts(D);
+  const int Lmax = (int)A.size() - 2;
+  if (Lmax < 1) return kOk;
+  const bool f64 = (g_minors_arith != 0);
+  struct ForceGuard {
+    ~ForceGuard() {
+      g_tune_force = nullptr;
+      g_tune_force_level.clear();
+    }
+  } guard;
+  const LevelTune none{};
+  std::vector<LevelTune> best(Lmax + 1);
+  std::vector<double> best_ms, ms;
+  double step0 = 0.0, step1 = 0.0;
+  g_tune_force = &none;
+  if ((st = tune_step(cx, matrix, m, D, reps, step0))) return st;
+  if ((st = tune_levels(cx, matrix, m, D, reps, best_ms))) return st;
+  for (int sh : {-2, -1, 1, 2}) {  // the split
+    const LevelTune c{sh, 0};
+    g_tune_force = &c;
+    if ((st = tune_levels(cx, matrix, m, D, reps, ms))) return st;
+    for (int k = 2; k <= Lmax; ++k)
+      if (ms[k] < 0.97 * best_ms[k]) {
+        best_ms[k] = ms[k];
+        best[k] = c;
+      }
+  }
+  g_tune_force = nullptr;
+  for (int gm : {1, 4, 8, 16}) {  // the group size's cap, with each level's best split
+    g_tune_force_level.assign(Lmax + 1, LevelTune{});
+    for (int k = 2; k <= Lmax; ++k) g_tune_force_level[k] = LevelTune{best[k].shift, gm};
+    if ((st = tune_levels(cx, matrix, m, D, reps, ms))) return st;
+    for (int k = 2; k <= Lmax; ++k)
+      if (ms[k] < 0.97 * best_ms[k]) {
+        best_ms[k] = ms[k];
+        best[k].gmax = gm;
+      }
+  }
+  g_tune_force_level = best;
+  if ((st = tune_step(cx, matrix, m, D, reps, step1))) return st;
+  g_tune_force_level.clear();
+  const bool keep = step1 < step0;
+  int changed = 0;
+  for (int k = 2; k <= Lmax; ++k) {
+    if (A[k] <= 0) continue;
+    const LevelTune v = keep ? best[k] : LevelTune{};
+    g_level_tune[tune_key(f64, k, A[k])] = v;
+    changed += (v.shift != 0 || v.gmax != 0) ? 1 : 0;
+  }
+  report[0] = step0;
+  report[1] = keep ? step1 : step0;
+  report[2] = changed;
+  // The pipelined split, on end-to-end calls of the same stream.
+  report[3] = g_pipeline_shift;
+  if (n_samples >= kGccbPipelineMin) {
+    std::vector<int32_t> out((size_t)n_samples * m);
+    double best_e2e = 1e30;
+    int best_shift = g_pipeline_shift;
+    for (int sh : {2, 1, 3, 4}) {  // the quarter split first: the reference point
+      g_pipeline_shift = sh;
+      double t_min = 1e30;
+      for (int it = 0; it <= reps; ++it) {
+        MT19937 t = mt0;
+        const auto t0 = std::chrono::steady_clock::now();
+        if ((st = sample_slice_locked(matrix, m, input_state, weights, nw, t, n_samples, 0, n_samples, out.data())))
+          break;
+        const double dt = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+        if (it > 0) t_min = std::min(t_min, dt);
+      }
+      if (st) break;
+      if (sh == 2) report[4] = t_min;
+      if (t_min < 0.97 * best_e2e || (sh == 2 && t_min < best_e2e)) {
+        best_e2e = t_min;
+        best_shift = sh;
+      }
+    }
+    g_pipeline_shift = best_shift;
+    report[3] = best_shift;
+    report[5] = best_e2e;
+    if (st) return st;
+  }
+  tune_save();
+  return kOk;
 }
 
 }  // namespace boss
@@ -1448,51 +1793,44 @@ int boss_gccb_sample_slice(const double* matrix, int32_t m, const int32_t* input
   int st = load_mt(mt, mt_key, mt_pos);
   if (st) return st;
   const int nw = particle_weights ? n_weights : 0;
-  // Large batches run as two parts: the host replays and plans the second part
-  // while the GPU samples the first (separate buffers, pinned memory and graphs).
-  // The first part is a quarter, so that the GPU starts early and the host's work
-  // on the rest (~0.1 ms per 10^3 samples) still ends before the GPU finishes the
-  // first part (~0.45 ms plus ~0.3 ms per 10^3 samples).
-  const int halves = (count >= kGccbPipelineMin) ? 2 : 1;
-  const int c0 = (halves == 2) ? count / 4 : count;
-  const int cut[3] = {first, first + c0, first + count};
-  GccbRun R[2];
-  bool launched[2] = {false, false};
-  Context* cx = nullptr;
-  int done = 0;  // stream samples replayed so far
-  for (int h = 0; h < halves; ++h) {
-    Draws D;
-    const int upto = (h + 1 == halves) ? n_samples : cut[h + 1];  // the last half replays the stream's tail
-    st = predraw(input_state, m, particle_weights, nw, mt, upto - done, D);
-    if (st) return st;
-    if (D.n > kMaxMinorDigits) {
-      set_error("the batched sampler supports at most 32 input particles");
-      return kErrLimit;
-    }
-    keep_rows(D, cut[h] - done, cut[h + 1] - cut[h]);
-    done = upto;
-    if (!std::any_of(D.L.begin(), D.L.end(), [](int32_t l) { return l > 0; })) continue;
-    if (!cx && !(cx = context(&st))) return st;
-    if ((st = gccb_prepare(cx, matrix, 1, m, D, false, R[h], h))) return st;
-    if ((st = gccb_launch(cx, h))) return st;
-    if ((st = gccb_queue_results(cx, R[h]))) return st;
-    launched[h] = true;
-  }
-  if (cx) {
-    cudaError_t e = cudaStreamSynchronize(cx->stream);
-    if (e != cudaSuccess) return fail_cuda(e, "sampler");
-  }
-  for (int h = 0; h < halves && count > 0; ++h) {  // every row is written: sampled, or empty
-    int32_t* rows = samples + (size_t)(cut[h] - first) * m;
-    if (launched[h]) {
-      if ((st = gccb_read_results(R[h], rows))) return st;
-    } else {
-      memset(rows, 0, sizeof(int32_t) * (size_t)(cut[h + 1] - cut[h]) * m);
+  const char* at = getenv("BOSS_AUTOTUNE");
+  if (at && at[0] == '1' && count > 0) {  // tune once per workload shape, on this call's own draws
+    Context* cx = context(&st);
+    if (!cx) return st;
+    tune_load(cx->device);
+    if (!workload_tuned(input_state, m, particle_weights, nw, mt, count)) {
+      double report[8];
+      if ((st = gccb_autotune_locked(cx, matrix, m, input_state, particle_weights, nw, mt, count, 3, report)))
+        return st;
     }
   }
+  if ((st = sample_slice_locked(matrix, m, input_state, particle_weights, nw, mt, n_samples, first, count, samples)))
+    return st;
   memcpy(mt_key, mt.key, sizeof(mt.key));
   *mt_pos = mt.pos;
   return kOk;
+}
+
+int boss_gccb_autotune(const double* matrix, int32_t m, const int32_t* input_state, const double* particle_weights,
+                       int32_t n_weights, const uint32_t* mt_key, const int32_t* mt_pos, int32_t n_samples,
+                       int32_t reps, double* report) {
+  if (!matrix || !input_state || !report || m <= 0 || n_samples <= 0 || reps <= 0) {
+    set_error("null pointer or bad size");
+    return kErrArg;
+  }
+  if (m > 256) {
+    set_error("the batched sampler supports at most 256 modes");
+    return kErrLimit;
+  }
+  std::lock_guard<std::mutex> lk(g_api_mutex);
+  MT19937 mt;
+  int st = load_mt(mt, mt_key, mt_pos);
+  if (st) return st;
+  Context* cx = context(&st);
+  if (!cx) return st;
+  tune_load(cx->device);
+  return gccb_autotune_locked(cx, matrix, m, input_state, particle_weights, particle_weights ? n_weights : 0, mt,
+                              n_samples, reps, report);
 }
 
 int boss_gccb_near_ties(int64_t* count, int32_t reset) {
@@ -1566,7 +1904,7 @@ int boss_gccb_bench(const double* matrix, int32_t m, const int32_t* input_state,
   cudaError_t e = cudaSuccess;
   // (1) the plain graph, timed per step
   GccbRun R;
-  st = gccb_prepare(cx, matrix, 1, m, D, false, R);
+  st = gccb_prepare(cx, matrix, 1, m, D, 0, R);
   for (int it = 0; !st && it < n_warmup + n_steps; ++it) {
     if (flush_bytes > 0 && (e = cudaMemsetAsync(cx->misc.ptr, it & 0xff, (size_t)flush_bytes, cx->stream)))
       break;
@@ -1584,7 +1922,7 @@ int boss_gccb_bench(const double* matrix, int32_t m, const int32_t* input_state,
   // (2) the same work with an event pair around every sweep launch: the sweep
   // kernels' share of a step (event nodes cost time, so steps are not timed here)
   GccbRun RT;
-  if (!st && e == cudaSuccess) st = gccb_prepare(cx, matrix, 1, m, D, true, RT);
+  if (!st && e == cudaSuccess) st = gccb_prepare(cx, matrix, 1, m, D, 1, RT);
   for (int it = 0; !st && e == cudaSuccess && it < n_steps; ++it) {
     if (flush_bytes > 0 && (e = cudaMemsetAsync(cx->misc.ptr, it & 0xff, (size_t)flush_bytes, cx->stream)))
       break;
