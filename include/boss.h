@@ -217,7 +217,9 @@ BOSS_API int boss_gccb_near_ties(int64_t* count, int32_t reset);
  * report (8 doubles): step ms with the heuristic shapes, step ms with the tuned
  * shapes, levels whose shape changed, the pipeline shift (first part = count >>
  * shift), end-to-end ms with the quarter split and with the tuned split (0 below
- * 4096 samples).  No reference counterpart.
+ * 4096 samples), and the summed per-level times of the heuristic shapes (each
+ * level from its sweep's start to its finalize's end; the step time minus this is
+ * the time between levels).  No reference counterpart.
  */
 BOSS_API int boss_gccb_autotune(const double* matrix, int32_t m, const int32_t* input_state,
                                 const double* particle_weights, int32_t n_weights, const uint32_t* mt_key,

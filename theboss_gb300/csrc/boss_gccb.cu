@@ -414,28 +414,54 @@ __global__ void __launch_bounds__(kFinWarps * 32) gccb_finalize_kernel(FinalizeA
           if (lane == d) subf_s[w][d] = make_float4(rh * sc, rl * sc, ih * sc, il * sc);
         }
       }
-    } else if (parts <= 64) {  // lane d sums digit d's partials
-      if (lane < nd) {
+    } else {
+      // FP64 partials (parts x nd), summed in a fixed order.  Every FP64
+      // instruction holds the pipe for a whole warp however few lanes are active,
+      // so the lanes are spread over the partials: either gc = 32 / nd groups of
+      // nd lanes (lane g * nd + d sums rows g, g + gc, .. of digit d, then lane d
+      // adds up the gc group sums), or, with many partials, all 32 lanes stripe
+      // over each digit's rows and a butterfly sums them; whichever issues fewer
+      // FP64 instructions.
+      const int gc = 32 / nd;
+      const int64_t cost_groups = 2 * ((parts + gc - 1) / gc) + 2 * (gc - 1);
+      const int64_t cost_stripes = (int64_t)nd * (2 * ((parts + 31) / 32) + 10);
+      if (cost_groups <= cost_stripes) {
+        const int g = lane / nd, d = lane - g * nd;
         double sx = 0.0, sy = 0.0;
-#pragma unroll 8
-        for (int64_t q = 0; q < parts; ++q) {
-          const double2 v = a.partials[P.part_off + q * nd + lane];
-          sx += v.x;
-          sy += v.y;
+        if (g < gc) {
+#pragma unroll 4
+          for (int64_t q = g; q < parts; q += gc) {
+            const double2 v = a.partials[P.part_off + q * nd + d];
+            sx += v.x;
+            sy += v.y;
+          }
         }
-        sub_s[w][lane] = make_double2(sx * P.scale, sy * P.scale);
-      }
-    } else {  // many partials: the lanes stripe over them, then a fixed-order warp sum
-      for (int d = 0; d < nd; ++d) {
-        double sx = 0.0, sy = 0.0;
-        for (int64_t q = lane; q < parts; q += 32) {
-          const double2 v = a.partials[P.part_off + q * nd + d];
-          sx += v.x;
-          sy += v.y;
+        sub_s[w][lane] = make_double2(sx, sy);
+        __syncwarp();
+        if (lane < nd) {
+          double tx = 0.0, ty = 0.0;
+          for (int gg = 0; gg < gc; ++gg) {
+            const double2 v = sub_s[w][gg * nd + lane];
+            tx += v.x;
+            ty += v.y;
+          }
+          sx = tx * P.scale;
+          sy = ty * P.scale;
         }
-        sx = warp_sum(sx);
-        sy = warp_sum(sy);
-        if (lane == d) sub_s[w][d] = make_double2(sx * P.scale, sy * P.scale);
+        __syncwarp();
+        if (lane < nd) sub_s[w][lane] = make_double2(sx, sy);
+      } else {  // many partials: the lanes stripe over them, then a fixed-order warp sum
+        for (int d = 0; d < nd; ++d) {
+          double sx = 0.0, sy = 0.0;
+          for (int64_t q = lane; q < parts; q += 32) {
+            const double2 v = a.partials[P.part_off + q * nd + d];
+            sx += v.x;
+            sy += v.y;
+          }
+          sx = warp_sum(sx);
+          sy = warp_sum(sy);
+          if (lane == d) sub_s[w][d] = make_double2(sx * P.scale, sy * P.scale);
+        }
       }
     }
     if (lane < nd) {
@@ -1625,9 +1651,11 @@ static int tune_step(Context* cx, const double* matrix, int m, Draws& D, int rep
 // The tuner: times the levels under power-of-two shifts of the split, then under
 // caps of the group size G, keeps each level's fastest shape if the whole step
 // gets faster, then times the pipelined first part's size on end-to-end calls.
-// report[0..5]: step ms with the heuristic shapes and with the tuned ones, levels
+// report[0..6]: step ms with the heuristic shapes and with the tuned ones, levels
 // whose shape changed, the pipeline shift, end-to-end ms with the quarter split
-// and with the tuned split (0 when the call is below the pipelining size).
+// and with the tuned split (0 when the call is below the pipelining size), and the
+// sum over levels of each level's own time (sweep to end of finalize, heuristic
+// shapes): the step minus it is the graph's time between levels.
 static int gccb_autotune_locked(Context* cx, const double* matrix, int m, const int32_t* input_state,
                                 const double* weights, int nw, const MT19937& mt0, int n_samples, int reps,
                                 double* report) {
@@ -1657,6 +1685,7 @@ static int gccb_autotune_locked(Context* cx, const double* matrix, int m, const 
   g_tune_force = &none;
   if ((st = tune_step(cx, matrix, m, D, reps, step0))) return st;
   if ((st = tune_levels(cx, matrix, m, D, reps, best_ms))) return st;
+  for (int k = 1; k <= Lmax; ++k) report[6] += best_ms[k];  // the levels' own time, gaps excluded
   for (int sh : {-2, -1, 1, 2}) {  // the split
     const LevelTune c{sh, 0};
     g_tune_force = &c;
