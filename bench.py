@@ -223,6 +223,34 @@ def cpu_baseline(U, inp, w, seed, budget_s=10.0, gpu_samples=None):
     return res, parity
 
 
+def theboss_python_line(U, inp, seed, gpu_samples, n=32):
+    """theboss's own GCC-B sampler (its unmodified Python, installed in
+    baseline/_ref: generalized_cliffords_b_uniform_losses_simulation_strategy.py
+    with its Ryser calculator), single-threaded on the host, on the first n samples
+    of the workload's stream (same seed and matrix as the GPU's timed step): its
+    speed, and whether its samples equal the GPU's."""
+    ref = os.path.join(ROOT, "baseline", "_ref")
+    if not os.path.isdir(os.path.join(ref, "theboss")):
+        return {"unavailable": "theboss is not installed in baseline/_ref"}
+    sys.path.insert(0, ref)
+    try:
+        from theboss.boson_sampling_utilities.permanent_calculators.ryser_permanent_calculator import (
+            RyserPermanentCalculator)
+        from theboss.simulation_strategies.generalized_cliffords_b_uniform_losses_simulation_strategy import (
+            GeneralizedCliffordsBUniformLossesSimulationStrategy)
+    finally:
+        sys.path.remove(ref)
+    np.random.seed(seed)
+    strat = GeneralizedCliffordsBUniformLossesSimulationStrategy(RyserPermanentCalculator(U), ETA)
+    t = time.perf_counter()
+    out = strat.simulate(list(inp), n)
+    dt = time.perf_counter() - t
+    return {"value": n / dt, "unit": "samples/s", "cores": 1, "kind": "theboss's own Python (baseline/_ref)",
+            "sample": f"the first {n} samples of the workload's stream (same seed and matrix), {dt:.1f} s",
+            "samples_equal_to_gpu": bool(np.array_equal(np.array(out, dtype=np.int64),
+                                                         np.asarray(gpu_samples[:n], dtype=np.int64)))}
+
+
 def c2_patterns(n, count, seed):
     """Output patterns with about 20% of the occupied modes doubly occupied."""
     rng = np.random.default_rng(seed)
@@ -612,6 +640,8 @@ def run_ours(args, rank, world):
     if rank == 0:
         line["cpu_baseline"], parity = cpu_baseline(U, inp, w, args.seed, gpu_samples=b["samples"])
         line["parity"] = parity
+        if not args.quick:
+            line["theboss_python"] = theboss_python_line(U, inp, args.seed, b["samples"])
         print(json.dumps(line), flush=True)
         if parity["gpu_disagrees_with_double_double"]:
             raise SystemExit("the device-timed samples differ from the oracle's beyond its near ties")
