@@ -417,20 +417,30 @@ __global__ void __launch_bounds__(kFinWarps * 32) gccb_finalize_kernel(FinalizeA
     } else {
       // FP64 partials (parts x nd), summed in a fixed order.  Every FP64
       // instruction holds the pipe for a whole warp however few lanes are active,
-      // so the lanes are spread over the partials: either gc = 32 / nd groups of
+      // so the lanes are spread over the partials: either gc <= 32 / nd groups of
       // nd lanes (lane g * nd + d sums rows g, g + gc, .. of digit d, then lane d
-      // adds up the gc group sums), or, with many partials, all 32 lanes stripe
-      // over each digit's rows and a butterfly sums them; whichever issues fewer
-      // FP64 instructions.
-      const int gc = 32 / nd;
-      const int64_t cost_groups = 2 * ((parts + gc - 1) / gc) + 2 * (gc - 1);
+      // adds up the gc group sums; gc = 1 is one lane per digit), or, with many
+      // partials, all 32 lanes stripe over each digit's rows and a butterfly sums
+      // them; whichever issues fewer FP64 instructions.
+      int gc = 1;
+      int64_t cost_groups = 2 * (parts - 1);  // each group's first row is a copy, not an add
+      for (int g2 = 2; g2 * nd <= 32 && g2 <= parts; ++g2) {
+        const int64_t c = 2 * ((parts + g2 - 1) / g2 - 1) + 2 * (g2 - 1);
+        if (c < cost_groups) {
+          cost_groups = c;
+          gc = g2;
+        }
+      }
       const int64_t cost_stripes = (int64_t)nd * (2 * ((parts + 31) / 32) + 10);
       if (cost_groups <= cost_stripes) {
         const int g = lane / nd, d = lane - g * nd;
         double sx = 0.0, sy = 0.0;
-        if (g < gc) {
+        if (g < gc) {  // gc <= parts: every group has a first row
+          const double2 v0 = a.partials[P.part_off + (int64_t)g * nd + d];
+          sx = v0.x;
+          sy = v0.y;
 #pragma unroll 4
-          for (int64_t q = g; q < parts; q += gc) {
+          for (int64_t q = g + gc; q < parts; q += gc) {
             const double2 v = a.partials[P.part_off + q * nd + d];
             sx += v.x;
             sy += v.y;
@@ -439,8 +449,8 @@ __global__ void __launch_bounds__(kFinWarps * 32) gccb_finalize_kernel(FinalizeA
         sub_s[w][lane] = make_double2(sx, sy);
         __syncwarp();
         if (lane < nd) {
-          double tx = 0.0, ty = 0.0;
-          for (int gg = 0; gg < gc; ++gg) {
+          double tx = sx, ty = sy;  // group 0 is this lane's own sum
+          for (int gg = 1; gg < gc; ++gg) {
             const double2 v = sub_s[w][gg * nd + lane];
             tx += v.x;
             ty += v.y;
