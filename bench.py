@@ -373,14 +373,19 @@ def adjoint_section(seed):
     S2 = np.zeros((64, m2), dtype=np.int32)
     S2[:, :n2] = 1
     T2 = patterns(m2, n2, 64, seed + 2)
-    _native.perm_batch(U, S2, T2, _native.GLYNN)
-    t0 = time.perf_counter()
-    _native.perm_batch(U, S2, T2, _native.GLYNN)
-    t1 = time.perf_counter()
+    _native.perm_batch(U, S2, T2, _native.GLYNN)  # warm-up of both (buffers, kernel attributes)
     _native.perm_grad_batch(U, S2, T2)
-    t2 = time.perf_counter()
-    c5 = {"forward_ms": 1e3 * (t1 - t0), "gradient_ms": 1e3 * (t2 - t1), "gradient_over_forward": (t2 - t1) / (t1 - t0),
-          "patterns": 64, "n": n2, "m": m2}
+    fw2, gr2 = [], []
+    for _ in range(3):
+        t0 = time.perf_counter()
+        _native.perm_batch(U, S2, T2, _native.GLYNN)
+        t1 = time.perf_counter()
+        _native.perm_grad_batch(U, S2, T2)
+        t2 = time.perf_counter()
+        fw2.append(t1 - t0)
+        gr2.append(t2 - t1)
+    c5 = {"forward_ms": 1e3 * min(fw2), "gradient_ms": 1e3 * min(gr2), "gradient_over_forward": min(gr2) / min(fw2),
+          "patterns": 64, "n": n2, "m": m2, "timing": "minimum of 3 calls of each, after one warm-up call of each"}
     return {"clements_log_likelihood_n12_m24": c4, "gradients_n24_m48": c5}
 
 

@@ -43,7 +43,8 @@ Context* context(int* status) {
     *status = fail_cuda(e, "cudaDeviceGetAttribute");
     return nullptr;
   }
-  if ((e = cudaStreamCreateWithFlags(&g_ctx.stream, cudaStreamNonBlocking)) != cudaSuccess) {
+  if ((e = cudaStreamCreateWithFlags(&g_ctx.stream, cudaStreamNonBlocking)) != cudaSuccess ||
+      (e = cudaStreamCreateWithFlags(&g_ctx.stream2, cudaStreamNonBlocking)) != cudaSuccess) {
     *status = fail_cuda(e, "cudaStreamCreate");
     return nullptr;
   }

@@ -968,7 +968,7 @@ static int64_t g_gccb_near_ties = 0;
 // staging buffer and a graph each): the host can plan one batch while the GPU
 // runs the other.
 constexpr int kGccbSlots = 2;
-constexpr int kGccbPipelineMin = 4096;  // samples from which a call runs as two pipelined halves
+constexpr int kGccbPipelineMin = 4096;  // samples from which a call runs as pipelined parts
 static cudaGraphExec_t g_gccb_exec[kGccbSlots] = {nullptr, nullptr};
 static void* g_gccb_pinned[kGccbSlots] = {nullptr, nullptr};
 static size_t g_gccb_pinned_bytes[kGccbSlots] = {0, 0};
@@ -1033,7 +1033,8 @@ struct LevelTune {
 static std::map<uint64_t, LevelTune> g_level_tune;
 static bool g_tune_loaded = false;
 static std::string g_tune_gpu;
-static int g_pipeline_shift = 2;   // the pipelined first part is count >> shift (tuned: 1..4)
+static int g_pipeline_shift = 3;   // the pipelined first part is count >> shift (tuned: 1..4)
+static int g_pipeline_parts = 2;   // parts after the first one (tuned: 1..4)
 static const LevelTune* g_tune_force = nullptr;  // while tuning: one shape for every level
 static std::vector<LevelTune> g_tune_force_level;  // while tuning: a shape per level (index k)
 
@@ -1052,7 +1053,7 @@ static std::string tune_path() {
   return std::string(h && *h ? h : "/tmp") + "/.cache/theboss_gb300/gccb_tune.txt";
 }
 // The cache file: one line per entry, "<gpu name>|<key>|<shift>|<gmax>", and
-// "<gpu name>|pipeline|<shift>".  Lines of other GPUs are kept as they are.
+// "<gpu name>|pipeline|<shift>|<parts>".  Lines of other GPUs are kept as they are.
 static void tune_load(int device) {
   if (g_tune_loaded) return;
   g_tune_loaded = true;
@@ -1072,8 +1073,9 @@ static void tune_load(int device) {
     const std::string rest = l.substr(a + 1);
     unsigned long long key = 0;
     int x = 0, y = 0;
-    if (sscanf(rest.c_str(), "pipeline|%d", &x) == 1) {
+    if (sscanf(rest.c_str(), "pipeline|%d|%d", &x, &y) >= 1) {
       if (x >= 1 && x <= 4) g_pipeline_shift = x;
+      if (y >= 1 && y <= 4) g_pipeline_parts = y;
     } else if (sscanf(rest.c_str(), "%llu|%d|%d", &key, &x, &y) == 3) {
       g_level_tune[(uint64_t)key] = LevelTune{std::max(-3, std::min(x, 3)), std::max(0, std::min(y, 128))};
     }
@@ -1098,7 +1100,7 @@ static void tune_save() {
   for (const std::string& l : keep) fputs(l.c_str(), f);
   for (const auto& kv : g_level_tune)
     fprintf(f, "%s|%llu|%d|%d\n", g_tune_gpu.c_str(), (unsigned long long)kv.first, kv.second.shift, kv.second.gmax);
-  fprintf(f, "%s|pipeline|%d\n", g_tune_gpu.c_str(), g_pipeline_shift);
+  fprintf(f, "%s|pipeline|%d|%d\n", g_tune_gpu.c_str(), g_pipeline_shift, g_pipeline_parts);
   fclose(f);
 }
 static LevelTune level_tune(bool f64, int k, int64_t A) {
@@ -1108,6 +1110,11 @@ static LevelTune level_tune(bool f64, int k, int64_t A) {
   return it == g_level_tune.end() ? LevelTune{} : it->second;
 }
 
+// Slot 0 runs on the library's stream, slot 1 on the context's second stream, so
+// that the parts of a pipelined call overlap on the GPU (one part's latency-bound
+// first levels beside the other part's heavy ones).
+static inline cudaStream_t slot_stream(Context* cx, int slot) { return slot ? cx->stream2 : cx->stream; }
+
 // matrices: n_mats complex m x m matrices, U[out][in]; one for every sample
 // (n_mats == 1) or one per sample (n_mats == number of samples).
 // timing: 0 none; 1 an event pair around every sweep launch; 2 an event pair
@@ -1115,6 +1122,7 @@ static LevelTune level_tune(bool f64, int k, int64_t A) {
 static int gccb_prepare(Context* cx, const double* matrix, int n_mats, int m, Draws& D, int timing, GccbRun& R,
                         int slot = 0) {
   const int N = (int)D.L.size();
+  tune_load(cx->device);  // the tuned shapes of an earlier process, if any (once per process)
   R.slot = slot;
   DeviceBuffer* B = cx->gccb + 8 * slot;
   const int n = std::max(D.n, 1);
@@ -1236,9 +1244,9 @@ static int gccb_prepare(Context* cx, const double* matrix, int n_mats, int m, Dr
       if (lt.shift > 0) tps = std::min<int64_t>((int64_t)code0, tps << lt.shift);
       if (lt.shift < 0) tps = std::max<int64_t>(1, tps >> -lt.shift);
       // Each aligned group of G threads of a sample sums its minors inside the sweep:
-      // the largest G (up to a warp; up to a block of 128 for float-pair sweeps whose
-      // threads then fill whole blocks) that costs at most 2% of the sample's threads.
-      int G = ffl[k] ? 128 : 32;
+      // the largest G (up to a block of 128, when the launch's threads then fill
+      // whole blocks) that costs at most 2% of the sample's threads.
+      int G = 128;
       if (lt.gmax > 0) G = std::min(G, lt.gmax);
       auto ok = [&](int g) {
         if (!(tps >= g && (double)(tps / g * g) >= 0.98 * (double)tps)) return false;
@@ -1339,7 +1347,7 @@ static int gccb_prepare(Context* cx, const double* matrix, int n_mats, int m, Dr
   uint8_t* dmode[2] = {(uint8_t*)B[3].ptr, (uint8_t*)B[3].ptr + (size_t)A[1] * 32};
   longlong2* pool[2] = {(longlong2*)B[4].ptr, (longlong2*)B[4].ptr + max_pool};
   double2* partials = (double2*)B[5].ptr;
-  cudaStream_t s = cx->stream;
+  cudaStream_t s = slot_stream(cx, slot);
   cudaError_t e = cudaMemcpyAsync(d, h, arena, cudaMemcpyHostToDevice, s);
   if (e != cudaSuccess) return fail_cuda(e, "H2D sampler arena");
   longlong2* dUfx = (longlong2*)B[7].ptr;
@@ -1463,13 +1471,13 @@ static int gccb_prepare(Context* cx, const double* matrix, int n_mats, int m, Dr
 }
 
 static int gccb_launch(Context* cx, int slot = 0) {
-  cudaError_t e = cudaGraphLaunch(g_gccb_exec[slot], cx->stream);
+  cudaError_t e = cudaGraphLaunch(g_gccb_exec[slot], slot_stream(cx, slot));
   return e == cudaSuccess ? kOk : fail_cuda(e, "graph launch");
 }
 
 // Queues the copies of a run's samples and status into its slot's pinned buffer.
 static int gccb_queue_results(Context* cx, GccbRun& R) {
-  cudaStream_t s = cx->stream;
+  cudaStream_t s = slot_stream(cx, R.slot);
   char* h = (char*)g_gccb_pinned[R.slot];
   cudaError_t e = cudaMemcpyAsync(h, R.dT, (size_t)R.N * R.m, cudaMemcpyDeviceToHost, s);
   if (e != cudaSuccess) return fail_cuda(e, "D2H samples");
@@ -1500,7 +1508,7 @@ static int gccb_read_results(const GccbRun& R, int32_t* samples_out) {
 static int gccb_collect(Context* cx, GccbRun& R, int32_t* samples_out) {
   int st = gccb_queue_results(cx, R);
   if (st) return st;
-  cudaError_t e = cudaStreamSynchronize(cx->stream);
+  cudaError_t e = cudaStreamSynchronize(slot_stream(cx, R.slot));
   if (e != cudaSuccess) return fail_cuda(e, "sampler");
   return gccb_read_results(R, samples_out);
 }
@@ -1535,51 +1543,66 @@ static void keep_rows(Draws& D, int first, int count) {
 static int sample_slice_locked(const double* matrix, int m, const int32_t* input_state,
                                const double* particle_weights, int nw, MT19937& mt, int n_samples, int first,
                                int count, int32_t* samples) {
-  // Large batches run as two parts: the host replays and plans the second part
-  // while the GPU samples the first (separate buffers, pinned memory and graphs).
-  // The first part is count >> g_pipeline_shift (a quarter unless tuned), so that
-  // the GPU starts early and the host's work on the rest (~0.1 ms per 10^3
-  // samples) still ends before the GPU finishes the first part (~0.45 ms plus
-  // ~0.3 ms per 10^3 samples).
-  const int halves = (count >= kGccbPipelineMin) ? 2 : 1;
-  const int c0 = (halves == 2) ? (count >> g_pipeline_shift) : count;
-  const int cut[3] = {first, first + c0, first + count};
-  GccbRun R[2];
-  bool launched[2] = {false, false};
+  // Large batches run as pipelined parts: while the GPU samples one part, the host
+  // replays and plans the next.  The first part is count >> g_pipeline_shift (an
+  // eighth unless tuned), so that the GPU starts early; the rest is cut into
+  // g_pipeline_parts nearly equal parts.  Parts alternate between the two slots
+  // (device buffers, pinned buffer, graph and stream each), so consecutive parts
+  // overlap on the GPU; a slot is reused once its previous part has finished,
+  // and that part's rows are read while the GPU works on the other slot.
+  std::vector<int> cut(1, first);
   Context* cx = nullptr;
   int st = kOk;
+  if (count >= kGccbPipelineMin) {
+    if (!(cx = context(&st))) return st;
+    tune_load(cx->device);  // the tuned parts of an earlier process, if any
+    const int c0 = count >> g_pipeline_shift, rest = count - c0;
+    for (int p = 0; p < g_pipeline_parts; ++p) cut.push_back(first + c0 + (int)((int64_t)rest * p / g_pipeline_parts));
+  }
+  cut.push_back(first + count);
+  const int parts = (int)cut.size() - 1;
+  GccbRun R[kGccbSlots];
+  int in_flight[kGccbSlots] = {-1, -1};  // the part each slot is running, or -1
+  // Waits for the slot's part and writes its rows (or, after an error, only waits).
+  auto retire = [&](int slot, bool read) -> int {
+    const int p = in_flight[slot];
+    if (p < 0) return kOk;
+    in_flight[slot] = -1;
+    const cudaError_t e = cudaStreamSynchronize(slot_stream(cx, slot));
+    if (e != cudaSuccess) return fail_cuda(e, "sampler");
+    return read ? gccb_read_results(R[slot], samples + (size_t)(cut[p] - first) * m) : kOk;
+  };
   int done = 0;  // stream samples replayed so far
-  for (int h = 0; h < halves; ++h) {
+  for (int p = 0; p < parts && !st; ++p) {
+    const int slot = p % kGccbSlots;
+    if ((st = retire(slot, true))) break;
     Draws D;
-    const int upto = (h + 1 == halves) ? n_samples : cut[h + 1];  // the last half replays the stream's tail
-    st = predraw(input_state, m, particle_weights, nw, mt, upto - done, D);
-    if (st) return st;
+    const int upto = (p + 1 == parts) ? n_samples : cut[p + 1];  // the last part replays the stream's tail
+    if ((st = predraw(input_state, m, particle_weights, nw, mt, upto - done, D))) break;
     if (D.n > kMaxMinorDigits) {
       set_error("the batched sampler supports at most 32 input particles");
-      return kErrLimit;
+      st = kErrLimit;
+      break;
     }
-    keep_rows(D, cut[h] - done, cut[h + 1] - cut[h]);
+    keep_rows(D, cut[p] - done, cut[p + 1] - cut[p]);
     done = upto;
-    if (!std::any_of(D.L.begin(), D.L.end(), [](int32_t l) { return l > 0; })) continue;
-    if (!cx && !(cx = context(&st))) return st;
-    if ((st = gccb_prepare(cx, matrix, 1, m, D, 0, R[h], h))) return st;
-    if ((st = gccb_launch(cx, h))) return st;
-    if ((st = gccb_queue_results(cx, R[h]))) return st;
-    launched[h] = true;
-  }
-  if (cx) {
-    cudaError_t e = cudaStreamSynchronize(cx->stream);
-    if (e != cudaSuccess) return fail_cuda(e, "sampler");
-  }
-  for (int h = 0; h < halves && count > 0; ++h) {  // every row is written: sampled, or empty
-    int32_t* rows = samples + (size_t)(cut[h] - first) * m;
-    if (launched[h]) {
-      if ((st = gccb_read_results(R[h], rows))) return st;
-    } else {
-      memset(rows, 0, sizeof(int32_t) * (size_t)(cut[h + 1] - cut[h]) * m);
+    if (!std::any_of(D.L.begin(), D.L.end(), [](int32_t l) { return l > 0; })) {  // every row empty
+      memset(samples + (size_t)(cut[p] - first) * m, 0, sizeof(int32_t) * (size_t)(cut[p + 1] - cut[p]) * m);
+      continue;
     }
+    if (!cx && !(cx = context(&st))) break;
+    in_flight[slot] = p;  // from here on the slot's stream may hold work of this part
+    if ((st = gccb_prepare(cx, matrix, 1, m, D, 0, R[slot], slot))) break;
+    if ((st = gccb_launch(cx, slot))) break;
+    if ((st = gccb_queue_results(cx, R[slot]))) break;
   }
-  return kOk;
+  // The remaining parts in order of their slots; after an error every slot is
+  // still drained, so that no copy into a pinned buffer outlives the call.
+  for (int slot = 0; slot < kGccbSlots; ++slot) {
+    const int rs = retire(slot, st == kOk);
+    if (!st) st = rs;
+  }
+  return st;
 }
 
 // Samples with at least k particles, k = 0..Lmax.
@@ -1660,12 +1683,13 @@ static int tune_step(Context* cx, const double* matrix, int m, Draws& D, int rep
 
 // The tuner: times the levels under power-of-two shifts of the split, then under
 // caps of the group size G, keeps each level's fastest shape if the whole step
-// gets faster, then times the pipelined first part's size on end-to-end calls.
-// report[0..6]: step ms with the heuristic shapes and with the tuned ones, levels
-// whose shape changed, the pipeline shift, end-to-end ms with the quarter split
-// and with the tuned split (0 when the call is below the pipelining size), and the
-// sum over levels of each level's own time (sweep to end of finalize, heuristic
-// shapes): the step minus it is the graph's time between levels.
+// gets faster, then times the pipelined parts on end-to-end calls.
+// report[0..7]: step ms with the heuristic shapes and with the tuned ones, levels
+// whose shape changed, the pipeline shift, end-to-end ms with the default parts
+// (shift 3, two more parts) and with the tuned ones (0 when the call is below the
+// pipelining size), the sum over levels of each level's own time (sweep to end of
+// finalize, heuristic shapes: the step minus it is the graph's time between
+// levels), and the number of parts after the first.
 static int gccb_autotune_locked(Context* cx, const double* matrix, int m, const int32_t* input_state,
                                 const double* weights, int nw, const MT19937& mt0, int n_samples, int reps,
                                 double* report) {
@@ -1731,14 +1755,21 @@ static int gccb_autotune_locked(Context* cx, const double* matrix, int m, const 
   report[0] = step0;
   report[1] = keep ? step1 : step0;
   report[2] = changed;
-  // The pipelined split, on end-to-end calls of the same stream.
+  // The pipelined parts, on end-to-end calls of the same stream: the first part's
+  // shift and the number of parts after it, the default (3, 2) first as the reference.
   report[3] = g_pipeline_shift;
+  report[7] = g_pipeline_parts;
   if (n_samples >= kGccbPipelineMin) {
     std::vector<int32_t> out((size_t)n_samples * m);
     double best_e2e = 1e30;
-    int best_shift = g_pipeline_shift;
-    for (int sh : {2, 1, 3, 4}) {  // the quarter split first: the reference point
-      g_pipeline_shift = sh;
+    int best_shift = 3, best_parts = 2;
+    std::vector<std::pair<int, int>> cand(1, std::make_pair(3, 2));
+    for (int sh = 1; sh <= 4; ++sh)
+      for (int np = 1; np <= 4; ++np)
+        if (sh != 3 || np != 2) cand.push_back(std::make_pair(sh, np));
+    for (size_t c = 0; c < cand.size() && !st; ++c) {
+      g_pipeline_shift = cand[c].first;
+      g_pipeline_parts = cand[c].second;
       double t_min = 1e30;
       for (int it = 0; it <= reps; ++it) {
         MT19937 t = mt0;
@@ -1749,14 +1780,17 @@ static int gccb_autotune_locked(Context* cx, const double* matrix, int m, const 
         if (it > 0) t_min = std::min(t_min, dt);
       }
       if (st) break;
-      if (sh == 2) report[4] = t_min;
-      if (t_min < 0.97 * best_e2e || (sh == 2 && t_min < best_e2e)) {
+      if (c == 0) report[4] = t_min;
+      if (c == 0 || t_min < 0.97 * best_e2e) {
         best_e2e = t_min;
-        best_shift = sh;
+        best_shift = cand[c].first;
+        best_parts = cand[c].second;
       }
     }
     g_pipeline_shift = best_shift;
+    g_pipeline_parts = best_parts;
     report[3] = best_shift;
+    report[7] = best_parts;
     report[5] = best_e2e;
     if (st) return st;
   }

@@ -96,7 +96,7 @@ enum Status : int {
 void set_error(const std::string& msg);
 int fail_cuda(cudaError_t e, const char* where);
 
-// Per-process device context: one non-blocking stream, SM count, grow-only buffers.
+// Per-process device context: non-blocking streams, SM count, grow-only buffers.
 struct DeviceBuffer {
   void* ptr = nullptr;
   size_t bytes = 0;
@@ -106,6 +106,7 @@ struct Context {
   int device = 0;
   int sm_count = 0;
   cudaStream_t stream = nullptr;
+  cudaStream_t stream2 = nullptr;  // the sampler's second pipelined slot (boss_gccb.cu)
   DeviceBuffer plans, pool, partials, out, counter, index, misc, gpart, pperm;
   DeviceBuffer gccb[16];
   DeviceBuffer dist[4];

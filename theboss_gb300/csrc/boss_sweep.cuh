@@ -65,9 +65,10 @@ struct SweepProblem {
                      // im hi, im lo, each factor in its own scale), then nf int32 exponent biases
   double scale;      // final real scale
   int32_t fixed_digit;  // gradients, all-minors: a binary digit held at r = 0 (Glynn halving) adds a weight-1 row
-  int32_t group;     // all-minors: each aligned group of `group` threads (1, 2, 4, .., 32; float pairs up to 128) sums its
-                     // minors, so the partials are (n_threads / group) x nd; n_threads and
-                     // thread_begin are multiples of it, and every sweep of the launch has the same
+  int32_t group;     // all-minors: each aligned group of `group` threads (1, 2, 4, .., 128; above 32 only when the
+                     // launch's threads fill whole blocks) sums its minors, so the partials are
+                     // (n_threads / group) x nd; n_threads and thread_begin are multiples of it, and
+                     // every sweep of the launch has the same
   uint8_t mult[kMaxDigits];
 };
 
@@ -383,6 +384,20 @@ __device__ __forceinline__ void thread_range(const SweepProblem& P, int64_t q, i
   const int64_t per = P.n_codes / P.n_threads, rem = P.n_codes % P.n_threads;
   a = q * per + (q < rem ? q : rem);
   len = per + (q < rem ? 1 : 0);
+}
+
+// The same split in whole units of 2^c codes (lengths differ by at most one
+// unit; the last unit of the sweep may be short).  Every range then starts at a
+// multiple of 2^c, so at every step the lanes of a warp flip the same binary
+// digit whenever that digit is below c: their per-digit updates touch the same
+// row, and rows laid out by lane are read and written in whole lines.
+__device__ __forceinline__ void thread_range_aligned(const SweepProblem& P, int64_t q, int c, int64_t& a,
+                                                     int64_t& len) {
+  const int64_t units = (P.n_codes + (1ll << c) - 1) >> c;
+  const int64_t per = units / P.n_threads, rem = units % P.n_threads;
+  a = (q * per + (q < rem ? q : rem)) << c;
+  const int64_t want = (per + (q < rem ? 1 : 0)) << c;
+  len = (a >= P.n_codes) ? 0 : (a + want <= P.n_codes ? want : P.n_codes - a);
 }
 
 __device__ __forceinline__ int find_problem(const SweepProblem* __restrict__ probs, int n, int64_t gt) {

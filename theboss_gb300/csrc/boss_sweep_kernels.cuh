@@ -171,7 +171,36 @@ __global__ void __launch_bounds__(128) minors_sweep_kernel(const SweepProblem* _
   double2* M = minors_smem + threadIdx.x;
   minors_walk<NF, 128>(P, pool + P.mat_off, pool + P.base_off, q, M);
   const int G = P.group;
-  if (G > 1) {  // each aligned group of G lanes (one sweep's threads) sums its minors:
+  if (G > 32) {
+    // Groups of 64 or 128 threads (the planner allows them only when the launch's
+    // threads fill whole blocks, so no thread of this block has exited): each warp
+    // sums its lanes' minors (lane l: digit l, nd <= 32) into the warp's first
+    // column of row l, then thread t of each group adds up digit t over its warps,
+    // both in a fixed order.
+    const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
+    __syncwarp();
+    if (lane < nd) {
+      const double2* row = minors_smem + lane * 128 + wp * 32;
+      double sx = 0.0, sy = 0.0;
+      for (int i = 0; i < 32; ++i) {
+        const double2 v = row[(i + lane) & 31];  // staggered: fewer bank conflicts
+        sx += v.x;
+        sy += v.y;
+      }
+      minors_smem[lane * 128 + wp * 32] = make_double2(sx, sy);
+    }
+    __syncthreads();
+    const int tin = threadIdx.x & (G - 1), w0 = (threadIdx.x - tin) >> 5;
+    if (tin < nd) {
+      double sx = 0.0, sy = 0.0;
+      for (int wv = 0; wv < (G >> 5); ++wv) {
+        const double2 v = minors_smem[tin * 128 + (w0 + wv) * 32];
+        sx += v.x;
+        sy += v.y;
+      }
+      partials[P.part_off + (q / G) * nd + tin] = make_double2(sx, sy);
+    }
+  } else if (G > 1) {  // each aligned group of G lanes (one sweep's threads) sums its minors:
                 // lane l of the group adds up digits l, l + G, .. over the group, in a fixed order
     const int lane = threadIdx.x & 31;
     const int64_t warp0 = gt - lane;  // lanes past the launch's last thread have exited
@@ -581,6 +610,11 @@ __global__ void __launch_bounds__(128, kFFPermMinBlocks<NF>) perm_sweep_ff_kerne
 // Per-thread G lives in global scratch: (nd + fixed) x NF complex, row = digit,
 // lane-interleaved within each group of 32 threads; each warp sums its lanes'
 // rows at the end and leaves one group partial.
+// Gradient ranges start at multiples of 2^kGradAlign codes (thread_range_aligned):
+// the six lowest binary digits, which make 98% of the flips, then flip in step
+// across a warp and their rows are updated in whole lines.
+constexpr int kGradAlign = 6;
+
 template <int NF>
 __global__ void __launch_bounds__(64) grad_sweep_kernel(const SweepProblem* __restrict__ probs, int n_probs,
                                                         const longlong2* __restrict__ pool, int64_t total_threads,
@@ -599,7 +633,7 @@ __global__ void __launch_bounds__(64) grad_sweep_kernel(const SweepProblem* __re
   uint64_t touched = 0;  // rows of G written so far (the first write of a row stores, later ones add)
   double totr = 0.0, toti = 0.0;  // weighted permanent over finished segments
   int64_t a, len;
-  thread_range(P, q, a, len);
+  thread_range_aligned(P, q, P.nb < kGradAlign ? P.nb : kGradAlign, a, len);
   const longlong2* D = pool + P.mat_off;
   const longlong2* base = pool + P.base_off;
   const int bias = 1023 + 63 - P.fx;
