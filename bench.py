@@ -472,14 +472,14 @@ def strategies_section(seed):
     (10^6 samples over the 12,376 outcomes of n=6, m=12)."""
     from theboss_gb300 import _native
     from theboss_gb300.approximation_strategies import LossyStateApproximationSimulationStrategy
-    from theboss_gb300.permanent_calculators import RyserPermanentCalculator
+    from theboss_gb300.permanent_calculators import GlynnGrayPermanentCalculator, RyserPermanentCalculator
     from theboss_gb300.simulation_strategies import (GeneralizedCliffordsSimulationStrategy,
                                                      LossyNetworksGeneralizedCliffordsSimulationStrategy)
     from theboss_gb300.utilities import haar_unitary, possible_states_array
 
     out = {}
     U = haar_unitary(16, seed + 8)
-    strat = GeneralizedCliffordsSimulationStrategy(RyserPermanentCalculator(U))
+    strat = GeneralizedCliffordsSimulationStrategy(GlynnGrayPermanentCalculator(U))
     np.random.seed(seed)
     strat.simulate([1] * 8 + [0] * 8, 50)  # warm-up
     np.random.seed(seed)

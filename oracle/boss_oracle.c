@@ -271,6 +271,30 @@ int oracle_perm_classic(const double* U, int m, const int* S, const int* T, int 
 }
 
 /* ---------------------------------------------------------------------------
+ * A batch of permanents: row k of S and of T (len modes each) with the
+ * calculator named by variant (0 Ryser, 1 Chin-Huh, 2 Glynn, 3 classic), the
+ * values of the functions above, one call for a whole sampler stream.
+ * ------------------------------------------------------------------------- */
+int oracle_perm_batch(const double* U, int m, const int* S, const int* T, int len, int count, int variant,
+                      double* out) {
+  for (int k = 0; k < count; ++k) {
+    const int* s = S + (size_t)k * len;
+    const int* t = T + (size_t)k * len;
+    double* o = out + 2 * (size_t)k;
+    int rc;
+    switch (variant) {
+      case 0: rc = oracle_perm_ryser(U, m, s, t, len, o); break;
+      case 1: rc = oracle_perm_chin_huh(U, m, s, t, len, o); break;
+      case 2: rc = oracle_perm_glynn(U, m, s, t, len, o); break;
+      case 3: rc = oracle_perm_classic(U, m, s, t, len, o); break;
+      default: return 4;
+    }
+    if (rc) return rc;
+  }
+  return 0;
+}
+
+/* ---------------------------------------------------------------------------
  * All-minors ("submatrices") permanents, Ryser flavour:
  * bs_cc_ryser_submatrices_permanent_calculator.py:73-119 driven by
  * bs_submatrices_permanent_calculator_base.py:150-189.

@@ -71,6 +71,8 @@ def lib():
         L.oracle_gccb_run.argtypes = [
             dp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ip, ip, dp, ctypes.POINTER(ctypes.c_int64)
         ]
+        L.oracle_perm_batch.restype = ctypes.c_int
+        L.oracle_perm_batch.argtypes = [dp, ctypes.c_int, ip, ip, ctypes.c_int, ctypes.c_int, ctypes.c_int, dp]
         L.oracle_guan_sequence.restype = ctypes.c_long
         L.oracle_guan_sequence.argtypes = [ip, ctypes.c_int, ip, ip, ctypes.c_long]
         _lib = L
@@ -115,6 +117,24 @@ def perm(U, S: Sequence[int], T: Sequence[int], variant: int = RYSER) -> complex
     if rc:
         raise ValueError(f"oracle rc={rc}")
     return complex(out[0], out[1])
+
+
+def perm_batch(U, S: np.ndarray, T: np.ndarray, variant: int = RYSER) -> np.ndarray:
+    """perm() of every row pair of the occupation arrays S and T (count x len):
+    the same values, one call (oracle_perm_batch)."""
+    U = _mat(U)
+    S = np.ascontiguousarray(S, dtype=np.int32)
+    T = np.ascontiguousarray(T, dtype=np.int32)
+    if S.shape != T.shape:
+        raise AttributeError("input and output state lengths differ")
+    count, n = S.shape
+    out = np.zeros(2 * count)
+    rc = lib().oracle_perm_batch(_dp(U), U.shape[0], _ip(S), _ip(T), n, count, variant, _dp(out))
+    if rc == 1:
+        raise AttributeError("size mismatch")
+    if rc:
+        raise ValueError(f"oracle rc={rc}")
+    return out.view(np.complex128)
 
 
 def perm_dd(U, S, T) -> Tuple[complex, complex]:
