@@ -94,6 +94,36 @@ struct MT19937 {
   }
 };
 
+// The generator's position in a local variable for the length of a tight loop:
+// the compiler keeps it in a register, where the member would be reloaded after
+// every store through the byte arrays the loop fills (they may alias it).  The
+// same draws as MT19937's own functions; the position is written back at the end.
+struct MTReader {
+  MT19937& mt;
+  int pos;
+  explicit MTReader(MT19937& g) : mt(g), pos(g.pos) {}
+  ~MTReader() { mt.pos = pos; }
+  inline uint32_t next32() {
+    if (pos >= 624) {
+      mt.twist();
+      pos = 0;
+    }
+    return mt.out[pos++];
+  }
+  inline double next_double() {
+    const uint32_t a = next32() >> 5, b = next32() >> 6;
+    return (a * 67108864.0 + b) / 9007199254740992.0;
+  }
+  inline uint32_t bounded(uint32_t n, uint32_t mask) {
+    const uint32_t rng = n - 1;
+    if (rng == 0) return 0;
+    uint32_t v;
+    while ((v = (next32() & mask)) > rng) {
+    }
+    return v;
+  }
+};
+
 static inline uint32_t mask_for(uint32_t n) {
   uint32_t m = n - 1;
   m |= m >> 1;
@@ -185,10 +215,11 @@ static int predraw(const int32_t* input_state, int m, const double* weights, int
   D.modes.clear();
   uint32_t masks[257];
   for (int r = 1; r <= n; ++r) masks[r] = mask_for((uint32_t)r);
+  MTReader rd(mt);
   for (int s = 0; s < n_samples; ++s) {
     int l = n;
     if (weights) {  // generalized_cliffords_b_uniform_losses_simulation_strategy.py:67-85
-      const double thr = mt.next_double();
+      const double thr = rd.next_double();
       double acc = 0.0;
       l = 0;
       for (int i = 0; i < n_weights; ++i) {
@@ -206,9 +237,9 @@ static int predraw(const int32_t* input_state, int m, const double* weights, int
     uint8_t* is = &D.idx[(size_t)s * n];
     double* us = &D.u[(size_t)s * n];
     for (int k = 0; k < l; ++k) {  // generalized_cliffords_b_simulation_strategy.py:97-110
-      is[k] = (uint8_t)mt.bounded((uint32_t)remaining, masks[remaining]);
+      is[k] = (uint8_t)rd.bounded((uint32_t)remaining, masks[remaining]);
       --remaining;
-      us[k] = mt.next_double();
+      us[k] = rd.next_double();
     }
   }
   return kOk;
@@ -235,7 +266,9 @@ struct FinalizeArgs {
   const longlong2* Ufx;   // m x m, U * 2^fx rounded
   const float4* Uff;      // float-pair pmf: m x m transposed, Uff[i * m + o] = U[o][i] as float pairs
                           // (re hi, re lo, im hi, im lo)
-  const double2* Ud;      // FP64 pmf: m x m transposed, Ud[i * m + o] = U[o][i]
+  const int4* Ulimb;      // FP64 pmf: m x m transposed, U[o][i] * 2^lfx rounded, as 27-bit limbs
+                          // (re lo, re hi, im lo, im hi; lo in [0, 2^27), value = hi 2^27 + lo)
+  int lfx;                // |U| * 2^lfx < 2^53
   const float* Uabs;      // m x m transposed, |Re U[o][i]| + |Im U[o][i]| (the pmf error bound)
   uint8_t* S;             // [sample][m] current input occupations
   uint8_t* T;             // [sample][m] output occupations
@@ -337,7 +370,7 @@ __device__ __forceinline__ int pop_particle(uint32_t* rem, int r) {
 // kF64: the minors, the Laplace step, |.|^2 and the pmf are FP64 (the default);
 // otherwise float pairs on the FP32 pipe (the opt-in float-pair arithmetic).
 template <bool kF64>
-__global__ void __launch_bounds__(kFinWarps * 32) gccb_finalize_kernel(FinalizeArgs a) {
+__global__ void __launch_bounds__(kFinWarps * 32, 8) gccb_finalize_kernel(FinalizeArgs a) {
   __shared__ double2 sub_s[kFinWarps][32];
   __shared__ float4 subf_s[kFinWarps][32];
   __shared__ uint8_t dm_s[kFinWarps][32];
@@ -345,6 +378,8 @@ __global__ void __launch_bounds__(kFinWarps * 32) gccb_finalize_kernel(FinalizeA
   __shared__ uint8_t fm_s[kFinWarps][32];
   __shared__ double pmf_s[kFinWarps][256];
   __shared__ float cn_s[kFinWarps][32];  // |c_d|_1 2^-Ec (the pmf error bound)
+  __shared__ int4 climb_s[kFinWarps][32];  // FP64 pmf: the minors as 27-bit limbs (re lo, re hi, im lo, im hi)
+  __shared__ int2 cnb_s[kFinWarps][32];    // and -Im as limbs
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int j = blockIdx.x * kFinWarps + w;
   if (j >= a.A) return;
@@ -435,11 +470,39 @@ __global__ void __launch_bounds__(kFinWarps * 32) gccb_finalize_kernel(FinalizeA
       if (cost_groups <= cost_stripes) {
         const int g = lane / nd, d = lane - g * nd;
         double sx = 0.0, sy = 0.0;
-        if (g < gc) {  // gc <= parts: every group has a first row
+        if (g < gc && parts >= 8 * gc) {
+          // long sums (the top levels, where one warp has the SM's FP64 unit to
+          // itself): four interleaved chains, rows g + (4 i + c) gc in chain c,
+          // combined in a fixed order, a quarter of one chain's latency
+          double x0 = 0.0, y0 = 0.0, x1 = 0.0, y1 = 0.0, x2 = 0.0, y2 = 0.0, x3 = 0.0, y3 = 0.0;
+          int64_t q = g;
+#pragma unroll 4
+          for (; q + 3 * gc < parts; q += 4 * gc) {
+            const double2 v0 = a.partials[P.part_off + q * nd + d];
+            const double2 v1 = a.partials[P.part_off + (q + gc) * nd + d];
+            const double2 v2 = a.partials[P.part_off + (q + 2 * gc) * nd + d];
+            const double2 v3 = a.partials[P.part_off + (q + 3 * gc) * nd + d];
+            x0 += v0.x;
+            y0 += v0.y;
+            x1 += v1.x;
+            y1 += v1.y;
+            x2 += v2.x;
+            y2 += v2.y;
+            x3 += v3.x;
+            y3 += v3.y;
+          }
+          for (; q < parts; q += gc) {
+            const double2 v = a.partials[P.part_off + q * nd + d];
+            x0 += v.x;
+            y0 += v.y;
+          }
+          sx = (x0 + x1) + (x2 + x3);
+          sy = (y0 + y1) + (y2 + y3);
+        } else if (g < gc) {  // gc <= parts: every group has a first row
           const double2 v0 = a.partials[P.part_off + (int64_t)g * nd + d];
           sx = v0.x;
           sy = v0.y;
-#pragma unroll 4
+#pragma unroll 8
           for (int64_t q = g + gc; q < parts; q += gc) {
             const double2 v = a.partials[P.part_off + q * nd + d];
             sx += v.x;
@@ -460,17 +523,29 @@ __global__ void __launch_bounds__(kFinWarps * 32) gccb_finalize_kernel(FinalizeA
         }
         __syncwarp();
         if (lane < nd) sub_s[w][lane] = make_double2(sx, sy);
-      } else {  // many partials: the lanes stripe over them, then a fixed-order warp sum
-        for (int d = 0; d < nd; ++d) {
-          double sx = 0.0, sy = 0.0;
+      } else {  // many partials: the lanes stripe over them, then a fixed-order warp
+                // sum; two digits at a time (independent chains in flight)
+        for (int d = 0; d < nd; d += 2) {
+          const int d1 = (d + 1 < nd) ? d + 1 : d;  // an odd last digit is summed twice, stored once
+          double sx = 0.0, sy = 0.0, tx = 0.0, ty = 0.0;
+#pragma unroll 4
           for (int64_t q = lane; q < parts; q += 32) {
             const double2 v = a.partials[P.part_off + q * nd + d];
+            const double2 u = a.partials[P.part_off + q * nd + d1];
             sx += v.x;
             sy += v.y;
+            tx += u.x;
+            ty += u.y;
           }
-          sx = warp_sum(sx);
-          sy = warp_sum(sy);
+#pragma unroll
+          for (int o = 16; o > 0; o >>= 1) {  // warp_sum's butterfly, the four sums interleaved
+            sx += __shfl_xor_sync(0xffffffffu, sx, o);
+            sy += __shfl_xor_sync(0xffffffffu, sy, o);
+            tx += __shfl_xor_sync(0xffffffffu, tx, o);
+            ty += __shfl_xor_sync(0xffffffffu, ty, o);
+          }
           if (lane == d) sub_s[w][d] = make_double2(sx * P.scale, sy * P.scale);
+          if (lane == d1 && d1 != d) sub_s[w][d1] = make_double2(tx * P.scale, ty * P.scale);
         }
       }
     }
@@ -507,75 +582,115 @@ __global__ void __launch_bounds__(kFinWarps * 32) gccb_finalize_kernel(FinalizeA
   // and counted in err[1]; outside it the fast path's decision is the exact one.
   if constexpr (kF64) {
     // ---- FP64 pmf (the default arithmetic) ----
-    const double2* UT = a.Ud + (size_t)j * a.mstride;
+    // The Laplace sums are exact: the minors (scaled by 2^(52 - Ec), Ec their
+    // largest 1-norm's exponent) and U (scaled by 2^lfx) are rounded once to
+    // integers below 2^53, split into 27-bit limbs (x = x1 2^27 + x0, x0 >= 0),
+    // and every limb product (below 2^54) is added into three 64-bit sums per
+    // component (the 2^54, 2^27 and 2^0 parts; at most 4 nd <= 128 products each,
+    // no overflow).  Those sums are combined in 128 bits and rounded once to a
+    // double.  The products run on the integer pipe (a 32 x 32 -> 64-bit
+    // multiply-add each, 16 per digit and output), which GB300 issues far faster
+    // than its FP64 pipe; only |.|^2 (2 DFMA per output) stays on the FP64 pipe.
+    const int4* UL = a.Ulimb + (size_t)j * a.mstride;
     const float* UA = a.Uabs + (size_t)j * a.mstride;
     double* pmf = pmf_s[w];
     // the bound's scale: 2^-Ec, 2^Ec <= max_d |c_d|_1 < 2^(Ec + 1)
     double c1 = 0.0;
+    double2 cv = make_double2(0.0, 0.0);
     if (lane < nd) {
-      const double2 c = sub_s[w][lane];
-      c1 = fabs(c.x) + fabs(c.y);
+      cv = sub_s[w][lane];
+      c1 = fabs(cv.x) + fabs(cv.y);
     }
     const unsigned long long cb = warp_max_u64((unsigned long long)__double_as_longlong(c1));
     const int Ec = (int)(cb >> 52) - 1023;  // non-negative doubles order as integers
     const double sc = (cb >> 52) ? __longlong_as_double((long long)(1023 - Ec) << 52) : 1.0;  // 2^-Ec
-    if (lane < nd) cn_s[w][lane] = __double2float_ru(c1 * sc);  // in [0, 2)
+    float cn = 0.0f;
+    if (lane < nd) {
+      cn = __double2float_ru(c1 * sc);  // in [0, 2)
+      cn_s[w][lane] = cn;
+      // c * 2^(52 - Ec) (exact: a power of two; every component < 2^53), rounded
+      const double s52 = sc * 4503599627370496.0;  // 2^52
+      const long long A = __double2ll_rn(cv.x * s52), B = __double2ll_rn(cv.y * s52);
+      const long long NB = -B;
+      climb_s[w][lane] = make_int4((int)(A & 0x7FFFFFF), (int)(A >> 27), (int)(B & 0x7FFFFFF), (int)(B >> 27));
+      cnb_s[w][lane] = make_int2((int)(NB & 0x7FFFFFF), (int)(NB >> 27));
+    }
+    const float csum = warp_sum_f(cn);  // sum_d |c_d|_1 2^-Ec
     __syncwarp();
-    const float eps2 = 2.0f * kMinorsErrF64;                          // eps_m * max|c| (scaled max < 2)
-    const float gam = (float)(nd + 2) * 2.220446e-16f;                // (nd + 2) 2^-52: the FMAs' rounding
-    float errsum = 0.0f;                                              // this lane's share of E * 2^-2Ec
+    // e_o in units of 2^Ec: the minors' error, the rounding of c (half a unit of
+    // 2^(Ec - 52) per component) and of U (half a unit of 2^-lfx) to integers, and
+    // the rounding of the exact sum to a double, each counted twice
+    const float ec_b = 2.0f * kMinorsErrF64 + 4.440892e-16f;  // times b_o: eps_m max|c| + 2 2^-52
+    const float ec_c = scale_pow2f(csum, 1 - a.lfx);            // 2^(1 - lfx) sum_d |c_d|_1
+    const float ec_a = 2.220446e-16f;                           // times a_o: 2 2^-53
+    const double pscale = ldexp(1.0, Ec - 52 - a.lfx);         // the sums' unit
+    float errsum = 0.0f;                                        // this lane's share of E * 2^-2Ec
     for (int o = lane; o < full; o += 32) {
-      double pr = 0.0, pi = 0.0;
+      long long r2 = 0, r1 = 0, r0 = 0, i2 = 0, i1 = 0, i0 = 0;
       float ao = 0.0f, bo = 0.0f;
-#pragma unroll 4  // independent gathers in flight
+#pragma unroll 8  // independent gathers in flight
       for (int d = 0; d < nd; ++d) {
-        const double2 c = sub_s[w][d];
+        const int4 c = climb_s[w][d];  // a0 a1 b0 b1
+        const int2 nb = cnb_s[w][d];   // (-b)0 (-b)1
         const int e = dm_s[w][d] * m + o;
-        const double2 u = UT[e];
+        const int4 u = UL[e];          // x0 x1 y0 y1
         const float ua = UA[e];
-        pr = fma(c.x, u.x, pr);
-        pr = fma(-c.y, u.y, pr);
-        pi = fma(c.x, u.y, pi);
-        pi = fma(c.y, u.x, pi);
+        r2 += (long long)c.y * u.y + (long long)nb.y * u.w;
+        r1 += (long long)c.y * u.x + (long long)c.x * u.y + (long long)nb.y * u.z + (long long)nb.x * u.w;
+        r0 += (long long)c.x * u.x + (long long)nb.x * u.z;
+        i2 += (long long)c.y * u.w + (long long)c.w * u.y;
+        i1 += (long long)c.y * u.z + (long long)c.x * u.w + (long long)c.w * u.x + (long long)c.z * u.y;
+        i0 += (long long)c.x * u.z + (long long)c.z * u.x;
         ao = fmaf(cn_s[w][d], ua, ao);
         bo += ua;
       }
+      const double pr = (double)(((__int128)r2 << 54) + ((__int128)r1 << 27) + r0) * pscale;
+      const double pi = (double)(((__int128)i2 << 54) + ((__int128)i1 << 27) + i0) * pscale;
       pmf[o] = fma(pr, pr, pi * pi);
-      const float eo = eps2 * bo + gam * ao;
-      errsum += eo * (2.0f * ao + eo);
+      const float eo = ec_b * bo + ec_c + ec_a * ao;
+      errsum += eo * (2.0f * ao + eo) + 4.440892e-16f * ao * ao;  // + |.|^2's two roundings
     }
     if (m > full) {
       const int r = m - full;
       int s = 1;  // lanes per remaining output (a power of two, r * s <= 32)
       while (r * (s << 1) <= 32) s <<= 1;
       const int oi = lane / s, c0 = lane & (s - 1);
-      double pr = 0.0, pi = 0.0;
+      long long r2 = 0, r1 = 0, r0 = 0, i2 = 0, i1 = 0, i0 = 0;
       float ao = 0.0f, bo = 0.0f;
       if (oi < r) {
 #pragma unroll 4
         for (int d = c0; d < nd; d += s) {
-          const double2 c = sub_s[w][d];
+          const int4 c = climb_s[w][d];
+          const int2 nb = cnb_s[w][d];
           const int e = dm_s[w][d] * m + full + oi;
-          const double2 u = UT[e];
+          const int4 u = UL[e];
           const float ua = UA[e];
-          pr = fma(c.x, u.x, pr);
-          pr = fma(-c.y, u.y, pr);
-          pi = fma(c.x, u.y, pi);
-          pi = fma(c.y, u.x, pi);
+          r2 += (long long)c.y * u.y + (long long)nb.y * u.w;
+          r1 += (long long)c.y * u.x + (long long)c.x * u.y + (long long)nb.y * u.z + (long long)nb.x * u.w;
+          r0 += (long long)c.x * u.x + (long long)nb.x * u.z;
+          i2 += (long long)c.y * u.w + (long long)c.w * u.y;
+          i1 += (long long)c.y * u.z + (long long)c.x * u.w + (long long)c.w * u.x + (long long)c.z * u.y;
+          i0 += (long long)c.x * u.z + (long long)c.z * u.x;
           ao = fmaf(cn_s[w][d], ua, ao);
           bo += ua;
         }
       }
-      for (int off = s >> 1; off > 0; off >>= 1) {  // fixed butterfly order over the output's lanes
-        pr += __shfl_xor_sync(0xffffffffu, pr, off);
-        pi += __shfl_xor_sync(0xffffffffu, pi, off);
+      for (int off = s >> 1; off > 0; off >>= 1) {  // the output's lanes: exact integer sums
+        r2 += __shfl_xor_sync(0xffffffffu, r2, off);
+        r1 += __shfl_xor_sync(0xffffffffu, r1, off);
+        r0 += __shfl_xor_sync(0xffffffffu, r0, off);
+        i2 += __shfl_xor_sync(0xffffffffu, i2, off);
+        i1 += __shfl_xor_sync(0xffffffffu, i1, off);
+        i0 += __shfl_xor_sync(0xffffffffu, i0, off);
         ao += __shfl_xor_sync(0xffffffffu, ao, off);
         bo += __shfl_xor_sync(0xffffffffu, bo, off);
       }
       if (oi < r && c0 == 0) {
+        const double pr = (double)(((__int128)r2 << 54) + ((__int128)r1 << 27) + r0) * pscale;
+        const double pi = (double)(((__int128)i2 << 54) + ((__int128)i1 << 27) + i0) * pscale;
         pmf[full + oi] = fma(pr, pr, pi * pi);
-        const float eo = eps2 * bo + (gam + 5.0f * 2.220446e-16f) * ao;  // + the butterfly's adds
-        errsum += eo * (2.0f * ao + eo);
+        const float eo = ec_b * bo + ec_c + ec_a * ao;
+        errsum += eo * (2.0f * ao + eo) + 4.440892e-16f * ao * ao;
       }
     }
     const float E = warp_sum_f(errsum) * 1.01f;  // 1.01: the float sums' own rounding (< 2^-18)
@@ -868,7 +983,7 @@ __global__ void __launch_bounds__(kFinWarps * 32) gccb_finalize_kernel(FinalizeA
   // rows: -2 U[out][in] for the sweep's digits; base sums: sum_i S_i U[out][i]
   // over every input mode (all signs +1 at r = 0), exact in fixed point
   longlong2* D = a.pool_next + ls.pool_off;
-  #pragma unroll 4  // independent gathers in flight
+  #pragma unroll 8  // independent gathers in flight
   for (int e = lane; e < nds * nf; e += 32) {
     const int d = e / nf, f = e - d * nf;
     const longlong2 u = Ufxs[(size_t)fm_s[w][f] * m + dm_s[w][d]];
@@ -884,7 +999,7 @@ __global__ void __launch_bounds__(kFinWarps * 32) gccb_finalize_kernel(FinalizeA
   for (int f = lane; f < nf; f += 32) {
     long long bx = 0, by = 0;
     unsigned long long ax = 0, ay = 0;
-    #pragma unroll 4  // independent gathers in flight
+    #pragma unroll 8  // independent gathers in flight
     for (int d = 0; d < nd; ++d) {
       const longlong2 u = Ufxs[(size_t)fm_s[w][f] * m + dm_s[w][d]];
       bx += (long long)mult_s[w][d] * u.x;
@@ -904,7 +1019,7 @@ __global__ void __launch_bounds__(kFinWarps * 32) gccb_finalize_kernel(FinalizeA
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) esum += __shfl_xor_sync(0xffffffffu, esum, off);
     __syncwarp();  // fbias written by the other lanes
-    #pragma unroll 4  // independent gathers in flight
+    #pragma unroll 8  // independent gathers in flight
     for (int e = lane; e < (nb - held) * nf; e += 32) {
       const int d = e / nf, f = e - d * nf;
       const longlong2 u = Ufxs[(size_t)fm_s[w][f] * m + dm_s[w][d]];
@@ -969,6 +1084,7 @@ static int64_t g_gccb_near_ties = 0;
 // runs the other.
 constexpr int kGccbSlots = 2;
 constexpr int kGccbPipelineMin = 4096;  // samples from which a call runs as pipelined parts
+constexpr int kGccbMaxParts = 8;         // parts of a pipelined call at most
 static cudaGraphExec_t g_gccb_exec[kGccbSlots] = {nullptr, nullptr};
 static void* g_gccb_pinned[kGccbSlots] = {nullptr, nullptr};
 static size_t g_gccb_pinned_bytes[kGccbSlots] = {0, 0};
@@ -991,9 +1107,10 @@ static void destroy_events(GccbRun& R) {
 }
 
 // The Laplace step's coalesced layouts, out[mat][i][o] from U[mat][o][i]: as
-// doubles (FP64 pmf) or float pairs, and |Re| + |Im| in float (the pmf error bound).
+// 27-bit limbs of U * 2^lfx rounded (FP64 pmf) or as float pairs, and |Re| + |Im|
+// in float (the pmf error bound).
 __global__ void transpose_matrices_kernel(const double2* __restrict__ U, void* __restrict__ out,
-                                          float* __restrict__ uabs, int m, int64_t count, int f64) {
+                                          float* __restrict__ uabs, int m, int64_t count, int f64, int lfx) {
   const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (idx >= count) return;
   const int64_t mm = (int64_t)m * m;
@@ -1002,7 +1119,9 @@ __global__ void transpose_matrices_kernel(const double2* __restrict__ U, void* _
   const double2 v = U[idx];
   const int64_t t = mat * mm + (int64_t)i * m + o;
   if (f64) {
-    reinterpret_cast<double2*>(out)[t] = v;
+    const long long X = __double2ll_rn(ldexp(v.x, lfx)), Y = __double2ll_rn(ldexp(v.y, lfx));  // |.| < 2^53
+    reinterpret_cast<int4*>(out)[t] =
+        make_int4((int)(X & 0x7FFFFFF), (int)(X >> 27), (int)(Y & 0x7FFFFFF), (int)(Y >> 27));
   } else {
     float4 f;
     double_to_ff(v.x, f.x, f.y);
@@ -1033,8 +1152,8 @@ struct LevelTune {
 static std::map<uint64_t, LevelTune> g_level_tune;
 static bool g_tune_loaded = false;
 static std::string g_tune_gpu;
-static int g_pipeline_shift = 3;   // the pipelined first part is count >> shift (tuned: 1..4)
-static int g_pipeline_parts = 2;   // parts after the first one (tuned: 1..4)
+static int g_pipeline_shift = 4;   // the pipelined first part is count >> shift (tuned: 1..6)
+static int g_pipeline_growth = 2;  // each later part is this many times the one before (tuned: 1..4)
 static const LevelTune* g_tune_force = nullptr;  // while tuning: one shape for every level
 static std::vector<LevelTune> g_tune_force_level;  // while tuning: a shape per level (index k)
 
@@ -1074,8 +1193,8 @@ static void tune_load(int device) {
     unsigned long long key = 0;
     int x = 0, y = 0;
     if (sscanf(rest.c_str(), "pipeline|%d|%d", &x, &y) >= 1) {
-      if (x >= 1 && x <= 4) g_pipeline_shift = x;
-      if (y >= 1 && y <= 4) g_pipeline_parts = y;
+      if (x >= 1 && x <= 6) g_pipeline_shift = x;
+      if (y >= 1 && y <= 4) g_pipeline_growth = y;
     } else if (sscanf(rest.c_str(), "%llu|%d|%d", &key, &x, &y) == 3) {
       g_level_tune[(uint64_t)key] = LevelTune{std::max(-3, std::min(x, 3)), std::max(0, std::min(y, 128))};
     }
@@ -1100,7 +1219,7 @@ static void tune_save() {
   for (const std::string& l : keep) fputs(l.c_str(), f);
   for (const auto& kv : g_level_tune)
     fprintf(f, "%s|%llu|%d|%d\n", g_tune_gpu.c_str(), (unsigned long long)kv.first, kv.second.shift, kv.second.gmax);
-  fprintf(f, "%s|pipeline|%d|%d\n", g_tune_gpu.c_str(), g_pipeline_shift, g_pipeline_parts);
+  fprintf(f, "%s|pipeline|%d|%d\n", g_tune_gpu.c_str(), g_pipeline_shift, g_pipeline_growth);
   fclose(f);
 }
 static LevelTune level_tune(bool f64, int k, int64_t A) {
@@ -1160,6 +1279,10 @@ static int gccb_prepare(Context* cx, const double* matrix, int n_mats, int m, Dr
   int ex = 0;
   std::frexp(std::max(umax, 1e-300) * std::max(n, 1), &ex);
   const int fx = std::max(-900, std::min(61 - ex, 200));
+  // the Laplace step's fixed point: |U| * 2^lfx < 2^53 (umax < 2^eu)
+  int eu = 0;
+  std::frexp(std::max(umax, 1e-300), &eu);
+  const int lfx = std::max(-900, std::min(53 - eu, 1000));
   // Per-level layout (levels 2..Lmax need sweeps).
   std::vector<std::vector<LevelSample>> tab(Lmax + 2);
   std::vector<int64_t> lvl_threads(Lmax + 2, 0), lvl_parts(Lmax + 2, 0), lvl_pool(Lmax + 2, 0);
@@ -1359,7 +1482,7 @@ static int gccb_prepare(Context* cx, const double* matrix, int n_mats, int m, Dr
     if ((e = cudaGetLastError()) != cudaSuccess) return fail_cuda(e, "fixed-point matrices");
     const int64_t cnt2 = (int64_t)mm * n_mats;
     transpose_matrices_kernel<<<(unsigned)((cnt2 + 255) / 256), 256, 0, s>>>((const double2*)(d + o_U), dUt, dUabs,
-                                                                              m, cnt2, f64 ? 1 : 0);
+                                                                              m, cnt2, f64 ? 1 : 0, lfx);
     if ((e = cudaGetLastError()) != cudaSuccess) return fail_cuda(e, "transposed matrices");
   }
   destroy_events(R);
@@ -1406,7 +1529,8 @@ static int gccb_prepare(Context* cx, const double* matrix, int n_mats, int m, Dr
     fa.fx = fx;
     fa.Ufx = dUfx;
     fa.Uff = f64 ? nullptr : (const float4*)dUt;
-    fa.Ud = f64 ? (const double2*)dUt : nullptr;
+    fa.Ulimb = f64 ? (const int4*)dUt : nullptr;
+    fa.lfx = lfx;
     fa.Uabs = dUabs;
     fa.mstride = (n_mats > 1) ? (int64_t)mm : 0;
     fa.npart = (const uint8_t*)(d + o_np);
@@ -1543,12 +1667,15 @@ static void keep_rows(Draws& D, int first, int count) {
 static int sample_slice_locked(const double* matrix, int m, const int32_t* input_state,
                                const double* particle_weights, int nw, MT19937& mt, int n_samples, int first,
                                int count, int32_t* samples) {
-  // Large batches run as pipelined parts: while the GPU samples one part, the host
-  // replays and plans the next.  The first part is count >> g_pipeline_shift (an
-  // eighth unless tuned), so that the GPU starts early; the rest is cut into
-  // g_pipeline_parts nearly equal parts.  Parts alternate between the two slots
-  // (device buffers, pinned buffer, graph and stream each), so consecutive parts
-  // overlap on the GPU; a slot is reused once its previous part has finished,
+  // Large batches run as pipelined parts: while the GPU samples the parts it has,
+  // the host replays and plans the next.  The first part is count >> g_pipeline_shift
+  // (a sixteenth unless tuned), so that the GPU starts early, and every later part
+  // is g_pipeline_growth times the one before (the last one takes the rest), so
+  // that the host's replay of a part (about 0.1 ms per 10^3 samples) stays ahead
+  // of the GPU's work on the parts before it.  Parts alternate between the two
+  // slots (device buffers, pinned buffer, graph and stream each), so consecutive
+  // parts overlap on the GPU, one part's latency-bound first and last levels beside
+  // the other's heavy ones; a slot is reused once its previous part has finished,
   // and that part's rows are read while the GPU works on the other slot.
   std::vector<int> cut(1, first);
   Context* cx = nullptr;
@@ -1556,8 +1683,14 @@ static int sample_slice_locked(const double* matrix, int m, const int32_t* input
   if (count >= kGccbPipelineMin) {
     if (!(cx = context(&st))) return st;
     tune_load(cx->device);  // the tuned parts of an earlier process, if any
-    const int c0 = count >> g_pipeline_shift, rest = count - c0;
-    for (int p = 0; p < g_pipeline_parts; ++p) cut.push_back(first + c0 + (int)((int64_t)rest * p / g_pipeline_parts));
+    int64_t size = std::max(count >> g_pipeline_shift, 1), at = 0;
+    while (at + size < count && (int)cut.size() < kGccbMaxParts) {
+      at += size;
+      cut.push_back(first + (int)at);
+      size *= g_pipeline_growth;
+    }
+    if (cut.size() > 2 && count - at < (at - (cut[cut.size() - 2] - first)) / 2)
+      cut.pop_back();  // a short tail joins the part before it
   }
   cut.push_back(first + count);
   const int parts = (int)cut.size() - 1;
@@ -1575,8 +1708,7 @@ static int sample_slice_locked(const double* matrix, int m, const int32_t* input
   int done = 0;  // stream samples replayed so far
   for (int p = 0; p < parts && !st; ++p) {
     const int slot = p % kGccbSlots;
-    if ((st = retire(slot, true))) break;
-    Draws D;
+    Draws D;  // replayed before waiting for the slot: the host's share of the overlap
     const int upto = (p + 1 == parts) ? n_samples : cut[p + 1];  // the last part replays the stream's tail
     if ((st = predraw(input_state, m, particle_weights, nw, mt, upto - done, D))) break;
     if (D.n > kMaxMinorDigits) {
@@ -1586,6 +1718,7 @@ static int sample_slice_locked(const double* matrix, int m, const int32_t* input
     }
     keep_rows(D, cut[p] - done, cut[p + 1] - cut[p]);
     done = upto;
+    if ((st = retire(slot, true))) break;
     if (!std::any_of(D.L.begin(), D.L.end(), [](int32_t l) { return l > 0; })) {  // every row empty
       memset(samples + (size_t)(cut[p] - first) * m, 0, sizeof(int32_t) * (size_t)(cut[p + 1] - cut[p]) * m);
       continue;
@@ -1686,10 +1819,10 @@ static int tune_step(Context* cx, const double* matrix, int m, Draws& D, int rep
 // gets faster, then times the pipelined parts on end-to-end calls.
 // report[0..7]: step ms with the heuristic shapes and with the tuned ones, levels
 // whose shape changed, the pipeline shift, end-to-end ms with the default parts
-// (shift 3, two more parts) and with the tuned ones (0 when the call is below the
+// (shift 4, growth 2) and with the tuned ones (0 when the call is below the
 // pipelining size), the sum over levels of each level's own time (sweep to end of
 // finalize, heuristic shapes: the step minus it is the graph's time between
-// levels), and the number of parts after the first.
+// levels), and the growth of the later parts.
 static int gccb_autotune_locked(Context* cx, const double* matrix, int m, const int32_t* input_state,
                                 const double* weights, int nw, const MT19937& mt0, int n_samples, int reps,
                                 double* report) {
@@ -1756,20 +1889,20 @@ static int gccb_autotune_locked(Context* cx, const double* matrix, int m, const 
   report[1] = keep ? step1 : step0;
   report[2] = changed;
   // The pipelined parts, on end-to-end calls of the same stream: the first part's
-  // shift and the number of parts after it, the default (3, 2) first as the reference.
+  // shift and the growth of the later parts, the default (4, 2) first as the reference.
   report[3] = g_pipeline_shift;
-  report[7] = g_pipeline_parts;
+  report[7] = g_pipeline_growth;
   if (n_samples >= kGccbPipelineMin) {
     std::vector<int32_t> out((size_t)n_samples * m);
     double best_e2e = 1e30;
-    int best_shift = 3, best_parts = 2;
-    std::vector<std::pair<int, int>> cand(1, std::make_pair(3, 2));
-    for (int sh = 1; sh <= 4; ++sh)
-      for (int np = 1; np <= 4; ++np)
-        if (sh != 3 || np != 2) cand.push_back(std::make_pair(sh, np));
+    int best_shift = 4, best_growth = 2;
+    std::vector<std::pair<int, int>> cand(1, std::make_pair(4, 2));
+    for (int sh = 2; sh <= 6; ++sh)
+      for (int gr = 1; gr <= 3; ++gr)
+        if (sh != 4 || gr != 2) cand.push_back(std::make_pair(sh, gr));
     for (size_t c = 0; c < cand.size() && !st; ++c) {
       g_pipeline_shift = cand[c].first;
-      g_pipeline_parts = cand[c].second;
+      g_pipeline_growth = cand[c].second;
       double t_min = 1e30;
       for (int it = 0; it <= reps; ++it) {
         MT19937 t = mt0;
@@ -1784,13 +1917,13 @@ static int gccb_autotune_locked(Context* cx, const double* matrix, int m, const 
       if (c == 0 || t_min < 0.97 * best_e2e) {
         best_e2e = t_min;
         best_shift = cand[c].first;
-        best_parts = cand[c].second;
+        best_growth = cand[c].second;
       }
     }
     g_pipeline_shift = best_shift;
-    g_pipeline_parts = best_parts;
+    g_pipeline_growth = best_growth;
     report[3] = best_shift;
-    report[7] = best_parts;
+    report[7] = best_growth;
     report[5] = best_e2e;
     if (st) return st;
   }
