@@ -158,7 +158,7 @@ __device__ __forceinline__ void minors_walk(const SweepProblem& P, const longlon
 // One launch over many all-minors sweeps (128 threads per block); every thread
 // writes nd + held complex partials, or its group of `group` threads writes their sum.
 template <int NF>
-__global__ void __launch_bounds__(128) minors_sweep_kernel(const SweepProblem* __restrict__ probs, int n_probs,
+__global__ void __launch_bounds__(128, 3) minors_sweep_kernel(const SweepProblem* __restrict__ probs, int n_probs,
                                                            const longlong2* __restrict__ pool, int64_t total_threads,
                                                            double2* __restrict__ partials, int64_t uniform_threads) {
   extern __shared__ double2 minors_smem[];
