@@ -63,3 +63,36 @@ def test_expanded_space_matrix_matches_reference():
         assert np.allclose(got[:m, :m], M, atol=1e-12)
         assert np.allclose(got[m:, m:], np.diag(s), atol=1e-12)
         assert np.allclose(np.linalg.norm(got[m:, :m], axis=1), loss, atol=1e-12)
+
+
+@pytest.mark.parametrize("inp,eta,N,skip", [([1] * 20 + [0] * 20, 0.5, 10000, 0), ([1] * 20 + [0] * 20, 0.5, 4097, 313),
+                                            ([1] * 12 + [0] * 12, None, 3000, 623), ([1] * 5 + [0] * 5, 0.9, 20000, 1),
+                                            ([2, 1, 1, 0, 0], 0.8, 2048, 17), ([1], 0.5, 5000, 600)])
+def test_parallel_replay_equals_numpy(oracle, inp, eta, N, skip):
+    """From 1024 samples on the replay runs on several host threads, each parsing
+    a slice of the word stream from a guessed start, stitched where the slices'
+    parses meet the true one.  The draws, the zero tails of the rows and numpy's
+    final state must be the sequential replay's, from any starting position in
+    the generator's 624-word block."""
+    from theboss_gb300 import _native
+
+    n = sum(inp)
+    w = None if eta is None else oracle.binomial_weights(n, eta)
+    np.random.seed(99)
+    np.random.random(skip)
+    st = np.random.get_state()
+    L_ref, A_ref, U_ref = oracle.predraw_gccb(inp, N, w)
+    st_ref = np.random.get_state()
+    np.random.set_state(st)
+    kept, popped, uni = _native.gccb_predraw(inp, w, N)
+    st_got = np.random.get_state()
+    assert st_got[2] == st_ref[2] and np.array_equal(st_got[1], st_ref[1])
+    assert np.array_equal(kept, L_ref)
+    width = uni.shape[1]
+    A = np.zeros((N, width), dtype=A_ref.dtype)
+    Uu = np.zeros((N, width))
+    A[:, :A_ref.shape[1]] = A_ref[:, :width]
+    Uu[:, :U_ref.shape[1]] = U_ref[:, :width]
+    mask = np.arange(width)[None, :] < kept[:, None]
+    assert np.array_equal(np.where(mask, popped, 0), np.where(mask, A, 0))
+    assert np.array_equal(uni, np.where(mask, Uu, 0.0))  # rows past the kept particles stay zero

@@ -24,12 +24,16 @@
 #include <sys/stat.h>
 
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <cmath>
+#include <condition_variable>
+#include <functional>
 #include <map>
 #include <mutex>
 #include <string>
 #include <numeric>
+#include <thread>
 #include <vector>
 
 #include "../../include/boss.h"
@@ -177,6 +181,354 @@ static void modes_from_draws(Draws& D) {
   }
 }
 
+// ---------------------------------------------------------------------------
+// Parallel replay.  A sample's draws take a data-dependent number of words of
+// the MT19937 stream (the particle count from the loss threshold, randint's
+// rejections), so the stream's split into samples is sequential by nature.  But
+// a parse begun at an arbitrary word meets the true one after a few samples
+// (at 20 photons and eta = 0.5: 19 samples on average, at most 141 in 2000
+// trials): both are functions of the same words, and from the first sample
+// start they share they agree.  So T host threads parse T slices of the
+// pre-generated word stream, each from a guessed start; the stitch follows the
+// true parse from the stream's start, parses on sequentially across the short
+// gap where one slice's parse has not yet met the next one's, and switches to
+// the next slice where they meet.  The result is the sequential replay's, word
+// for word, and the generator ends in the same state.
+// ---------------------------------------------------------------------------
+
+// Host threads for the replay, created on first use and never destroyed (the
+// process ends with them parked).  run(T, fn) runs fn(1..T-1) on the pool and
+// fn(0) on the caller, and returns when all have finished.
+class HostPool {
+ public:
+  static HostPool& get() {
+    static HostPool* p = new HostPool();
+    return *p;
+  }
+  void run(int T, const std::function<void(int)>& fn) {
+    std::lock_guard<std::mutex> serial(run_mu_);
+    while (nthreads_ < T - 1) {
+      const int id = ++nthreads_;
+      std::thread([this, id] { worker(id); }).detach();
+    }
+    {
+      std::lock_guard<std::mutex> lk(mu_);
+      fn_ = &fn;
+      T_ = T;
+      pending_ = T - 1;
+      ++epoch_;
+    }
+    cv_.notify_all();
+    fn(0);
+    std::unique_lock<std::mutex> lk(mu_);
+    done_.wait(lk, [&] { return pending_ == 0; });
+  }
+
+ private:
+  void worker(int id) {
+    uint64_t seen = 0;
+    std::unique_lock<std::mutex> lk(mu_);
+    for (;;) {
+      cv_.wait(lk, [&] { return epoch_ != seen; });
+      seen = epoch_;
+      if (id < T_) {
+        const std::function<void(int)>* f = fn_;
+        lk.unlock();
+        (*f)(id);
+        lk.lock();
+        if (--pending_ == 0) done_.notify_one();
+      }
+    }
+  }
+  std::mutex run_mu_, mu_;
+  std::condition_variable cv_, done_;
+  const std::function<void(int)>* fn_ = nullptr;
+  uint64_t epoch_ = 0;
+  int T_ = 0, pending_ = 0, nthreads_ = 0;
+};
+
+// The generator's output words from its current state on, with the key of every
+// block generated, so that the state after any number of words can be set.  The
+// storage is the caller's (kept between calls: no page faults on reuse).  One
+// thread generates (generate / extend); others may read the words below
+// `ready` (release/acquire) while it does.
+struct WordStream {
+  MT19937& mt;
+  std::vector<uint32_t>& W;     // the words, in stream order
+  std::vector<uint32_t>& keys;  // 624 per generated block
+  uint32_t key0[624];
+  int pos0;
+  uint64_t prefix;               // words left in the generator's current block
+  uint64_t size = 0;             // words generated
+  std::atomic<uint64_t> ready{0};  // words other threads may read
+  std::atomic<bool> done{false};   // the parallel phase's generation has ended
+  WordStream(MT19937& g, std::vector<uint32_t>& words, std::vector<uint32_t>& block_keys)
+      : mt(g), W(words), keys(block_keys), pos0(g.pos) {
+    memcpy(key0, g.key, sizeof(key0));
+    prefix = (pos0 < 624) ? (uint64_t)(624 - pos0) : 0;
+  }
+  // Sizes the storage for `words` words and generates them, publishing each block.
+  void generate(uint64_t words) {
+    const uint64_t blocks = (words > prefix) ? (words - prefix + 623) / 624 : 0;
+    if (W.size() < prefix + blocks * 624) W.resize(prefix + blocks * 624);
+    if (keys.size() < blocks * 624) keys.resize(blocks * 624);
+    memcpy(W.data(), mt.out + (pos0 < 624 ? pos0 : 624), sizeof(uint32_t) * prefix);
+    size = prefix;
+    ready.store(size, std::memory_order_release);
+    for (uint64_t k = 0; k < blocks; ++k) {
+      mt.twist();
+      memcpy(&W[size], mt.out, sizeof(mt.out));
+      memcpy(&keys[k * 624], mt.key, sizeof(mt.key));
+      size += 624;
+      ready.store(size, std::memory_order_release);
+    }
+    done.store(true, std::memory_order_release);
+  }
+  void extend(uint64_t words) {  // after the parallel phase: at least `words` words
+    while (size < words) {
+      const uint64_t k = (size - prefix) / 624;
+      if (W.size() < size + 624) W.resize(size + 624 * 8);
+      if (keys.size() < (k + 1) * 624) keys.resize((k + 8) * 624);
+      mt.twist();
+      memcpy(&W[size], mt.out, sizeof(mt.out));
+      memcpy(&keys[k * 624], mt.key, sizeof(mt.key));
+      size += 624;
+    }
+  }
+  // The generator as the sequential replay leaves it after `used` words.
+  void finish(uint64_t used) {
+    if (used <= prefix) {
+      memcpy(mt.key, key0, sizeof(key0));
+      mt.pos = pos0 + (int)used;
+    } else {
+      const uint64_t g = used - prefix, b = (g - 1) / 624;  // block b (0-based) holds the last word used
+      memcpy(mt.key, &keys[b * 624], sizeof(mt.key));
+      mt.pos = (int)(g - b * 624);                         // in [1, 624]
+    }
+    if (mt.pos < 624) mt.temper_all();
+  }
+};
+
+static inline double words_to_double(uint32_t a, uint32_t b) {  // numpy's random_sample from two words
+  return ((a >> 5) * 67108864.0 + (b >> 6)) / 9007199254740992.0;
+}
+
+struct ReplayParams {
+  int n;                  // input particles
+  const double* weights;  // particle-number weights (null: every particle kept)
+  int nw;
+  const uint32_t* masks;  // randint's masks, by particles left
+};
+
+// One sample's draws from W[p..avail): 1 done (p advanced), 0 the words ran out
+// (p unchanged), -1 the loss threshold lies beyond the weights' sum (theboss's
+// randint(low >= high) error; p advanced past the threshold).  The row's
+// entries from l on are set to zero.
+static inline int parse_sample(const ReplayParams& R, const uint32_t* W, uint64_t avail, uint64_t& p, int32_t& l_out,
+                               uint8_t* is, double* us) {
+  uint64_t q = p;
+  int l = R.n;
+  if (R.weights) {  // generalized_cliffords_b_uniform_losses_simulation_strategy.py:67-85
+    if (q + 2 > avail) return 0;
+    const double thr = words_to_double(W[q], W[q + 1]);
+    q += 2;
+    double acc = 0.0;
+    l = 0;
+    for (int i = 0; i < R.nw; ++i) {
+      acc += R.weights[i];
+      if (acc > thr) break;
+      ++l;
+    }
+    if (l > R.n) {
+      p = q;
+      l_out = l;
+      return -1;
+    }
+  }
+  int remaining = R.n;
+  for (int k = 0; k < l; ++k) {  // generalized_cliffords_b_simulation_strategy.py:97-110
+    const uint32_t rng = (uint32_t)remaining - 1, mask = R.masks[remaining];
+    uint32_t v = 0;
+    if (rng) {
+      do {
+        if (q >= avail) return 0;
+        v = W[q++] & mask;
+      } while (v > rng);
+    }
+    is[k] = (uint8_t)v;
+    --remaining;
+    if (q + 2 > avail) return 0;
+    us[k] = words_to_double(W[q], W[q + 1]);
+    q += 2;
+  }
+  for (int k = l; k < R.n; ++k) {
+    is[k] = 0;
+    us[k] = 0.0;
+  }
+  p = q;
+  l_out = l;
+  return 1;
+}
+
+// One slice's parse: the samples from word `start` on, until a sample ends at or
+// past `stop` or the words run out, in rows of n like the replay's own output.
+// The arrays grow as needed and keep their storage between calls; `count`
+// records are valid.
+struct SliceParse {
+  size_t count = 0;
+  std::vector<uint64_t> begin, end;
+  std::vector<int32_t> L;
+  std::vector<uint8_t> idx;  // count x n
+  std::vector<double> u;     // count x n
+};
+
+static void parse_slice(const ReplayParams& R, WordStream& ws, uint64_t start, uint64_t stop, uint64_t expect_end,
+                        double words_per_sample, SliceParse& S) {
+  const size_t n = (size_t)std::max(R.n, 1);
+  auto grow = [&](size_t c) {
+    if (S.begin.size() >= c) return;
+    S.begin.resize(c);
+    S.end.resize(c);
+    S.L.resize(c);
+    S.idx.resize(c * n);
+    S.u.resize(c * n);
+  };
+  grow((size_t)((double)(std::min(stop, expect_end) - std::min(start, expect_end)) / std::max(words_per_sample, 1.0) *
+               1.1) + 16);
+  const uint32_t* W = ws.W.data();  // sized before the parallel phase: stable
+  size_t c = 0;
+  uint64_t p = start;
+  uint64_t avail = ws.ready.load(std::memory_order_acquire);
+  while (p < stop) {
+    if (c == S.begin.size()) grow(2 * c + 16);
+    int32_t l = 0;
+    const uint64_t b = p;
+    const int r = parse_sample(R, W, avail, p, l, &S.idx[c * n], &S.u[c * n]);
+    if (r == 0) {  // past the generated words: wait for the next block, or stop when generation has ended
+      const bool fin = ws.done.load(std::memory_order_acquire);
+      const uint64_t now = ws.ready.load(std::memory_order_acquire);
+      if (now > avail) {
+        avail = now;
+        continue;
+      }
+      if (fin) break;
+      std::this_thread::yield();
+      continue;
+    }
+    S.begin[c] = b;
+    S.end[c] = p;
+    S.L[c] = l;  // l > n marks theboss's error; it matters only on the true parse
+    ++c;
+  }
+  S.count = c;
+}
+
+// Expected words per sample (the word buffer's size; a short guess only costs a
+// sequential extension at the end).
+static double expected_words(const ReplayParams& R) {
+  auto kept_words = [&](int l) {
+    double w = 0.0;
+    for (int k = 0; k < l; ++k) {
+      const int r = R.n - k;
+      w += 2.0 + (r > 1 ? (double)(R.masks[r] + 1u) / r : 0.0);
+    }
+    return w;
+  };
+  if (!R.weights) return kept_words(R.n);
+  double e = 2.0, tot = 0.0;
+  for (int l = 0; l <= R.n && l < R.nw; ++l) tot += std::max(R.weights[l], 0.0);
+  for (int l = 0; l <= R.n && l < R.nw; ++l) e += std::max(R.weights[l], 0.0) / (tot > 0 ? tot : 1.0) * kept_words(l);
+  return e;
+}
+
+struct ReplayScratch {
+  std::vector<uint32_t> W, keys;
+  std::vector<SliceParse> S;
+};
+
+// The parallel replay of N samples into L (N), idx and u (N x n).  The calling
+// thread generates the words while T pool threads parse the T slices, each
+// following the words as they appear; then the calling thread stitches.
+static int replay_parallel(const ReplayParams& R, MT19937& mt, int N, int T, int32_t* L, uint8_t* idx, double* u) {
+  const size_t n = (size_t)std::max(R.n, 1);
+  static thread_local ReplayScratch rs;  // the calling thread's, reused
+  const double ew = expected_words(R);
+  const uint64_t est = (uint64_t)(N * ew * 1.03) + 4096;
+  WordStream ws(mt, rs.W, rs.keys);
+  std::vector<uint64_t> cut(T + 1);
+  for (int t = 0; t <= T; ++t) cut[t] = est * (uint64_t)t / (uint64_t)T;
+  if ((int)rs.S.size() < T) rs.S.resize(T);
+  std::vector<SliceParse>& S = rs.S;
+  {
+    // storage sized before any reader starts; generate() only writes into it
+    const uint64_t blocks = (est > ws.prefix) ? (est - ws.prefix + 623) / 624 : 0;
+    if (rs.W.size() < ws.prefix + blocks * 624) rs.W.resize(ws.prefix + blocks * 624);
+  }
+  HostPool::get().run(T + 1, [&](int t) {
+    if (t == 0)
+      ws.generate(est);
+    else
+      parse_slice(R, ws, cut[t - 1], t < T ? cut[t] : UINT64_MAX, est, ew, S[t - 1]);
+  });
+  // stitch: follow the true parse from word 0
+  int count = 0;
+  uint64_t p = 0;
+  bool failed = false;  // theboss's randint error on the true parse
+  auto sequential = [&]() {  // one sample parsed at p, extending the words as needed
+    for (;;) {
+      int32_t l = 0;
+      const int r = parse_sample(R, ws.W.data(), ws.size, p, l, idx + (size_t)count * n, u + (size_t)count * n);
+      if (r < 0) {
+        failed = true;
+        return;
+      }
+      if (r > 0) {
+        L[count++] = l;
+        return;
+      }
+      ws.extend(ws.size + 624 * 8);
+    }
+  };
+  for (int t = 0; t < T && count < N && !failed; ++t) {
+    const SliceParse& P = S[t];
+    const size_t cnt = P.count;
+    size_t j = std::lower_bound(P.begin.begin(), P.begin.begin() + cnt, p) - P.begin.begin();
+    while (count < N && !failed && j < cnt && P.begin[j] != p) {  // not met yet: parse across the gap
+      sequential();
+      while (j < cnt && P.begin[j] < p) ++j;
+    }
+    if (failed || j >= cnt || P.begin[j] != p || count >= N) continue;
+    // from row j on the slice's parse is the true one: copy its rows in one piece
+    size_t j1 = std::min(cnt, j + (size_t)(N - count));
+    for (size_t q = j; q < j1; ++q)
+      if (P.L[q] > R.n) {  // theboss's error on the true parse: rows before it stand
+        j1 = q;
+        failed = true;
+        break;
+      }
+    memcpy(L + count, &P.L[j], sizeof(int32_t) * (j1 - j));
+    memcpy(idx + (size_t)count * n, &P.idx[j * n], (j1 - j) * n);
+    memcpy(u + (size_t)count * n, &P.u[j * n], sizeof(double) * (j1 - j) * n);
+    count += (int)(j1 - j);
+    p = failed ? P.end[j1] : P.end[j1 - 1];
+  }
+  while (count < N && !failed) sequential();
+  ws.finish(p);
+  if (failed) {
+    set_error("randint: low >= high (particle-number weights sum below the threshold)");
+    return kErrArg;
+  }
+  return kOk;
+}
+
+// Host threads for a replay of N samples: one per 512 samples, at most 8 and at
+// most half the host's hardware threads; 1 means the sequential replay.
+static int replay_threads(int N, int n) {
+  if (n < 1 || N < 1024) return 1;
+  const int hw = (int)std::thread::hardware_concurrency();
+  return std::max(1, std::min({8, N / 512, hw > 1 ? hw / 2 : 1}));
+}
+
 // The whole random stream of `n_samples` GC&C-B samples, in theboss's draw order.
 static int predraw(const int32_t* input_state, int m, const double* weights, int n_weights, MT19937& mt,
                    int n_samples, Draws& D) {
@@ -215,6 +567,11 @@ static int predraw(const int32_t* input_state, int m, const double* weights, int
   D.modes.clear();
   uint32_t masks[257];
   for (int r = 1; r <= n; ++r) masks[r] = mask_for((uint32_t)r);
+  const int T = replay_threads(n_samples, n);
+  if (T > 1) {
+    const ReplayParams R{n, weights, n_weights, masks};
+    return replay_parallel(R, mt, n_samples, T, L.data(), D.idx.data(), D.u.data());
+  }
   MTReader rd(mt);
   for (int s = 0; s < n_samples; ++s) {
     int l = n;
