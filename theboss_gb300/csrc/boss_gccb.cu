@@ -698,30 +698,89 @@ __device__ __forceinline__ unsigned long long fixed_of_double(double x, int F) {
   return (mant >> -sh) + ((mant >> (-sh - 1)) & 1ull);
 }
 
-// Removes and returns the r-th (0-based) particle still in the 256-bit set `rem`
-// (r is below the number of set bits: the host drew it with randint(0, remaining)).
-__device__ __forceinline__ int pop_particle(uint32_t* rem, int r) {
-  int q = 0;
-  for (; q < 7; ++q) {
-    const int c = __popc(rem[q]);
-    if (r < c) break;
-    r -= c;
+// Removes the r-th (0-based) particle still in a 256-bit set held one 32-bit word
+// per lane (lanes 0..7, the rest 0; r is below the set's size: the host drew it
+// with randint(0, remaining)).  Every lane gets the particle's index; the owning
+// lane's word loses its bit.
+__device__ __forceinline__ int pop_particle_warp(uint32_t& remw, int r, int lane) {
+  const int c = (lane < 8) ? __popc(remw) : 0;
+  int incl = c;  // inclusive prefix over the words
+#pragma unroll
+  for (int off = 1; off < 8; off <<= 1) {
+    const int y = __shfl_up_sync(0xffffffffu, incl, off);
+    if (lane >= off) incl += y;
   }
-  uint32_t x = rem[q];
+  const int excl = incl - c;
+  const unsigned who = __ballot_sync(0xffffffffu, lane < 8 && r >= excl && r < incl);
+  const int q = __ffs(who) - 1;  // the word holding it (r is below the set's size: the host drew it)
   int pos = 0;
-  for (int s = 16; s > 0; s >>= 1) {  // binary search for the bit
-    const uint32_t lo = x & ((1u << s) - 1u);
-    const int c = __popc(lo);
-    if (r >= c) {
-      r -= c;
-      x >>= s;
-      pos += s;
-    } else {
-      x = lo;
+  if (lane == q) {
+    int rr = r - excl;
+    uint32_t x = remw;
+    for (int s = 16; s > 0; s >>= 1) {  // binary search for the bit
+      const uint32_t lo = x & ((1u << s) - 1u);
+      const int cl = __popc(lo);
+      if (rr >= cl) {
+        rr -= cl;
+        x >>= s;
+        pos += s;
+      } else {
+        x = lo;
+      }
     }
+    remw &= ~(1u << pos);
   }
-  rem[q] &= ~(1u << pos);
-  return q * 32 + pos;
+  return q * 32 + __shfl_sync(0xffffffffu, pos, q);
+}
+
+// (r2 2^54 + r1 2^27 + r0) 2^e rounded to the nearest double (ties to even), in
+// integer instructions: the three 64-bit sums of the exact Laplace step (|sum| <
+// 2^113) combined in 128 bits, normalised by a leading-zero count, rounded once.
+// The exponent is folded in when the result is a normal double; otherwise the
+// rounded value is scaled by ldexp (exact unless it under- or overflows).
+__device__ __forceinline__ double limbs_to_double(long long r2, long long r1, long long r0, int e) {
+  // 128-bit two's complement value hi:lo
+  unsigned long long lo = (unsigned long long)r2 << 54;
+  long long hi = r2 >> 10;
+  const unsigned long long l1 = (unsigned long long)r1 << 27;
+  const unsigned long long s1 = lo + l1;
+  hi += (r1 >> 37) + (s1 < lo ? 1 : 0);
+  const unsigned long long s2 = s1 + (unsigned long long)r0;
+  hi += (r0 >> 63) + (s2 < s1 ? 1 : 0);
+  lo = s2;
+  const bool neg = hi < 0;
+  unsigned long long mh = (unsigned long long)hi, ml = lo;
+  if (neg) {  // magnitude
+    ml = ~ml + 1ull;
+    mh = ~mh + (ml == 0 ? 1ull : 0ull);
+  }
+  if ((mh | ml) == 0) return 0.0;
+  const int lz = mh ? __clzll((long long)mh) : 64 + __clzll((long long)ml);
+  unsigned long long th, tl;  // the magnitude shifted left by lz: its top bit at bit 127
+  if (lz >= 64) {
+    th = ml << (lz - 64);
+    tl = 0;
+  } else if (lz == 0) {
+    th = mh;
+    tl = ml;
+  } else {
+    th = (mh << lz) | (ml >> (64 - lz));
+    tl = ml << lz;
+  }
+  unsigned long long m = th >> 11;  // 53 bits
+  const unsigned long long rem = th & 0x7FFull;
+  if (rem > 0x400ull || (rem == 0x400ull && (tl != 0 || (m & 1ull)))) m += 1ull;
+  int ex = 127 - lz;  // |value| = m 2^(ex - 52)
+  if (m >> 53) {
+    m >>= 1;
+    ++ex;
+  }
+  const int be = ex + e + 1023;
+  const unsigned long long sign = neg ? (1ull << 63) : 0ull;
+  if (be >= 1 && be <= 2046)
+    return __longlong_as_double((long long)(sign | ((unsigned long long)be << 52) | (m & 0xFFFFFFFFFFFFFull)));
+  const double v = __longlong_as_double((long long)(sign | ((unsigned long long)(ex + 1023) << 52) | (m & 0xFFFFFFFFFFFFFull)));
+  return ldexp(v, e);
 }
 
 // kF64: the minors, the Laplace step, |.|^2 and the pmf are FP64 (the default);
@@ -737,6 +796,8 @@ __global__ void __launch_bounds__(kFinWarps * 32, 8) gccb_finalize_kernel(Finali
   __shared__ float cn_s[kFinWarps][32];  // |c_d|_1 2^-Ec (the pmf error bound)
   __shared__ int4 climb_s[kFinWarps][32];  // FP64 pmf: the minors as 27-bit limbs (re lo, re hi, im lo, im hi)
   __shared__ int2 cnb_s[kFinWarps][32];    // and -Im as limbs
+  __shared__ uint8_t srow_s[kFinWarps][256];  // the sample's input and output occupations, kept here
+  __shared__ uint8_t trow_s[kFinWarps][256];  // while the kernel updates them (written through to S, T)
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int j = blockIdx.x * kFinWarps + w;
   if (j >= a.A) return;
@@ -744,20 +805,33 @@ __global__ void __launch_bounds__(kFinWarps * 32, 8) gccb_finalize_kernel(Finali
   const longlong2* Ufxs = a.Ufx + (size_t)j * a.mstride;  // and its fixed-point copy
   uint8_t* S = a.S + (size_t)j * m;
   uint8_t* T = a.T + (size_t)j * m;
+  // Everything the particle bookkeeping needs, loaded up front (independent
+  // loads, in flight during the sums below): the occupations, the sample's
+  // randint results and particle modes (one per lane; at most 32 particles), and
+  // its set of particles not yet popped (one word per lane 0..7).
+  const size_t drow = (size_t)a.order[j] * a.n;  // this sample's replayed draws
+  for (int i = lane; i < m; i += 32) {
+    srow_s[w][i] = S[i];
+    trow_s[w][i] = T[i];
+  }
+  const int idxv = (lane < a.n) ? (int)a.idx[drow + lane] : 0;
+  const int pmv = (lane < a.n) ? (int)a.pmode[drow + lane] : 0;
+  uint32_t remw = 0;
+  if (a.k == 1) {
+    const int np = a.npart[a.order[j]];
+    const int lo = lane * 32;
+    if (lane < 8) remw = (np >= lo + 32) ? 0xffffffffu : (np > lo ? ((1u << (np - lo)) - 1u) : 0u);
+  } else if (lane < 8) {
+    remw = a.rem[(size_t)j * 8 + lane];
+  }
+  __syncwarp();
   int nd;
   if (a.k == 1) {
     // one particle: the minors are the input occupations themselves
     // (bs_submatrices_permanent_calculator_base.py:157-158)
-    int mode = 0;
+    const int mode = __shfl_sync(0xffffffffu, pmv, pop_particle_warp(remw, __shfl_sync(0xffffffffu, idxv, 0), lane));
     if (lane == 0) {
-      uint32_t* rem = a.rem + (size_t)j * 8;
-      const int np = a.npart[a.order[j]];
-      for (int q = 0; q < 8; ++q) {
-        const int lo = q * 32;
-        rem[q] = (np >= lo + 32) ? 0xffffffffu : (np > lo ? ((1u << (np - lo)) - 1u) : 0u);
-      }
-      const size_t row = (size_t)a.order[j] * a.n;
-      mode = a.pmode[row + pop_particle(rem, a.idx[row])];
+      srow_s[w][mode] = 1;
       S[mode] = 1;
       subf_s[w][0] = make_float4(1.0f, 0.0f, 0.0f, 0.0f);
       sub_s[w][0] = make_double2(1.0, 0.0);
@@ -912,7 +986,6 @@ __global__ void __launch_bounds__(kFinWarps * 32, 8) gccb_finalize_kernel(Finali
     }
   }
   __syncwarp();
-  const size_t drow = (size_t)a.order[j] * a.n;  // this sample's replayed draws
   const double uu = a.uni[drow + (a.k - 1)];
   const int K = (m + 31) >> 5;  // contiguous outputs per lane in the cdf scan
   const int o0 = lane * K;
@@ -980,7 +1053,7 @@ __global__ void __launch_bounds__(kFinWarps * 32, 8) gccb_finalize_kernel(Finali
     const float ec_b = 2.0f * kMinorsErrF64 + 4.440892e-16f;  // times b_o: eps_m max|c| + 2 2^-52
     const float ec_c = scale_pow2f(csum, 1 - a.lfx);            // 2^(1 - lfx) sum_d |c_d|_1
     const float ec_a = 2.220446e-16f;                           // times a_o: 2 2^-53
-    const double pscale = ldexp(1.0, Ec - 52 - a.lfx);         // the sums' unit
+    const int pexp = Ec - 52 - a.lfx;                          // the sums' unit: 2^pexp
     float errsum = 0.0f;                                        // this lane's share of E * 2^-2Ec
     for (int o = lane; o < full; o += 32) {
       long long r2 = 0, r1 = 0, r0 = 0, i2 = 0, i1 = 0, i0 = 0;
@@ -1001,8 +1074,8 @@ __global__ void __launch_bounds__(kFinWarps * 32, 8) gccb_finalize_kernel(Finali
         ao = fmaf(cn_s[w][d], ua, ao);
         bo += ua;
       }
-      const double pr = (double)(((__int128)r2 << 54) + ((__int128)r1 << 27) + r0) * pscale;
-      const double pi = (double)(((__int128)i2 << 54) + ((__int128)i1 << 27) + i0) * pscale;
+      const double pr = limbs_to_double(r2, r1, r0, pexp);
+      const double pi = limbs_to_double(i2, i1, i0, pexp);
       pmf[o] = fma(pr, pr, pi * pi);
       const float eo = ec_b * bo + ec_c + ec_a * ao;
       errsum += eo * (2.0f * ao + eo) + 4.440892e-16f * ao * ao;  // + |.|^2's two roundings
@@ -1043,8 +1116,8 @@ __global__ void __launch_bounds__(kFinWarps * 32, 8) gccb_finalize_kernel(Finali
         bo += __shfl_xor_sync(0xffffffffu, bo, off);
       }
       if (oi < r && c0 == 0) {
-        const double pr = (double)(((__int128)r2 << 54) + ((__int128)r1 << 27) + r0) * pscale;
-        const double pi = (double)(((__int128)i2 << 54) + ((__int128)i1 << 27) + i0) * pscale;
+        const double pr = limbs_to_double(r2, r1, r0, pexp);
+        const double pi = limbs_to_double(i2, i1, i0, pexp);
         pmf[full + oi] = fma(pr, pr, pi * pi);
         const float eo = ec_b * bo + ec_c + ec_a * ao;
         errsum += eo * (2.0f * ao + eo) + 4.440892e-16f * ao * ao;
@@ -1261,20 +1334,29 @@ __global__ void __launch_bounds__(kFinWarps * 32, 8) gccb_finalize_kernel(Finali
     for (int off = 16; off > 0; off >>= 1) cnt2 += __shfl_xor_sync(0xffffffffu, cnt2, off);
     idx = cnt2 < m ? cnt2 : m - 1;
   }
-  if (lane == 0) T[idx] = (uint8_t)(T[idx] + 1);
+  if (lane == 0) {
+    const uint8_t tv = (uint8_t)(trow_s[w][idx] + 1);
+    trow_s[w][idx] = tv;
+    T[idx] = tv;
+  }
   __syncwarp();
   if (j >= a.A_next) return;
 
   // ---- the all-minors sweep of level k + 1 ----
-  if (lane == 0) {
-    const int mode = a.pmode[drow + pop_particle(a.rem + (size_t)j * 8, a.idx[drow + a.k])];
-    S[mode] = (uint8_t)(S[mode] + 1);
+  {
+    const int mode = __shfl_sync(0xffffffffu, pmv, pop_particle_warp(remw, __shfl_sync(0xffffffffu, idxv, a.k), lane));
+    if (lane == 0) {
+      const uint8_t sv = (uint8_t)(srow_s[w][mode] + 1);
+      srow_s[w][mode] = sv;
+      S[mode] = sv;
+    }
+    if (lane < 8) a.rem[(size_t)j * 8 + lane] = remw;
   }
   __syncwarp();
   int nb = 0, nmul = 0, nf = 0;
   for (int base = 0; base < m; base += 32) {
     const int mode = base + lane;
-    const int sv = (mode < m) ? S[mode] : 0;
+    const int sv = (mode < m) ? srow_s[w][mode] : 0;
     const unsigned b1 = __ballot_sync(0xffffffffu, sv == 1);
     if (sv == 1) {
       const int pos = nb + __popc(b1 & ((1u << lane) - 1u));
@@ -1285,7 +1367,7 @@ __global__ void __launch_bounds__(kFinWarps * 32, 8) gccb_finalize_kernel(Finali
   }
   for (int base = 0; base < m; base += 32) {
     const int mode = base + lane;
-    const int sv = (mode < m) ? S[mode] : 0;
+    const int sv = (mode < m) ? srow_s[w][mode] : 0;
     const unsigned bm = __ballot_sync(0xffffffffu, sv > 1);
     if (sv > 1) {
       const int pos = nb + nmul + __popc(bm & ((1u << lane) - 1u));
@@ -1297,7 +1379,7 @@ __global__ void __launch_bounds__(kFinWarps * 32, 8) gccb_finalize_kernel(Finali
   // factors: every output particle (a mode occupied p times gives p factors)
   for (int base = 0; base < m; base += 32) {
     const int mode = base + lane;
-    const int tv = (mode < m) ? T[mode] : 0;
+    const int tv = (mode < m) ? trow_s[w][mode] : 0;
     int incl = tv;
 #pragma unroll
     for (int off = 1; off < 32; off <<= 1) {
