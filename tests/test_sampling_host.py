@@ -96,3 +96,24 @@ def test_parallel_replay_equals_numpy(oracle, inp, eta, N, skip):
     mask = np.arange(width)[None, :] < kept[:, None]
     assert np.array_equal(np.where(mask, popped, 0), np.where(mask, A, 0))
     assert np.array_equal(uni, np.where(mask, Uu, 0.0))  # rows past the kept particles stay zero
+
+
+def test_parallel_replay_across_growing_shapes(oracle):
+    """The replay keeps its per-thread storage between calls; calls whose particle
+    count grows must not write past what an earlier, smaller call sized."""
+    from theboss_gb300 import _native
+
+    for n, eta, N in [(1, 0.5, 9000), (5, 0.5, 20000), (12, None, 3000), (20, 0.5, 10000), (30, 0.7, 5000)]:
+        inp = [1] * n + [0] * n
+        w = None if eta is None else oracle.binomial_weights(n, eta)
+        np.random.seed(n)
+        L_ref, A_ref, U_ref = oracle.predraw_gccb(inp, N, w)
+        after_ref = np.random.random()
+        np.random.seed(n)
+        kept, popped, uni = _native.gccb_predraw(inp, w, N)
+        assert np.random.random() == after_ref
+        assert np.array_equal(kept, L_ref)
+        for s in range(0, N, 97):
+            l = kept[s]
+            assert popped[s, :l].tolist() == A_ref[s, :l].tolist()
+            assert uni[s, :l].tolist() == U_ref[s, :l].tolist()

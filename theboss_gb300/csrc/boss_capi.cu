@@ -43,11 +43,15 @@ Context* context(int* status) {
     *status = fail_cuda(e, "cudaDeviceGetAttribute");
     return nullptr;
   }
-  if ((e = cudaStreamCreateWithFlags(&g_ctx.stream, cudaStreamNonBlocking)) != cudaSuccess ||
-      (e = cudaStreamCreateWithFlags(&g_ctx.stream2, cudaStreamNonBlocking)) != cudaSuccess) {
+  if ((e = cudaStreamCreateWithFlags(&g_ctx.stream, cudaStreamNonBlocking)) != cudaSuccess) {
     *status = fail_cuda(e, "cudaStreamCreate");
     return nullptr;
   }
+  for (cudaStream_t& st : g_ctx.sampler_streams)
+    if ((e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking)) != cudaSuccess) {
+      *status = fail_cuda(e, "cudaStreamCreate");
+      return nullptr;
+    }
   if ((e = prepare_sweep_kernels()) != cudaSuccess) {
     *status = fail_cuda(e, "kernel attributes");
     return nullptr;

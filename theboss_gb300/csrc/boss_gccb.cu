@@ -385,13 +385,14 @@ struct SliceParse {
 static void parse_slice(const ReplayParams& R, WordStream& ws, uint64_t start, uint64_t stop, uint64_t expect_end,
                         double words_per_sample, SliceParse& S) {
   const size_t n = (size_t)std::max(R.n, 1);
+  size_t cap = 0;  // records the arrays hold (sized for this call's n: the storage is reused across calls)
   auto grow = [&](size_t c) {
-    if (S.begin.size() >= c) return;
-    S.begin.resize(c);
-    S.end.resize(c);
-    S.L.resize(c);
-    S.idx.resize(c * n);
-    S.u.resize(c * n);
+    if (S.begin.size() < c) S.begin.resize(c);
+    if (S.end.size() < c) S.end.resize(c);
+    if (S.L.size() < c) S.L.resize(c);
+    if (S.idx.size() < c * n) S.idx.resize(c * n);
+    if (S.u.size() < c * n) S.u.resize(c * n);
+    cap = c;
   };
   grow((size_t)((double)(std::min(stop, expect_end) - std::min(start, expect_end)) / std::max(words_per_sample, 1.0) *
                1.1) + 16);
@@ -400,7 +401,7 @@ static void parse_slice(const ReplayParams& R, WordStream& ws, uint64_t start, u
   uint64_t p = start;
   uint64_t avail = ws.ready.load(std::memory_order_acquire);
   while (p < stop) {
-    if (c == S.begin.size()) grow(2 * c + 16);
+    if (c == cap) grow(2 * c + 16);
     int32_t l = 0;
     const uint64_t b = p;
     const int r = parse_sample(R, W, avail, p, l, &S.idx[c * n], &S.u[c * n]);
@@ -1518,15 +1519,15 @@ struct GccbRun {
 // Draws decided by the exact sequential rule (a cdf step within the error window
 // of the uniform), summed over the sampler's calls until read (boss_gccb_near_ties).
 static int64_t g_gccb_near_ties = 0;
-// Two independent slots (device buffers cx->gccb[8 slot .. 8 slot + 7], a pinned
-// staging buffer and a graph each): the host can plan one batch while the GPU
-// runs the other.
-constexpr int kGccbSlots = 2;
+// Independent slots (device buffers cx->gccb[8 slot .. 8 slot + 7], a pinned
+// staging buffer, a graph and a stream each): the host can plan one batch while
+// the GPU runs the others, and their kernels overlap on the GPU.
+constexpr int kGccbSlots = 4;
 constexpr int kGccbPipelineMin = 4096;  // samples from which a call runs as pipelined parts
 constexpr int kGccbMaxParts = 8;         // parts of a pipelined call at most
-static cudaGraphExec_t g_gccb_exec[kGccbSlots] = {nullptr, nullptr};
-static void* g_gccb_pinned[kGccbSlots] = {nullptr, nullptr};
-static size_t g_gccb_pinned_bytes[kGccbSlots] = {0, 0};
+static cudaGraphExec_t g_gccb_exec[kGccbSlots] = {};
+static void* g_gccb_pinned[kGccbSlots] = {};
+static size_t g_gccb_pinned_bytes[kGccbSlots] = {};
 
 static int ensure_slot_pinned(int slot, size_t bytes) {
   if (g_gccb_pinned_bytes[slot] >= bytes) return kOk;
@@ -1668,10 +1669,10 @@ static LevelTune level_tune(bool f64, int k, int64_t A) {
   return it == g_level_tune.end() ? LevelTune{} : it->second;
 }
 
-// Slot 0 runs on the library's stream, slot 1 on the context's second stream, so
-// that the parts of a pipelined call overlap on the GPU (one part's latency-bound
-// first levels beside the other part's heavy ones).
-static inline cudaStream_t slot_stream(Context* cx, int slot) { return slot ? cx->stream2 : cx->stream; }
+// Slot 0 runs on the library's stream, slots 1.. on the context's sampler
+// streams, so that the parts of a pipelined call overlap on the GPU (one part's
+// latency-bound first levels beside another's heavy ones).
+static inline cudaStream_t slot_stream(Context* cx, int slot) { return slot ? cx->sampler_streams[slot - 1] : cx->stream; }
 
 // matrices: n_mats complex m x m matrices, U[out][in]; one for every sample
 // (n_mats == 1) or one per sample (n_mats == number of samples).
@@ -2111,11 +2112,11 @@ static int sample_slice_locked(const double* matrix, int m, const int32_t* input
   // (a sixteenth unless tuned), so that the GPU starts early, and every later part
   // is g_pipeline_growth times the one before (the last one takes the rest), so
   // that the host's replay of a part (about 0.1 ms per 10^3 samples) stays ahead
-  // of the GPU's work on the parts before it.  Parts alternate between the two
-  // slots (device buffers, pinned buffer, graph and stream each), so consecutive
-  // parts overlap on the GPU, one part's latency-bound first and last levels beside
-  // the other's heavy ones; a slot is reused once its previous part has finished,
-  // and that part's rows are read while the GPU works on the other slot.
+  // of the GPU's work on the parts before it.  Parts take the slots in turn
+  // (device buffers, pinned buffer, graph and stream each), so consecutive parts
+  // overlap on the GPU, one part's latency-bound first and last levels beside
+  // another's heavy ones; a slot is reused once its previous part has finished,
+  // and that part's rows are read while the GPU works on the other slots.
   std::vector<int> cut(1, first);
   Context* cx = nullptr;
   int st = kOk;
@@ -2134,7 +2135,8 @@ static int sample_slice_locked(const double* matrix, int m, const int32_t* input
   cut.push_back(first + count);
   const int parts = (int)cut.size() - 1;
   GccbRun R[kGccbSlots];
-  int in_flight[kGccbSlots] = {-1, -1};  // the part each slot is running, or -1
+  int in_flight[kGccbSlots];  // the part each slot is running, or -1
+  for (int& f : in_flight) f = -1;
   // Waits for the slot's part and writes its rows (or, after an error, only waits).
   auto retire = [&](int slot, bool read) -> int {
     const int p = in_flight[slot];

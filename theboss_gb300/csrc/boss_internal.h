@@ -106,9 +106,9 @@ struct Context {
   int device = 0;
   int sm_count = 0;
   cudaStream_t stream = nullptr;
-  cudaStream_t stream2 = nullptr;  // the sampler's second pipelined slot (boss_gccb.cu)
+  cudaStream_t sampler_streams[3] = {nullptr, nullptr, nullptr};  // the sampler's pipelined slots 1..3 (boss_gccb.cu)
   DeviceBuffer plans, pool, partials, out, counter, index, misc, gpart, pperm;
-  DeviceBuffer gccb[16];
+  DeviceBuffer gccb[32];  // the sampler's slots, 8 each
   DeviceBuffer dist[4];
   void* pinned = nullptr;
   size_t pinned_bytes = 0;
