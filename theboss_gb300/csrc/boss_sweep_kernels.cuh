@@ -117,7 +117,7 @@ __device__ __forceinline__ void minors_walk(const SweepProblem& P, const longlon
     double w;
     decode_code<NF>(P, D, base, (uint64_t)a, sr, si, g, parity, w);
     double Rr = 0.0, Ri = 0.0;
-    accumulate_product<NF>(sr, si, bias, parity << 31, Rr, Ri);
+    accumulate_product<NF, 2>(sr, si, bias, parity << 31, Rr, Ri);
     const uint64_t end = (uint64_t)(a + len);
     for (uint64_t t = (uint64_t)a + 1; t < end; ++t) {
       const int i = __ffsll((long long)t) - 1;
@@ -149,7 +149,7 @@ __device__ __forceinline__ void minors_walk(const SweepProblem& P, const longlon
           decode_code<NF>(P, D, base, t, sr, si, g, parity, w);
         }
       }
-      accumulate_product<NF>(sr, si, bias, parity << 31, Rr, Ri);
+      accumulate_product<NF, 2>(sr, si, bias, parity << 31, Rr, Ri);
     }
     settle_minors<STRIDE>(P, M, Rr, Ri, w, g, t_seg);
   }
