@@ -527,8 +527,9 @@ def roofline(b, sweep_s, achieved, peak, peak32, traffic):
     sweeps against the FP64 peak."""
     common = {"traffic": traffic, "sweep_ms_per_step": sweep_s * 1e3, "flops_per_step": b["sweep_flops"],
               "flops_note": "9k - 12 flops per Guan code at level k over the codes the Glynn-form all-minors "
-                            "sweeps walk (half of theboss's Ryser-form codes for single photons); "
-                            "ryser_form_* count theboss's codes",
+                            "sweeps walk (half of theboss's Ryser-form codes for single photons); of these "
+                            "the row-sum updates and the first two factor-pair products run exactly on the "
+                            "integer pipe, the rest on the FP64 pipe; ryser_form_* count theboss's codes",
               "ryser_form_flops_per_step": b["ref_flops"],
               "ryser_form_equivalent_tflops": b["ref_flops"] / sweep_s / 1e12}
     if b["ff_inst"] > 0:
