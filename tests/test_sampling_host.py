@@ -117,3 +117,28 @@ def test_parallel_replay_across_growing_shapes(oracle):
             l = kept[s]
             assert popped[s, :l].tolist() == A_ref[s, :l].tolist()
             assert uni[s, :l].tolist() == U_ref[s, :l].tolist()
+
+
+@pytest.mark.filterwarnings("ignore::DeprecationWarning")
+def test_parallel_replay_in_a_forked_child(oracle):
+    """A child forked after the replay's host threads started inherits none of
+    them; its replay must still finish, with the parent's draws."""
+    import os
+
+    from theboss_gb300 import _native
+
+    inp = [1] * 20 + [0] * 20
+    w = oracle.binomial_weights(20, 0.5)
+    np.random.seed(1)
+    ref, _, _ = _native.gccb_predraw(inp, w, 5000)
+    pid = os.fork()
+    if pid == 0:  # the child: exit code 0 when its replay equals the parent's
+        code = 1
+        try:
+            np.random.seed(1)
+            got, _, _ = _native.gccb_predraw(inp, w, 5000)
+            code = 0 if np.array_equal(got, ref) else 2
+        finally:
+            os._exit(code)
+    _, status = os.waitpid(pid, 0)
+    assert os.WIFEXITED(status) and os.WEXITSTATUS(status) == 0

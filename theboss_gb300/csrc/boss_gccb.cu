@@ -22,6 +22,7 @@
 #include <stdio.h>
 #include <stdlib.h>
 #include <sys/stat.h>
+#include <unistd.h>
 
 #include <algorithm>
 #include <atomic>
@@ -198,11 +199,20 @@ static void modes_from_draws(Draws& D) {
 
 // Host threads for the replay, created on first use and never destroyed (the
 // process ends with them parked).  run(T, fn) runs fn(1..T-1) on the pool and
-// fn(0) on the caller, and returns when all have finished.
+// fn(0) on the caller, and returns when all have finished.  A process forked
+// from one with a pool inherits the object but not its threads: its first
+// replay makes a pool of its own and leaves the inherited one untouched.
 class HostPool {
  public:
   static HostPool& get() {
-    static HostPool* p = new HostPool();
+    static std::atomic<HostPool*> pool{nullptr};
+    const pid_t me = getpid();
+    HostPool* p = pool.load(std::memory_order_acquire);
+    while (!p || p->pid_ != me) {
+      HostPool* fresh = new HostPool(me);  // no threads yet: safe to delete if another caller wins
+      if (pool.compare_exchange_strong(p, fresh, std::memory_order_acq_rel)) return *fresh;
+      delete fresh;
+    }
     return *p;
   }
   void run(int T, const std::function<void(int)>& fn) {
@@ -240,6 +250,8 @@ class HostPool {
       }
     }
   }
+  explicit HostPool(pid_t pid) : pid_(pid) {}
+  const pid_t pid_;
   std::mutex run_mu_, mu_;
   std::condition_variable cv_, done_;
   const std::function<void(int)>* fn_ = nullptr;
