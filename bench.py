@@ -11,7 +11,8 @@ samples through the captured sampler graph.
            in HBM, CUDA-event timed per step, L2 flushed (256 MiB memset) between
            steps.
   e2e      samples/s through the C ABI with host buffers (boss_gccb_sample: host
-           random-stream replay, H2D, graph, D2H).
+           random-stream replay, H2D, graph, D2H), timed over `steps` calls after
+           `warmup` untimed ones.
   roofline the all-minors sweep kernel (the dominant kernel) against the FP64 FMA
            peak measured live by boss_fp64_peak.
   plain_gpu / batched_vs_plain
@@ -604,13 +605,15 @@ def run_ours(args, rank, world):
             traffic = json.load(open(tpath)).get("dram_bytes_per_step")
         except Exception:
             traffic = None
-    # e2e through the C ABI with host buffers; the samples must equal the device run's
+    # e2e through the C ABI with host buffers; the samples must equal the device run's.
+    # The same warm-up count as the device section, untimed, then `steps` timed calls.
     e2e_t = []
-    for _ in range(args.steps):
+    for it in range(args.warmup + args.steps):
         np.random.seed(args.seed + rank)
         t = time.perf_counter()
         out = _native.gccb_sample(U, inp, w, args.samples)
-        e2e_t.append(time.perf_counter() - t)
+        if it >= args.warmup:
+            e2e_t.append(time.perf_counter() - t)
     clk = clocks.stop()
     if not np.array_equal(out, b["samples"]):
         raise SystemExit("e2e samples differ from the device-timed run")

@@ -652,6 +652,7 @@ struct FinalizeArgs {
   const SweepProblem* probs_cur;
   const uint8_t* dmode_cur;  // [sample][32]
   const double2* partials;
+  const double2* reduced;       // FP64 levels with long partial sums: the sums, 32 per sample (else null)
   SweepProblem* probs_next;
   uint8_t* dmode_next;
   longlong2* pool_next;
@@ -796,6 +797,43 @@ __device__ __forceinline__ double limbs_to_double(long long r2, long long r1, lo
   return ldexp(v, e);
 }
 
+// The levels where each sample's sweep leaves many partial rows (the top levels:
+// a few samples, thousands of threads each) sum them here, one block of 128
+// threads per (sample, digit), instead of in the finalize's single warp, whose
+// dependent loads and adds made that sum its slowest phase.  Thread t adds rows
+// t, t + 128, .. in order, then a fixed-order tree; the result is unscaled
+// (the finalize applies the problem's scale), row j of `out` holds sample j's
+// digits.
+constexpr int kReduceMinParts = 32;  // partial rows per sample from which a level gets this kernel
+__global__ void __launch_bounds__(128) gccb_partials_reduce_kernel(const SweepProblem* __restrict__ probs,
+                                                                  const double2* __restrict__ partials,
+                                                                  double2* __restrict__ out) {
+  __shared__ double sx[128], sy[128];
+  const int j = blockIdx.x, d = blockIdx.y;
+  const SweepProblem& P = probs[j];
+  const int nd = P.nd + P.fixed_digit;
+  if (d >= nd) return;
+  const int64_t parts = P.n_threads / P.group;
+  double x = 0.0, y = 0.0;
+#pragma unroll 4
+  for (int64_t q = threadIdx.x; q < parts; q += 128) {
+    const double2 v = partials[P.part_off + q * nd + d];
+    x += v.x;
+    y += v.y;
+  }
+  sx[threadIdx.x] = x;
+  sy[threadIdx.x] = y;
+  __syncthreads();
+  for (int h = 64; h > 0; h >>= 1) {
+    if ((int)threadIdx.x < h) {
+      sx[threadIdx.x] += sx[threadIdx.x + h];
+      sy[threadIdx.x] += sy[threadIdx.x + h];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) out[(size_t)j * 32 + d] = make_double2(sx[0], sy[0]);
+}
+
 // kF64: the minors, the Laplace step, |.|^2 and the pmf are FP64 (the default);
 // otherwise float pairs on the FP32 pipe (the opt-in float-pair arithmetic).
 template <bool kF64>
@@ -892,6 +930,11 @@ __global__ void __launch_bounds__(kFinWarps * 32, 8) gccb_finalize_kernel(Finali
           }
           if (lane == d) subf_s[w][d] = make_float4(rh * sc, rl * sc, ih * sc, il * sc);
         }
+      }
+    } else if (a.reduced) {  // summed by gccb_partials_reduce_kernel
+      if (lane < nd) {
+        const double2 v = a.reduced[(size_t)j * 32 + lane];
+        sub_s[w][lane] = make_double2(v.x * P.scale, v.y * P.scale);
       }
     } else {
       // FP64 partials (parts x nd), summed in a fixed order.  Every FP64
@@ -1794,6 +1837,8 @@ static int gccb_prepare(Context* cx, const double* matrix, int n_mats, int m, Dr
   std::vector<char> uniform(Lmax + 2, 0);
   std::vector<LevelSample> uni_lvl(Lmax + 2);
   std::vector<int> grp(Lmax + 2, 1);
+  std::vector<char> red(Lmax + 2, 0);  // level k's partial rows summed by gccb_partials_reduce_kernel
+  int64_t max_red = 0;                 // samples of the largest such level
   for (int k = 2; k <= Lmax; ++k) {
     const int Ak = A[k];
     const std::vector<uint64_t>& codes = lvl_codes[k];
@@ -1836,6 +1881,10 @@ static int gccb_prepare(Context* cx, const double* matrix, int n_mats, int m, Dr
       uni_lvl[k].n_threads = tps;
       uni_lvl[k].part_off = tps * nd0;
       uni_lvl[k].pool_off = pool_units(nd0);
+      if (!ffl[k] && tps / G >= kReduceMinParts && nd0 <= 32) {
+        red[k] = 1;
+        max_red = std::max<int64_t>(max_red, Ak);
+      }
       lvl_threads[k] = tps * Ak;
       lvl_parts[k] = tps * nd0 * Ak;
       lvl_pool[k] = pool_units(nd0) * Ak;
@@ -1892,7 +1941,7 @@ static int gccb_prepare(Context* cx, const double* matrix, int n_mats, int m, Dr
   if ((st = ensure(B[2], sizeof(SweepProblem) * (size_t)A[1] * 2 + 512))) return st;  // problems x2
   if ((st = ensure(B[3], (size_t)A[1] * 32 * 2))) return st;                          // digit modes x2
   if ((st = ensure(B[4], sizeof(longlong2) * (size_t)max_pool * 2 + 512))) return st;  // rows x2
-  if ((st = ensure(B[5], sizeof(double2) * (size_t)max_parts))) return st;            // partials
+  if ((st = ensure(B[5], sizeof(double2) * (size_t)(max_parts + 32 * max_red)))) return st;  // partials | sums
   if ((st = ensure(B[6], sizeof(uint32_t) * 8 * (size_t)N))) return st;                // particles left
   // U fixed point | U^T (doubles or float pairs) | U^T 1-norms
   if ((st = ensure(B[7], 36 * (size_t)m * m * n_mats + 256))) return st;
@@ -1922,6 +1971,7 @@ static int gccb_prepare(Context* cx, const double* matrix, int n_mats, int m, Dr
   uint8_t* dmode[2] = {(uint8_t*)B[3].ptr, (uint8_t*)B[3].ptr + (size_t)A[1] * 32};
   longlong2* pool[2] = {(longlong2*)B[4].ptr, (longlong2*)B[4].ptr + max_pool};
   double2* partials = (double2*)B[5].ptr;
+  double2* reduced = partials + max_parts;  // 32 per sample of a level with red[k]
   cudaStream_t s = slot_stream(cx, slot);
   cudaError_t e = cudaMemcpyAsync(d, h, arena, cudaMemcpyHostToDevice, s);
   if (e != cudaSuccess) return fail_cuda(e, "H2D sampler arena");
@@ -1971,6 +2021,12 @@ static int gccb_prepare(Context* cx, const double* matrix, int n_mats, int m, Dr
       if (le != cudaSuccess) break;
       ++R.kernels;
       ++R.sweeps;
+      if (red[k]) {
+        gccb_partials_reduce_kernel<<<dim3((unsigned)A[k], (unsigned)std::min(k, 32)), 128, 0, s>>>(probs[cur],
+                                                                                                 partials, reduced);
+        if ((le = cudaGetLastError()) != cudaSuccess) break;
+        ++R.kernels;
+      }
     }
     FinalizeArgs fa;
     fa.k = k;
@@ -1996,6 +2052,7 @@ static int gccb_prepare(Context* cx, const double* matrix, int n_mats, int m, Dr
     fa.probs_cur = probs[cur];
     fa.dmode_cur = dmode[cur];
     fa.partials = partials;
+    fa.reduced = (k >= 2 && red[k]) ? reduced : nullptr;
     fa.probs_next = probs[nxt];
     fa.dmode_next = dmode[nxt];
     fa.pool_next = pool[nxt];
