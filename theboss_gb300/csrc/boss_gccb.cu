@@ -63,6 +63,11 @@ struct MT19937 {
     }
   }
   void twist() {
+    twist_key();
+    temper_all();
+    pos = 0;
+  }
+  void twist_key() {  // the next block's key, without tempering it
     const uint32_t upper = 0x80000000u, lower = 0x7fffffffu, a = 0x9908b0dfu;
     int i = 0;
     for (; i < 624 - 397; ++i) {
@@ -75,8 +80,6 @@ struct MT19937 {
     }
     const uint32_t y = (key[623] & upper) | (key[0] & lower);
     key[623] = key[396] ^ (y >> 1) ^ ((0u - (y & 1u)) & a);
-    temper_all();
-    pos = 0;
   }
   inline uint32_t next32() {
     if (pos >= 624) twist();
@@ -260,14 +263,16 @@ class HostPool {
 };
 
 // The generator's output words from its current state on, with the key of every
-// block generated, so that the state after any number of words can be set.  The
-// storage is the caller's (kept between calls: no page faults on reuse).  One
-// thread generates (generate / extend); others may read the words below
-// `ready` (release/acquire) while it does.
+// kKeyStride-th block generated, so that the state after any number of words can
+// be set (by re-twisting at most kKeyStride - 1 blocks).  The storage is the
+// caller's (kept between calls: no page faults on reuse).  One thread generates
+// (generate / extend); others may read the words below `ready` (release/acquire)
+// while it does.
+constexpr uint64_t kKeyStride = 16;
 struct WordStream {
   MT19937& mt;
   std::vector<uint32_t>& W;     // the words, in stream order
-  std::vector<uint32_t>& keys;  // 624 per generated block
+  std::vector<uint32_t>& keys;  // 624 per kKeyStride generated blocks: the key of blocks 0, 16, ..
   uint32_t key0[624];
   int pos0;
   uint64_t prefix;               // words left in the generator's current block
@@ -280,31 +285,35 @@ struct WordStream {
     prefix = (pos0 < 624) ? (uint64_t)(624 - pos0) : 0;
   }
   // Sizes the storage for `words` words and generates them, publishing each block.
+  // One more block: its words appended, its key kept when it starts a stride.
+  void next_block() {
+    const uint64_t k = (size - prefix) / 624;
+    mt.twist();
+    memcpy(&W[size], mt.out, sizeof(mt.out));
+    if (k % kKeyStride == 0) {
+      const uint64_t slot = k / kKeyStride;
+      if (keys.size() < (slot + 1) * 624) keys.resize((slot + 8) * 624);
+      memcpy(&keys[slot * 624], mt.key, sizeof(mt.key));
+    }
+    size += 624;
+  }
   void generate(uint64_t words) {
     const uint64_t blocks = (words > prefix) ? (words - prefix + 623) / 624 : 0;
     if (W.size() < prefix + blocks * 624) W.resize(prefix + blocks * 624);
-    if (keys.size() < blocks * 624) keys.resize(blocks * 624);
+    if (keys.size() < (blocks / kKeyStride + 1) * 624) keys.resize((blocks / kKeyStride + 1) * 624);
     memcpy(W.data(), mt.out + (pos0 < 624 ? pos0 : 624), sizeof(uint32_t) * prefix);
     size = prefix;
     ready.store(size, std::memory_order_release);
     for (uint64_t k = 0; k < blocks; ++k) {
-      mt.twist();
-      memcpy(&W[size], mt.out, sizeof(mt.out));
-      memcpy(&keys[k * 624], mt.key, sizeof(mt.key));
-      size += 624;
+      next_block();
       ready.store(size, std::memory_order_release);
     }
     done.store(true, std::memory_order_release);
   }
   void extend(uint64_t words) {  // after the parallel phase: at least `words` words
     while (size < words) {
-      const uint64_t k = (size - prefix) / 624;
       if (W.size() < size + 624) W.resize(size + 624 * 8);
-      if (keys.size() < (k + 1) * 624) keys.resize((k + 8) * 624);
-      mt.twist();
-      memcpy(&W[size], mt.out, sizeof(mt.out));
-      memcpy(&keys[k * 624], mt.key, sizeof(mt.key));
-      size += 624;
+      next_block();
     }
   }
   // The generator as the sequential replay leaves it after `used` words.
@@ -314,8 +323,10 @@ struct WordStream {
       mt.pos = pos0 + (int)used;
     } else {
       const uint64_t g = used - prefix, b = (g - 1) / 624;  // block b (0-based) holds the last word used
-      memcpy(mt.key, &keys[b * 624], sizeof(mt.key));
-      mt.pos = (int)(g - b * 624);                         // in [1, 624]
+      const uint64_t b0 = b - b % kKeyStride;
+      memcpy(mt.key, &keys[(b0 / kKeyStride) * 624], sizeof(mt.key));
+      for (uint64_t q = b0; q < b; ++q) mt.twist_key();
+      mt.pos = (int)(g - b * 624);  // in [1, 624]
     }
     if (mt.pos < 624) mt.temper_all();
   }
