@@ -6,15 +6,17 @@
 // current input against the output so far, expands them into the m output
 // probabilities and draws one output mode.  Every random number it draws depends
 // only on counts, never on a probability, so the host replays numpy's MT19937
-// stream first (same calls, same order) and the GPU then runs all samples level
-// by level:
-//   level k (one graph node pair): the all-minors sweeps of every sample that has
-//   >= k particles, as one launch of minors_sweep_kernel, then gccb_finalize_kernel
-//   (one warp per sample): fixed-order reduction of the sweep partials, Laplace
-//   expansion over the m outputs, |.|^2, normalisation with a sequential sum,
-//   numpy.random.choice's cdf / searchsorted rule, and the sweep plan of the
-//   sample's next level.
-// The whole level loop is captured into one CUDA graph and launched once.
+// stream first (same calls, same order; on several host threads for large
+// batches) and the GPU then runs all samples level by level:
+//   level k: the all-minors sweeps of every sample that has >= k particles, as
+//   one launch of minors_sweep_kernel (at the last levels followed by
+//   gccb_partials_reduce_kernel), then gccb_finalize_kernel (one warp per
+//   sample): fixed-order reduction of the sweep partials, the Laplace expansion
+//   over the m outputs (exact integer sums), |.|^2, numpy.random.choice's cdf /
+//   searchsorted rule decided exactly, and the sweep plan of the sample's next
+//   level.
+// The whole level loop is captured into one CUDA graph and launched once; large
+// calls run as pipelined parts, each with its own graph and stream.
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <string.h>
