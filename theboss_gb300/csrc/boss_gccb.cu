@@ -817,7 +817,10 @@ __device__ __forceinline__ double limbs_to_double(long long r2, long long r1, lo
 // t, t + 128, .. in order, then a fixed-order tree; the result is unscaled
 // (the finalize applies the problem's scale), row j of `out` holds sample j's
 // digits.
-constexpr int kReduceMinParts = 32;  // partial rows per sample from which a level gets this kernel
+constexpr int kReduceMinParts = 32;   // partial rows per sample from which a level gets this kernel,
+constexpr int kReduceMaxSamples = 16; // when it has this many samples at most (at the level with 1297
+                                      // samples and 45 rows each it cost 64 us against the finalize's
+                                      // own few microseconds of summing)
 __global__ void __launch_bounds__(128) gccb_partials_reduce_kernel(const SweepProblem* __restrict__ probs,
                                                                   const double2* __restrict__ partials,
                                                                   double2* __restrict__ out) {
@@ -1894,7 +1897,7 @@ static int gccb_prepare(Context* cx, const double* matrix, int n_mats, int m, Dr
       uni_lvl[k].n_threads = tps;
       uni_lvl[k].part_off = tps * nd0;
       uni_lvl[k].pool_off = pool_units(nd0);
-      if (!ffl[k] && tps / G >= kReduceMinParts && nd0 <= 32) {
+      if (!ffl[k] && tps / G >= kReduceMinParts && Ak <= kReduceMaxSamples && nd0 <= 32) {
         red[k] = 1;
         max_red = std::max<int64_t>(max_red, Ak);
       }
