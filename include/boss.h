@@ -207,7 +207,7 @@ BOSS_API int boss_gccb_near_ties(int64_t* count, int32_t reset);
  * the sampler, power-of-two shifts of the split (threads per sample) and caps of
  * the size of the thread groups that sum their minors inside the sweep, keeps
  * the fastest shape of every level when the whole step gets faster, then times
- * the pipelined parts (the first part's size and the number of parts after it)
+ * the pipelined parts (the first part's size and the growth of the later ones)
  * on end-to-end calls (calls of at least 4096 samples).  The winners apply to later calls whose levels have the same
  * arithmetic, particle count and power-of-two sample count; they are kept for
  * the process and in a cache file keyed by the GPU's name ($BOSS_TUNE_CACHE, else
@@ -216,11 +216,11 @@ BOSS_API int boss_gccb_near_ties(int64_t* count, int32_t reset);
  * workload on its first call.  reps: timed runs per candidate (after one warm-up).
  * report (8 doubles): step ms with the heuristic shapes, step ms with the tuned
  * shapes, levels whose shape changed, the pipeline shift (first part = count >>
- * shift), end-to-end ms with the default parts (shift 3, two parts after the
- * first) and with the tuned ones (0 below 4096 samples), the summed per-level
- * times of the heuristic shapes (each level from its sweep's start to its
- * finalize's end; the step time minus this is the time between levels), and the
- * number of parts after the first.  No reference counterpart.
+ * shift), end-to-end ms with the default parts (shift 4, each later part twice
+ * the one before) and with the tuned ones (0 below 4096 samples), the summed
+ * per-level times of the heuristic shapes (each level from its sweep's start to
+ * its finalize's end; the step time minus this is the time between levels), and
+ * the growth factor of the later parts.  No reference counterpart.
  */
 BOSS_API int boss_gccb_autotune(const double* matrix, int32_t m, const int32_t* input_state,
                                 const double* particle_weights, int32_t n_weights, const uint32_t* mt_key,

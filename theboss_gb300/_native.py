@@ -384,7 +384,7 @@ def gccb_autotune(U: np.ndarray, input_state, weights, n_samples: int, reps: int
                                key.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32)), _ip(pos), n_samples, reps,
                                _dp(rep)))
     return {"default_step_ms": float(rep[0]), "tuned_step_ms": float(rep[1]), "levels_changed": int(rep[2]),
-            "pipeline_shift": int(rep[3]), "pipeline_parts": int(rep[7]), "e2e_default_split_ms": float(rep[4]),
+            "pipeline_shift": int(rep[3]), "pipeline_growth": int(rep[7]), "e2e_default_split_ms": float(rep[4]),
             "e2e_tuned_split_ms": float(rep[5]), "levels_sum_ms": float(rep[6])}
 
 
