@@ -187,13 +187,14 @@ template <int NF>
 __device__ __forceinline__ void flip_binary(const longlong2* __restrict__ D, int i, uint32_t bit, long long (&sr)[NF],
                                             long long (&si)[NF]) {
   const longlong2* row = D + (size_t)i * NF;
-  const long long sgn = bit ? -1ll : 0ll;  // x ^ -1 - (-1) = -x
+  const long long sgn = bit ? -1ll : 0ll;  // -x = (x ^ -1) + 1: one three-input add per word
+  const long long one = (long long)bit;
 #pragma unroll
   for (int f = 0; f < NF; ++f) {
     if (f > 0 && (f & 7) == 0) load_fence();
     const longlong2 d = row[f];
-    sr[f] += (d.x ^ sgn) - sgn;
-    si[f] += (d.y ^ sgn) - sgn;
+    sr[f] = sr[f] + (d.x ^ sgn) + one;
+    si[f] = si[f] + (d.y ^ sgn) + one;
   }
 }
 
@@ -209,19 +210,34 @@ struct I128 {
   unsigned long long lo;
   long long hi;
 };
-__device__ __forceinline__ I128 mul_s64(long long a, long long b) {
+// High half of the signed 128-bit product (floor(a b / 2^64)); a host build uses __int128.
+__host__ __device__ __forceinline__ long long mulhi_s64(long long a, long long b) {
+#ifdef __CUDA_ARCH__
+  return __mul64hi(a, b);
+#else
+  return (long long)(((__int128)a * (__int128)b) >> 64);
+#endif
+}
+__host__ __device__ __forceinline__ int clz_u64(unsigned long long x) {
+#ifdef __CUDA_ARCH__
+  return __clzll((long long)x);
+#else
+  return x ? __builtin_clzll(x) : 64;
+#endif
+}
+__host__ __device__ __forceinline__ I128 mul_s64(long long a, long long b) {
   I128 r;
   r.lo = (unsigned long long)a * (unsigned long long)b;
-  r.hi = __mul64hi(a, b);
+  r.hi = mulhi_s64(a, b);
   return r;
 }
-__device__ __forceinline__ I128 add128(I128 x, I128 y) {
+__host__ __device__ __forceinline__ I128 add128(I128 x, I128 y) {
   I128 r;
   r.lo = x.lo + y.lo;
   r.hi = x.hi + y.hi + (r.lo < x.lo ? 1 : 0);
   return r;
 }
-__device__ __forceinline__ I128 sub128(I128 x, I128 y) {
+__host__ __device__ __forceinline__ I128 sub128(I128 x, I128 y) {
   I128 r;
   r.lo = x.lo - y.lo;
   r.hi = x.hi - y.hi - (x.lo < y.lo ? 1 : 0);
@@ -270,6 +286,199 @@ __device__ __forceinline__ void cmul_fx_exact(long long a, long long b, long lon
                                               double& im) {
   re = i128_to_double(sub128(mul_s64(a, c), mul_s64(b, d)), e);
   im = i128_to_double(add128(mul_s64(a, d), mul_s64(b, c)), e);
+}
+
+// ---------------------------------------------------------------------------
+// Block floating point on the integer pipe.  A complex value is (re + i im) 2^e,
+// two 64-bit integers sharing one exponent, normalised so that the larger
+// component lies in [2^61, 2^62] in magnitude.  GB300 issues the 64-bit integer
+// multiplies on its FMA pipe and the shifts and adds on its ALU pipe, both far
+// faster than its FP64 pipe (2 lanes/clk/SM), so a chain of factors can be
+// multiplied with no FP64 instruction at all:
+//   * bf_pair: the exact 128-bit product of two fixed-point factors, truncated
+//     once to 62 bits (relative error below 2^-60);
+//   * bf_mul: the product of two normalised values from the high halves of the
+//     four 64 x 64 -> 128-bit products (|product| >= 2^122 before the shift, two
+//     truncations of one unit per component: relative error below 2^-56.5 of
+//     the product's magnitude);
+//   * bf_to_double: one rounding to FP64 (2^-53) at the end.
+// An FP64 complex product errs by up to about 2^-52 of its magnitude, so a chain
+// of these products is at least as accurate as the FP64 chain it replaces.
+// ---------------------------------------------------------------------------
+struct BFloat {
+  long long re, im;
+  int e;
+};
+__host__ __device__ __forceinline__ double bits_to_double(unsigned long long b) {
+#ifdef __CUDA_ARCH__
+  return __longlong_as_double((long long)b);
+#else
+  double d;
+  __builtin_memcpy(&d, &b, sizeof d);
+  return d;
+#endif
+}
+// (re + i im) 2^e normalised, for |re|, |im| <= 2^62.  The shift comes from the
+// leading bit of the one's-complement magnitudes (|x| or |x| - 1), so a negative
+// power of two may land on -2^62; zero stays zero (its exponent drops by 62).
+__host__ __device__ __forceinline__ BFloat bf_norm(long long re, long long im, int e) {
+  const unsigned long long m = (unsigned long long)(re ^ (re >> 63)) | (unsigned long long)(im ^ (im >> 63));
+  const int s = clz_u64(m) - 2;  // >= 0
+  BFloat r;
+  r.re = (long long)((unsigned long long)re << s);
+  r.im = (long long)((unsigned long long)im << s);
+  r.e = e - s;
+  return r;
+}
+__host__ __device__ __forceinline__ int clz_u32(unsigned x) {
+#ifdef __CUDA_ARCH__
+  return __clz((int)x);
+#else
+  return x ? __builtin_clz(x) : 32;
+#endif
+}
+// Bits [s, s + 32) of (hi, lo) for 0 <= s < 32 (and the left-shift form).
+__host__ __device__ __forceinline__ unsigned fshr32(unsigned lo, unsigned hi, int s) {
+#ifdef __CUDA_ARCH__
+  return __funnelshift_r(lo, hi, s);
+#else
+  return (unsigned)((((unsigned long long)hi << 32) | lo) >> (s & 31));
+#endif
+}
+__host__ __device__ __forceinline__ unsigned fshl32(unsigned lo, unsigned hi, int s) {
+#ifdef __CUDA_ARCH__
+  return __funnelshift_l(lo, hi, s);
+#else
+  return (unsigned)(((((unsigned long long)hi << 32) | lo) << (s & 31)) >> 32);
+#endif
+}
+__host__ __device__ __forceinline__ unsigned lo32(long long x) { return (unsigned)(unsigned long long)x; }
+__host__ __device__ __forceinline__ unsigned hi32(long long x) { return (unsigned)((unsigned long long)x >> 32); }
+__host__ __device__ __forceinline__ long long join32(unsigned hi, unsigned lo) {
+  return (long long)(((unsigned long long)hi << 32) | lo);
+}
+// One's-complement magnitude of a 64-bit value's high word (the leading bit of |x| or |x| - 1).
+__host__ __device__ __forceinline__ unsigned mag_hi32(long long x) {
+  const unsigned h = hi32(x);
+  return h ^ (unsigned)((int)h >> 31);
+}
+__host__ __device__ __forceinline__ BFloat bf_mul(const BFloat& x, const BFloat& y) {
+  // |x.re| ... |y.im| <= 2^62: every high half lies in [-2^60, 2^60], the sums in [-2^61, 2^61]
+  const long long re = mulhi_s64(x.re, y.re) - mulhi_s64(x.im, y.im);
+  const long long im = mulhi_s64(x.re, y.im) + mulhi_s64(x.im, y.re);
+  // |x|, |y| >= 2^61, so |x y| 2^-64 >= 2^58 and the larger component is at least
+  // 2^57: its leading bit is in the high word and the normalising shift is 0..5
+  // (30 for a zero product, which stays zero).
+  const int s = clz_u32(mag_hi32(re) | mag_hi32(im)) - 2;
+  BFloat z;
+  z.re = join32(fshl32(lo32(re), hi32(re), s), lo32(re) << (s & 31));
+  z.im = join32(fshl32(lo32(im), hi32(im), s), lo32(im) << (s & 31));
+  z.e = x.e + y.e + 64 - s;
+  return z;
+}
+// The 128-bit value (hi, lo) shifted right by r (arithmetic; 1 <= r <= 63), low 64 bits.
+__host__ __device__ __forceinline__ long long shr128_lo(I128 x, int r) {
+  return (long long)((x.lo >> r) | ((unsigned long long)x.hi << (64 - r)));
+}
+// (a + ib)(c + id) 2^e for fixed-point factors |a|, |b|, |c|, |d| < 2^61: exact
+// 128-bit products (|re|, |im| < 2^123), then one truncation to the normal form.
+__host__ __device__ __forceinline__ BFloat bf_pair(long long a, long long b, long long c, long long d, int e) {
+  const I128 re = sub128(mul_s64(a, c), mul_s64(b, d));
+  const I128 im = add128(mul_s64(a, d), mul_s64(b, c));
+  BFloat z;
+  const unsigned mt = mag_hi32(re.hi) | mag_hi32(im.hi);
+  if (mt != 0) {
+    // |value| >= 2^96 (the usual case): the leading bit (127 - clz) lies in the top
+    // word, below bit 123, so the shift r = 66 - clz is 32 + rp with rp in [3, 29]
+    // and the result is two 32-bit funnel shifts per component.
+    const int rp = 34 - clz_u32(mt);
+    z.re = join32(fshr32(lo32(re.hi), hi32(re.hi), rp), fshr32(hi32((long long)re.lo), lo32(re.hi), rp));
+    z.im = join32(fshr32(lo32(im.hi), hi32(im.hi), rp), fshr32(hi32((long long)im.lo), lo32(im.hi), rp));
+    z.e = e + 32 + rp;
+    return z;
+  }
+  const long long sr = re.hi >> 63, si = im.hi >> 63;
+  const unsigned long long mh = (unsigned long long)(re.hi ^ sr) | (unsigned long long)(im.hi ^ si);
+  if (mh != 0) {
+    const int r = 66 - clz_u64(mh);  // the leading bit (127 - clz) goes to bit 61: r in [3, 61]
+    z.re = shr128_lo(re, r);
+    z.im = shr128_lo(im, r);
+    z.e = e + r;
+    return z;
+  }
+  // Both high halves are sign bits: |re|, |im| < 2^64 (about 2^-58 of the largest products).
+  const unsigned long long ml = (re.lo ^ (unsigned long long)sr) | (im.lo ^ (unsigned long long)si);
+  const int r = 2 - clz_u64(ml);  // in [-62, 2]
+  if (r > 0) {
+    z.re = shr128_lo(re, r);
+    z.im = shr128_lo(im, r);
+  } else {  // |value| < 2^62: the low half is the value
+    z.re = (long long)(re.lo << -r);
+    z.im = (long long)(im.lo << -r);
+  }
+  z.e = e + r;
+  return z;
+}
+// x 2^e rounded to the nearest double (ties away from zero); integer instructions
+// except outside FP64's normal range (rare), which goes through ldexp.
+__host__ __device__ __forceinline__ double bf_to_double(long long x, int e) {
+  const unsigned long long sgn = (unsigned long long)(x >> 63);
+  const unsigned long long ax = ((unsigned long long)x ^ sgn) - sgn;
+  const int lz = clz_u64(ax);
+  const unsigned long long y = ax << (lz & 63);
+  const unsigned long long yr = y + 0x400ull;
+  const unsigned long long carry = (yr < y) ? 1ull : 0ull;
+  const unsigned long long mant = (yr >> 11) & 0xFFFFFFFFFFFFFull;
+  const int be = e + 1086 - lz + (int)carry;
+  if (be >= 1 && be <= 2046 && ax != 0) return bits_to_double((sgn << 63) | ((unsigned long long)be << 52) | mant);
+  return ax ? ldexp((double)x, e) : 0.0;
+}
+// Product of the fixed-point factors [LO, HI) (unit 2^efx each) as a balanced
+// tree: exact pairs at the leaves, bf_mul above them.
+template <int LO, int HI, int NF>
+__host__ __device__ __forceinline__ BFloat bf_product(const long long (&sr)[NF], const long long (&si)[NF], int efx) {
+  if constexpr (HI - LO == 1) {
+    return bf_norm(sr[LO], si[LO], efx);
+  } else if constexpr (HI - LO == 2) {
+    return bf_pair(sr[LO], si[LO], sr[LO + 1], si[LO + 1], 2 * efx);
+  } else {
+    constexpr int MID = LO + 2 * ((HI - LO + 2) / 4);
+    return bf_mul(bf_product<LO, MID, NF>(sr, si, efx), bf_product<MID, HI, NF>(sr, si, efx));
+  }
+}
+
+// acc += sign * prod_f s_f with the first K factors multiplied in block floating
+// point on the integer pipe and the others on the FP64 pipe (the last one fused
+// into the accumulation).  K = NF leaves 2 FP64 adds per code.
+template <int NF, int K>
+__device__ __forceinline__ void accumulate_product_bf(const long long (&sr)[NF], const long long (&si)[NF],
+                                                      int bias_exp, uint32_t neg_mask, double& ar, double& ai) {
+  static_assert(K >= 2 && K <= NF, "block-float factors");
+  const int efx = bias_exp - 1086;  // a factor's unit: 2^-fx
+  const BFloat p = bf_product<0, K, NF>(sr, si, efx);
+  double pr = bf_to_double(p.re, p.e), pi = bf_to_double(p.im, p.e);
+  if constexpr (K == NF) {
+    ar += xor_sign(pr, neg_mask);
+    ai += xor_sign(pi, neg_mask);
+  } else {
+#pragma unroll
+    for (int f = K; f < NF - 1; ++f) {
+      const double br = fx_to_double(sr[f], bias_exp);
+      const double bi = fx_to_double(si[f], bias_exp);
+      const double t_re = fma(pr, br, -(pi * bi));
+      const double t_im = fma(pr, bi, pi * br);
+      pr = t_re;
+      pi = t_im;
+    }
+    pr = xor_sign(pr, neg_mask);
+    pi = xor_sign(pi, neg_mask);
+    const double br = fx_to_double(sr[NF - 1], bias_exp);
+    const double bi = fx_to_double(si[NF - 1], bias_exp);
+    ar = fma(pr, br, ar);
+    ar = fma(-pi, bi, ar);
+    ai = fma(pr, bi, ai);
+    ai = fma(pi, br, ai);
+  }
 }
 
 // acc += sign * prod_f s_f.  With PAIRS = 2, factors 0, 1 (and 2, 3 from NF = 5 on)

@@ -6,9 +6,23 @@
 
 namespace boss {
 
+// Factors of a single permanent's product chain multiplied in block floating
+// point on the integer pipe (0: all on the FP64 pipe, accumulate_product<NF>).
+template <int NF>
+constexpr int kPermBF = NF >= 6 ? NF - 4 : (NF >= 2 ? NF : 0);
+
+template <int NF>
+__device__ __forceinline__ void perm_product(const long long (&sr)[NF], const long long (&si)[NF], int bias_exp,
+                                             uint32_t neg_mask, double& ar, double& ai) {
+  if constexpr (kPermBF<NF> >= 2)
+    accumulate_product_bf<NF, kPermBF<NF>>(sr, si, bias_exp, neg_mask, ar, ai);
+  else
+    accumulate_product<NF>(sr, si, bias_exp, neg_mask, ar, ai);
+}
+
 // One permanent per sweep problem; every thread writes one complex partial.
 template <int NF>
-__global__ void __launch_bounds__(128) perm_sweep_kernel(const SweepProblem* __restrict__ probs, int n_probs,
+__global__ void __launch_bounds__(128, 3) perm_sweep_kernel(const SweepProblem* __restrict__ probs, int n_probs,
                                                          const longlong2* __restrict__ pool, int64_t total_threads,
                                                          double2* __restrict__ partials) {
   const int64_t gt = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -29,7 +43,7 @@ __global__ void __launch_bounds__(128) perm_sweep_kernel(const SweepProblem* __r
     double w;
     decode_code<NF>(P, D, base, (uint64_t)a, sr, si, g, parity, w);
     double ar = 0.0, ai = 0.0;
-    accumulate_product<NF>(sr, si, bias, parity << 31, ar, ai);
+    perm_product<NF>(sr, si, bias, parity << 31, ar, ai);
     const uint64_t end = (uint64_t)(a + len);
     for (uint64_t t = (uint64_t)a + 1; t < end; ++t) {
       const int i = __ffsll((long long)t) - 1;
@@ -45,7 +59,7 @@ __global__ void __launch_bounds__(128) perm_sweep_kernel(const SweepProblem* __r
         ai = 0.0;
         decode_code<NF>(P, D, base, t, sr, si, g, parity, w);
       }
-      accumulate_product<NF>(sr, si, bias, parity << 31, ar, ai);
+      perm_product<NF>(sr, si, bias, parity << 31, ar, ai);
     }
     tr = fma(w, ar, tr);
     ti = fma(w, ai, ti);
@@ -83,6 +97,26 @@ __device__ __forceinline__ void settle_minors(const SweepProblem& P, double2* M,
   }
 }
 
+// Factors of the all-minors product chain multiplied in block floating point on
+// the integer pipe (0: exact pairs then FP64, accumulate_product<NF, 2>).
+template <int NF>
+constexpr int kMinorsBF = NF >= 2 ? (NF < 8 ? NF : 8) : 0;
+
+// Blocks of 128 threads per SM the all-minors kernel is compiled for: 4 (128
+// registers, a few spilled words at NF 11..16) up to NF = 16, where the fourth
+// block's warps hide more latency than the spills cost; 3 above.
+template <int NF>
+constexpr int kMinorsMinBlocks = NF <= 16 ? 4 : 3;
+
+template <int NF>
+__device__ __forceinline__ void minors_product(const long long (&sr)[NF], const long long (&si)[NF], int bias_exp,
+                                               uint32_t neg_mask, double& ar, double& ai) {
+  if constexpr (kMinorsBF<NF> >= 2)
+    accumulate_product_bf<NF, kMinorsBF<NF>>(sr, si, bias_exp, neg_mask, ar, ai);
+  else
+    accumulate_product<NF, 2>(sr, si, bias_exp, neg_mask, ar, ai);
+}
+
 // All-minors sweep (C&C-B), in Glynn form.  theboss sums each minor over the
 // Ryser codes with r_i = 0 (bs_cc_ryser_submatrices_permanent_calculator.py:96-119).
 // Here a row of variables x is appended: perm([U[T, S]; x]) = sum_i x_i S_i minor_i,
@@ -117,7 +151,7 @@ __device__ __forceinline__ void minors_walk(const SweepProblem& P, const longlon
     double w;
     decode_code<NF>(P, D, base, (uint64_t)a, sr, si, g, parity, w);
     double Rr = 0.0, Ri = 0.0;
-    accumulate_product<NF, 2>(sr, si, bias, parity << 31, Rr, Ri);
+    minors_product<NF>(sr, si, bias, parity << 31, Rr, Ri);
     const uint64_t end = (uint64_t)(a + len);
     for (uint64_t t = (uint64_t)a + 1; t < end; ++t) {
       const int i = __ffsll((long long)t) - 1;
@@ -149,7 +183,7 @@ __device__ __forceinline__ void minors_walk(const SweepProblem& P, const longlon
           decode_code<NF>(P, D, base, t, sr, si, g, parity, w);
         }
       }
-      accumulate_product<NF, 2>(sr, si, bias, parity << 31, Rr, Ri);
+      minors_product<NF>(sr, si, bias, parity << 31, Rr, Ri);
     }
     settle_minors<STRIDE>(P, M, Rr, Ri, w, g, t_seg);
   }
@@ -158,7 +192,7 @@ __device__ __forceinline__ void minors_walk(const SweepProblem& P, const longlon
 // One launch over many all-minors sweeps (128 threads per block); every thread
 // writes nd + held complex partials, or its group of `group` threads writes their sum.
 template <int NF>
-__global__ void __launch_bounds__(128, 3) minors_sweep_kernel(const SweepProblem* __restrict__ probs, int n_probs,
+__global__ void __launch_bounds__(128, kMinorsMinBlocks<NF>) minors_sweep_kernel(const SweepProblem* __restrict__ probs, int n_probs,
                                                            const longlong2* __restrict__ pool, int64_t total_threads,
                                                            double2* __restrict__ partials, int64_t uniform_threads) {
   extern __shared__ double2 minors_smem[];
