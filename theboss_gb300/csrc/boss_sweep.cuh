@@ -16,16 +16,17 @@
 //     D = -2U, sign (-1)^|r|, scale 2^-n.
 // The binomial weight follows bs_permanent_calculator_base.py:151-164.
 //
-// GB300 mapping.  The FP64 pipe issues 2 lanes/clk/SM, 1/64 of FP32, so only the
-// products use it:
+// GB300 mapping.  The FP64 pipe issues 2 lanes/clk/SM, 1/64 of FP32, so only
+// products and sums of products use it, and the integer pipes take what they can:
 //   * the row sums are exact 64-bit fixed-point integers (value = int * 2^-fx),
 //     updated with integer adds and converted to FP64 with integer instructions
 //     (fx_to_double), so the 2 adds per factor and code leave the FP64 pipe and
 //     the sums never drift;
+//   * the first factors of every product are multiplied in block floating point
+//     on the integer pipe (62-bit mantissas, accumulate_product_bf), the rest on
+//     the FP64 pipe, 4 instructions per factor (accumulate_product);
 //   * the last multiply of every product is fused into the accumulation (4 DFMA);
 //   * sign flips are integer XORs on the sign bit.
-// That leaves 4*(nf - 1) FP64 instructions per code, less 4 for every pair of
-// factors multiplied exactly on the integer pipe (accumulate_product).
 //
 // Work split: the codes of a sweep are cut into one contiguous range per thread
 // (lengths differ by at most one), each thread decodes its start code in closed
@@ -199,12 +200,7 @@ __device__ __forceinline__ void flip_binary(const longlong2* __restrict__ D, int
 }
 
 // ---------------------------------------------------------------------------
-// Exact products of two fixed-point factors on the integer pipe.  GB300 issues
-// 64-bit integer multiplies far faster than FP64, so the first two pairs of
-// factors of every product are multiplied exactly: (a + ib)(c + id) with
-// |a|, |b|, |c|, |d| < 2^61 in 128-bit two's complement (|re|, |im| < 2^123),
-// each component rounded once to a double (an FP64 complex product rounds
-// twice per component).
+// 128-bit integer helpers for the exact products of two fixed-point factors.
 // ---------------------------------------------------------------------------
 struct I128 {
   unsigned long long lo;
@@ -243,51 +239,6 @@ __host__ __device__ __forceinline__ I128 sub128(I128 x, I128 y) {
   r.hi = x.hi - y.hi - (x.lo < y.lo ? 1 : 0);
   return r;
 }
-// x 2^e rounded to the nearest double (ties to even), for |x| < 2^126 (the
-// sweeps' factor products: fixed-point units of 2^-fx with |factor| < 2^61).  A
-// result outside the normal range is scaled by ldexp instead.
-__device__ __forceinline__ double i128_to_double(I128 x, int e) {
-  const bool neg = x.hi < 0;
-  unsigned long long mh = (unsigned long long)x.hi, ml = x.lo;
-  if (neg) {
-    ml = ~ml + 1ull;
-    mh = ~mh + (ml == 0 ? 1ull : 0ull);
-  }
-  if ((mh | ml) == 0) return 0.0;
-  const int lz = mh ? __clzll((long long)mh) : 64 + __clzll((long long)ml);
-  unsigned long long th, tl;  // shifted left by lz: the leading bit at bit 127
-  if (lz >= 64) {
-    th = ml << (lz - 64);
-    tl = 0;
-  } else if (lz == 0) {
-    th = mh;
-    tl = ml;
-  } else {
-    th = (mh << lz) | (ml >> (64 - lz));
-    tl = ml << lz;
-  }
-  unsigned long long m = th >> 11;  // 53 bits
-  const unsigned long long rem = th & 0x7FFull;
-  if (rem > 0x400ull || (rem == 0x400ull && (tl != 0 || (m & 1ull)))) m += 1ull;
-  int ex = 127 - lz;  // |x| = m 2^(ex - 52)
-  if (m >> 53) {
-    m >>= 1;
-    ++ex;
-  }
-  const int be = ex + e + 1023;
-  const unsigned long long sign = neg ? (1ull << 63) : 0ull;
-  if (be >= 1 && be <= 2046)
-    return __longlong_as_double((long long)(sign | ((unsigned long long)be << 52) | (m & 0xFFFFFFFFFFFFFull)));
-  return ldexp(__longlong_as_double((long long)(sign | ((unsigned long long)(ex + 1023) << 52) | (m & 0xFFFFFFFFFFFFFull))),
-               e);
-}
-// (a + ib)(c + id) 2^e, each component exact and rounded once.
-__device__ __forceinline__ void cmul_fx_exact(long long a, long long b, long long c, long long d, int e, double& re,
-                                              double& im) {
-  re = i128_to_double(sub128(mul_s64(a, c), mul_s64(b, d)), e);
-  im = i128_to_double(add128(mul_s64(a, d), mul_s64(b, c)), e);
-}
-
 // ---------------------------------------------------------------------------
 // Block floating point on the integer pipe.  A complex value is (re + i im) 2^e,
 // two 64-bit integers sharing one exponent, normalised so that the larger
@@ -481,15 +432,10 @@ __device__ __forceinline__ void accumulate_product_bf(const long long (&sr)[NF],
   }
 }
 
-// acc += sign * prod_f s_f.  With PAIRS = 2, factors 0, 1 (and 2, 3 from NF = 5 on)
-// are multiplied exactly on the integer pipe; the rest are complex products on
-// the FP64 pipe (4 instructions each), the last fused with the accumulation (4
-// DFMA): per code 4 (nf - 1) FP64 instructions less 4 per exact pair.  The
-// all-minors sweeps use it (the sampler's step, 10^4 samples at n = 20: sweeps
-// 3.107 -> 2.946 ms with one exact pair, 2.919 ms with two, the same samples);
-// the single-permanent sweeps do not (PAIRS = 0): at nf >= 24 their registers
-// are full, and the pairs cost 1 % at n = 24 and 9 % at n = 28.
-template <int NF, int PAIRS = 0>
+// acc += sign * prod_f s_f on the FP64 pipe: complex products (4 instructions
+// each), the last fused with the accumulation (4 DFMA): 4 (nf - 1) FP64
+// instructions per code.
+template <int NF>
 __device__ __forceinline__ void accumulate_product(const long long (&sr)[NF], const long long (&si)[NF], int bias_exp,
                                                    uint32_t neg_mask, double& ar, double& ai) {
   if (NF == 1) {
@@ -497,25 +443,9 @@ __device__ __forceinline__ void accumulate_product(const long long (&sr)[NF], co
     ai += xor_sign(fx_to_double(si[0], bias_exp), neg_mask);
     return;
   }
-  double pr, pi;
-  constexpr int f0 = (PAIRS >= 2 && NF >= 5) ? 4 : ((PAIRS >= 1 && NF >= 3) ? 2 : 1);  // first factor for the FP64 pipe
-  const int e2 = 2 * (bias_exp - 1086);  // a pair's unit: 2^(-2 fx)
-  if constexpr (f0 == 4) {
-    double qr, qi;
-    cmul_fx_exact(sr[0], si[0], sr[1], si[1], e2, pr, pi);
-    cmul_fx_exact(sr[2], si[2], sr[3], si[3], e2, qr, qi);
-    const double t_re = fma(pr, qr, -(pi * qi));
-    const double t_im = fma(pr, qi, pi * qr);
-    pr = t_re;
-    pi = t_im;
-  } else if constexpr (f0 == 2) {
-    cmul_fx_exact(sr[0], si[0], sr[1], si[1], e2, pr, pi);
-  } else {
-    pr = fx_to_double(sr[0], bias_exp);
-    pi = fx_to_double(si[0], bias_exp);
-  }
+  double pr = fx_to_double(sr[0], bias_exp), pi = fx_to_double(si[0], bias_exp);
 #pragma unroll
-  for (int f = f0; f < NF - 1; ++f) {
+  for (int f = 1; f < NF - 1; ++f) {
     const double br = fx_to_double(sr[f], bias_exp);
     const double bi = fx_to_double(si[f], bias_exp);
     const double t_re = fma(pr, br, -(pi * bi));

@@ -98,7 +98,7 @@ __device__ __forceinline__ void settle_minors(const SweepProblem& P, double2* M,
 }
 
 // Factors of the all-minors product chain multiplied in block floating point on
-// the integer pipe (0: exact pairs then FP64, accumulate_product<NF, 2>).
+// the integer pipe (0: all on the FP64 pipe, accumulate_product<NF>).
 template <int NF>
 constexpr int kMinorsBF = NF >= 2 ? (NF < 8 ? NF : 8) : 0;
 
@@ -114,7 +114,7 @@ __device__ __forceinline__ void minors_product(const long long (&sr)[NF], const 
   if constexpr (kMinorsBF<NF> >= 2)
     accumulate_product_bf<NF, kMinorsBF<NF>>(sr, si, bias_exp, neg_mask, ar, ai);
   else
-    accumulate_product<NF, 2>(sr, si, bias_exp, neg_mask, ar, ai);
+    accumulate_product<NF>(sr, si, bias_exp, neg_mask, ar, ai);
 }
 
 // All-minors sweep (C&C-B), in Glynn form.  theboss sums each minor over the
