@@ -533,8 +533,9 @@ def roofline(b, sweep_s, achieved, peak, peak32, traffic):
     common = {"traffic": traffic, "sweep_ms_per_step": sweep_s * 1e3, "flops_per_step": b["sweep_flops"],
               "flops_note": "9k - 12 flops per Guan code at level k over the codes the Glynn-form all-minors "
                             "sweeps walk (half of theboss's Ryser-form codes for single photons); of these "
-                            "the row-sum updates and the products of the first 8 factors (block floating "
-                            "point, 62-bit mantissas) run on the integer pipe, the rest on the FP64 pipe, so "
+                            "the row-sum updates and the products of the first 8 factors (nf - 8 above 16 "
+                            "factors; block floating point, 62-bit mantissas) run on the integer pipe, the "
+                            "rest on the FP64 pipe, so "
                             "the FP64-equivalent rate can exceed the FP64 pipe's peak; ryser_form_* count "
                             "theboss's codes",
               "ryser_form_flops_per_step": b["ref_flops"],

@@ -98,9 +98,10 @@ __device__ __forceinline__ void settle_minors(const SweepProblem& P, double2* M,
 }
 
 // Factors of the all-minors product chain multiplied in block floating point on
-// the integer pipe (0: all on the FP64 pipe, accumulate_product<NF>).
+// the integer pipe (0: all on the FP64 pipe, accumulate_product<NF>): 8 up to 16
+// factors (4 blocks per SM), nf - 8 above (3 blocks, more registers per thread).
 template <int NF>
-constexpr int kMinorsBF = NF >= 2 ? (NF < 8 ? NF : 8) : 0;
+constexpr int kMinorsBF = NF >= 2 ? (NF < 8 ? NF : (NF <= 16 ? 8 : NF - 8)) : 0;
 
 // Blocks of 128 threads per SM the all-minors kernel is compiled for: 4 (128
 // registers, a few spilled words at NF 11..16) up to NF = 16, where the fourth
