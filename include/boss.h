@@ -178,7 +178,9 @@ BOSS_API int boss_gccb_sample(const double* matrix, int32_t m, const int32_t* in
 // pairs (two FP32 values, about 47 significant bits) on the FP32 pipe, for
 // sweeps of at most 24 product-side particles (larger ones stay FP64); -1: query
 // only.  *previous (if not null) receives the mode in force before the call.  Row
-// sums are exact 64-bit fixed point in both.
+// sums are exact 64-bit fixed point in both; in mode 1 the first factors of every
+// product are multiplied in block floating point on the integer pipe (62-bit
+// mantissas, each product within 2^-56.5 of its magnitude, rounded once to FP64).
 BOSS_API int boss_minors_arithmetic(int32_t mode, int32_t* previous);
 
 // The same choice for the single-permanent sweeps of boss_perm_batch and
@@ -186,7 +188,9 @@ BOSS_API int boss_minors_arithmetic(int32_t mode, int32_t* previous);
 // compute_permanent, bs_permanent_calculator_base.py:166-198): 1 FP64 (default),
 // 0 float pairs (up to 32 product-side particles, Glynn-kind sweeps: Glynn,
 // Chin-Huh, Classic), -1 query.  Ryser-form sweeps, whose alternating sum cancels
-// far more, the allocation-free entry point and the gradients always use FP64.
+// far more, the allocation-free entry point and the gradients always use FP64 (in
+// the FP64 single-permanent sweeps all but the last 4 factors of every product are
+// multiplied in block floating point on the integer pipe, as above).
 BOSS_API int boss_perm_arithmetic(int32_t mode, int32_t* previous);
 
 /*
