@@ -154,6 +154,7 @@ def as_states(states, length: int) -> np.ndarray:
 
 def perm_batch(U: np.ndarray, S: np.ndarray, T: np.ndarray, variant: int) -> np.ndarray:
     """Permanents of U[T_k, S_k]; S, T int32 (count x len).  Returns complex128 (count,)."""
+    U = as_matrix(U)
     L = load()
     count, n = S.shape
     out = np.empty(count, dtype=np.complex128)
@@ -166,6 +167,7 @@ def perm_batch(U: np.ndarray, S: np.ndarray, T: np.ndarray, variant: int) -> np.
 
 def perm_grad_batch(U: np.ndarray, S: np.ndarray, T: np.ndarray):
     """Permanents of U[T_k, S_k] and d perm_k / d U[j][i] (count x len x len)."""
+    U = as_matrix(U)
     L = load()
     count, n = S.shape
     perms = np.empty(count, dtype=np.complex128)
@@ -179,6 +181,7 @@ def perm_grad_batch(U: np.ndarray, S: np.ndarray, T: np.ndarray):
 
 def submatrices_batch(U: np.ndarray, S: np.ndarray, T: np.ndarray, variant: int) -> np.ndarray:
     """All-minors permanents; returns complex128 (count x len)."""
+    U = as_matrix(U)
     L = load()
     count, n = S.shape
     out = np.empty((count, n), dtype=np.complex128)
@@ -194,6 +197,7 @@ def perm_batch_noalloc(U: np.ndarray, S: np.ndarray, T: np.ndarray, variant: int
     """Queues the permanents of U[T_k, S_k] into a caller-owned device buffer of
     count complex128 without any GPU allocation (boss_perm_batch_noalloc).  The
     caller synchronises the stream before reading the buffer."""
+    U = as_matrix(U)
     L = load()
     count, n = S.shape
     check(L.boss_perm_batch_noalloc(_dp(U.view(np.float64)), U.shape[0], _ip(S), _ip(T), n, count, variant,
@@ -246,6 +250,7 @@ def count_outcomes(samples, outcomes, m: int) -> np.ndarray:
 def gccb_sample_slice(U: np.ndarray, input_state, weights, n_samples: int, first: int, count: int) -> np.ndarray:
     """Samples [first, first + count) of the stream of n_samples C&C-B samples;
     numpy's global RandomState advances over the whole stream.  int32 (count x m)."""
+    U = as_matrix(U)
     L = load()
     inp = np.ascontiguousarray(input_state, dtype=np.int32)
     m = U.shape[0]
@@ -374,6 +379,7 @@ def gccb_autotune(U: np.ndarray, input_state, weights, n_samples: int, reps: int
     """Tunes the sampler's launch shapes on the workload of gccb_sample(U,
     input_state, weights, n_samples) drawn from numpy's current global state
     (which is not advanced); boss_gccb_autotune."""
+    U = as_matrix(U)
     L = load()
     inp = np.ascontiguousarray(input_state, dtype=np.int32)
     m = U.shape[0]
@@ -452,6 +458,7 @@ def gccb_predraw(input_state, weights, n_samples: int):
 def gccb_sample(U: np.ndarray, input_state, weights, n_samples: int) -> np.ndarray:
     """n_samples C&C-B samples on the GPU; consumes numpy's global RandomState like
     theboss does.  Returns int32 (n_samples x m)."""
+    U = as_matrix(U)
     L = load()
     inp = np.ascontiguousarray(input_state, dtype=np.int32)
     m = U.shape[0]
@@ -473,6 +480,7 @@ def gccb_bench(U: np.ndarray, input_state, weights, n_samples: int, warmup: int,
                flush_bytes: int = 256 << 20):
     """Runs the captured sampler graph warmup + steps times on resident inputs.
     Returns dict(step_ms, sweep_ms, sweep_flops, h2d_bytes, d2h_bytes, kernels, sweeps, levels, samples)."""
+    U = as_matrix(U)
     L = load()
     inp = np.ascontiguousarray(input_state, dtype=np.int32)
     m = U.shape[0]
@@ -495,6 +503,7 @@ def perm_bench(U: np.ndarray, S: np.ndarray, T: np.ndarray, variant: int, warmup
                flush_bytes: int = 256 << 20):
     """Device-timed sweeps of a batch of permanents sharing one product size.
     Returns dict(sweep_ms, codes, flops, threads, nf, ff_inst, results)."""
+    U = as_matrix(U)
     L = load()
     count, n = S.shape
     sweep_ms = np.zeros(steps)
