@@ -308,7 +308,7 @@ def single_permanents(peak_tflops, seed, peak32=None):
         ms = float(np.mean(b["sweep_ms"]))
         tf = b["flops"] / (ms / 1e3) / 1e12
         res[str(n)] = {"perms_per_s": 64 / (ms / 1e3), "ms_per_64": ms, "codes": b["codes"], "arithmetic": "fp64",
-                       "arithmetic_note": "the first n - 4 factors of every product in block floating point on "
+                       "arithmetic_note": "the first n - 8 factors of every product in block floating point on "
                                           "the integer pipe; frac_of_fp64_peak counts FP64-equivalent flops",
                        "achieved_tflops": tf, "frac_of_fp64_peak": tf / peak_tflops, **errors(n, U, S, T, b["results"])}
         prev = _native.perm_arithmetic(_native.FLOAT_PAIRS)

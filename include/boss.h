@@ -189,7 +189,7 @@ BOSS_API int boss_minors_arithmetic(int32_t mode, int32_t* previous);
 // 0 float pairs (up to 32 product-side particles, Glynn-kind sweeps: Glynn,
 // Chin-Huh, Classic), -1 query.  Ryser-form sweeps, whose alternating sum cancels
 // far more, the allocation-free entry point and the gradients always use FP64 (in
-// the FP64 single-permanent sweeps all but the last 4 factors of every product are
+// the FP64 single-permanent sweeps all but the last 8 factors of every product are
 // multiplied in block floating point on the integer pipe, as above).
 BOSS_API int boss_perm_arithmetic(int32_t mode, int32_t* previous);
 

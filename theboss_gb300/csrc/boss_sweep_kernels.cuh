@@ -9,7 +9,7 @@ namespace boss {
 // Factors of a single permanent's product chain multiplied in block floating
 // point on the integer pipe (0: all on the FP64 pipe, accumulate_product<NF>).
 template <int NF>
-constexpr int kPermBF = NF >= 6 ? NF - 4 : (NF >= 2 ? NF : 0);
+constexpr int kPermBF = NF >= 10 ? NF - 8 : (NF >= 2 ? NF : 0);
 
 template <int NF>
 __device__ __forceinline__ void perm_product(const long long (&sr)[NF], const long long (&si)[NF], int bias_exp,
