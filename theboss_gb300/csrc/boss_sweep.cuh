@@ -351,7 +351,7 @@ __host__ __device__ __forceinline__ BFloat bf_pair(long long a, long long b, lon
   const long long sr = re.hi >> 63, si = im.hi >> 63;
   const unsigned long long mh = (unsigned long long)(re.hi ^ sr) | (unsigned long long)(im.hi ^ si);
   if (mh != 0) {
-    const int r = 66 - clz_u64(mh);  // the leading bit (127 - clz) goes to bit 61: r in [3, 61]
+    const int r = 66 - clz_u64(mh);  // the leading bit (127 - clz, below bit 96 here) goes to bit 61: r in [3, 34]
     z.re = shr128_lo(re, r);
     z.im = shr128_lo(im, r);
     z.e = e + r;
