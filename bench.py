@@ -197,9 +197,7 @@ def cpu_baseline(U, inp, w, seed, budget_s=10.0, gpu_samples=None):
     the oracle's stream for the GPU's: they are compared (the parity record)."""
     from oracle import oracle as O
 
-    threads = os.cpu_count() or 1
-    os.environ.setdefault("OMP_NUM_THREADS", str(threads))
-    O.lib()
+    cores = O.set_threads(os.cpu_count() or 1)
 
     def run(n):
         np.random.seed(seed)
@@ -214,7 +212,7 @@ def cpu_baseline(U, inp, w, seed, budget_s=10.0, gpu_samples=None):
     if gpu_samples is not None:
         n = max(n, len(gpu_samples))
     dt, (L, A, Uu, out) = run(n)
-    res = {"value": n / dt, "unit": "samples/s", "cores": int(os.environ["OMP_NUM_THREADS"]), "kind": "port",
+    res = {"value": n / dt, "unit": "samples/s", "cores": cores, "kind": "port",
            "sample": f"{n} samples of the workload (same seed and matrix), C restatement of theboss's "
                      f"GCC-B sampler, OpenMP over samples, {dt:.1f} s"}
     parity = None
@@ -671,9 +669,7 @@ def run_reference(args, rank):
     from oracle import oracle as O
 
     U, inp, w = workload(args.seed)
-    threads = os.cpu_count() or 1
-    os.environ.setdefault("OMP_NUM_THREADS", str(threads))
-    O.lib()
+    cores = O.set_threads(os.cpu_count() or 1)  # all host threads, whatever OMP_NUM_THREADS torchrun set
     # calibrate a per-step sample of about 3 s
     np.random.seed(args.seed)
     L, A, Uu = O.predraw_gccb(list(inp), 200, w)
@@ -693,11 +689,11 @@ def run_reference(args, rank):
     value = n * len(times) / sum(times)
     sample = (f"{n} of the {args.samples} samples per step (same seed and matrix), C restatement of theboss's "
               f"GCC-B sampler, OpenMP over samples")
-    line = {"metric": METRIC, "value": value, "unit": "samples/s", "impl": "reference", "n_gpus": 1,
+    line = {"metric": METRIC, "value": value, "unit": "samples/s", "impl": "reference", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * args.samples / value,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (seeded Haar unitary)", "config": config(args),
-            "cpu_baseline": {"value": value, "unit": "samples/s", "cores": int(os.environ["OMP_NUM_THREADS"]),
+            "cpu_baseline": {"value": value, "unit": "samples/s", "cores": cores,
                              "kind": "port", "sample": sample},
             "e2e": {"value": value, "unit": "samples/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)

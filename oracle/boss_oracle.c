@@ -24,6 +24,9 @@
 #include <stdint.h>
 #include <stdlib.h>
 #include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
 
 #define ORACLE_MAX_MODES 256
 #define ORACLE_MAX_PHOTONS 64
@@ -413,6 +416,18 @@ int oracle_gccb_step(const double* U, int m, const int* S, const int* T, double 
   for (int j = 0; j < m; ++j) { cdf[j] /= last; if (cdf[j] <= u) idx = j + 1; }
   if (idx > m - 1) idx = m - 1;
   return idx;
+}
+
+/* Threads of the OpenMP loops below (n >= 1), whatever OMP_NUM_THREADS the process
+ * inherited; returns the count now in force (1 without OpenMP). */
+int oracle_set_threads(int n) {
+#ifdef _OPENMP
+  if (n >= 1) omp_set_num_threads(n);
+  return omp_get_max_threads();
+#else
+  (void)n;
+  return 1;
+#endif
 }
 
 /* A whole batch of GCC-B samples from a pre-drawn random stream.  For sample s,

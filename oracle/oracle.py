@@ -75,8 +75,16 @@ def lib():
         L.oracle_perm_batch.argtypes = [dp, ctypes.c_int, ip, ip, ctypes.c_int, ctypes.c_int, ctypes.c_int, dp]
         L.oracle_guan_sequence.restype = ctypes.c_long
         L.oracle_guan_sequence.argtypes = [ip, ctypes.c_int, ip, ip, ctypes.c_long]
+        L.oracle_set_threads.restype = ctypes.c_int
+        L.oracle_set_threads.argtypes = [ctypes.c_int]
         _lib = L
     return _lib
+
+
+def set_threads(n: int) -> int:
+    """Threads of the OpenMP sample loop (gccb_run), overriding an inherited
+    OMP_NUM_THREADS (torchrun sets 1); returns the count in force."""
+    return int(lib().oracle_set_threads(int(n)))
 
 
 def _mat(U) -> np.ndarray:
